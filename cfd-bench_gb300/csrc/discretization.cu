@@ -1,0 +1,652 @@
+// FP64 discretization kernels of the NuSiF time step and the reference
+// entry points that launch them (src/discretization.h:34-41).
+//
+// Layout in HBM: each field is one cudaMalloc'd FP64 array in the reference
+// layout ((imax+2)(jmax+2)(kmax+2) doubles, i fastest, one ghost layer,
+// src/util.h:19-34). Threads map x -> i so every warp touches consecutive
+// doubles. All arithmetic is FP64 (the reference computes in double).
+#include <cfloat>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include "nusif_internal.h"
+#include "reduce.cuh"
+
+namespace nusif {
+
+DiscState *disc_state_create(const Discretization *d);
+void disc_state_erase(const Discretization *d);
+
+namespace {
+
+constexpr int kBlock = 256;
+
+inline int sm_count()
+{
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+// ---- fill (initDiscretization, discretization.c:96-105) ----
+__global__ void k_fill(double *a, int64_t n, double value)
+{
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x)
+    a[q] = value;
+}
+
+// ---- max |u|, |v|, |w| over the padded arrays (discretization.c:391-401) ----
+// Seeded with DBL_MIN like the reference. Block maxima go to partials; the
+// last block folds them.
+__global__ void __launch_bounds__(kBlock) k_max3(const double *__restrict__ u,
+    const double *__restrict__ v, const double *__restrict__ w, int64_t n,
+    double *__restrict__ partials, unsigned *ticket, double *__restrict__ out3)
+{
+  double mu = DBL_MIN, mv = DBL_MIN, mw = DBL_MIN;
+  const int64_t stride = (int64_t)gridDim.x * kBlock;
+  // pairs of doubles (cudaMalloc bases are 256-byte aligned)
+  const int64_t npair = n / 2;
+  const double2 *u2 = reinterpret_cast<const double2 *>(u);
+  const double2 *v2 = reinterpret_cast<const double2 *>(v);
+  const double2 *w2 = reinterpret_cast<const double2 *>(w);
+  for (int64_t q = blockIdx.x * (int64_t)kBlock + threadIdx.x; q < npair; q += stride) {
+    double2 a = __ldg(u2 + q), b = __ldg(v2 + q), c = __ldg(w2 + q);
+    mu = fmax(mu, fmax(fabs(a.x), fabs(a.y)));
+    mv = fmax(mv, fmax(fabs(b.x), fabs(b.y)));
+    mw = fmax(mw, fmax(fabs(c.x), fabs(c.y)));
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    mu = fmax(mu, fabs(u[n - 1]));
+    mv = fmax(mv, fabs(v[n - 1]));
+    mw = fmax(mw, fabs(w[n - 1]));
+  }
+  __shared__ double sm[3][kBlock / 32];
+  mu = block_reduce_max<kBlock>(mu, sm[0]);
+  mv = block_reduce_max<kBlock>(mv, sm[1]);
+  mw = block_reduce_max<kBlock>(mw, sm[2]);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    partials[3 * blockIdx.x + 0] = mu;
+    partials[3 * blockIdx.x + 1] = mv;
+    partials[3 * blockIdx.x + 2] = mw;
+    last = ticket_is_last(ticket);
+  }
+  __syncthreads();
+  if (!last) return;
+  double a = DBL_MIN, b = DBL_MIN, c = DBL_MIN;
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += kBlock) {
+    a = fmax(a, ld_cg(partials + 3 * q + 0));
+    b = fmax(b, ld_cg(partials + 3 * q + 1));
+    c = fmax(c, ld_cg(partials + 3 * q + 2));
+  }
+  a = block_reduce_max<kBlock>(a, sm[0]);
+  b = block_reduce_max<kBlock>(b, sm[1]);
+  c = block_reduce_max<kBlock>(c, sm[2]);
+  if (threadIdx.x == 0) {
+    out3[0] = a;
+    out3[1] = b;
+    out3[2] = c;
+    *ticket = 0;
+  }
+}
+
+// ---- velocity boundary conditions, one face per launch (discretization.c:119-332) ----
+// The normal component lives on the wall face (index 0 or n), the tangential
+// components have a ghost cell (0 or n+1) mirrored from the first interior
+// cell. Faces run in the reference order (top, bottom, left, right, front,
+// back) as separate launches: later faces read edge values earlier ones wrote.
+struct FaceArgs {
+  Dims g;
+  int axis, high, bc;
+};
+
+__global__ void k_face(FaceArgs fa, double *__restrict__ u, double *__restrict__ v,
+    double *__restrict__ w)
+{
+  const Dims &g = fa.g;
+  const int ax = fa.axis;
+  const int a1 = (ax == 0) ? 1 : 0;
+  const int a2 = (ax == 2) ? 1 : 2;
+  const int n[3] = { g.imax, g.jmax, g.kmax };
+  const int a = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int b = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (a > n[a1] || b > n[a2]) return;
+  const int s[3] = { 1, g.sj, g.sk };
+  const int64_t base = (int64_t)a * s[a1] + (int64_t)b * s[a2];
+  const int na = n[ax];
+  const int wall = fa.high ? na : 0, wall_in = fa.high ? na - 1 : 1;
+  const int ghost = fa.high ? na + 1 : 0, inner = fa.high ? na : 1;
+  double *vel[3] = { u, v, w };
+  for (int comp = 0; comp < 3; comp++) {
+    double *q = vel[comp];
+    if (comp == ax) {
+      q[base + (int64_t)wall * s[ax]] =
+          (fa.bc == OUTFLOW) ? q[base + (int64_t)wall_in * s[ax]] : 0.0;
+    } else {
+      const double in = q[base + (int64_t)inner * s[ax]];
+      q[base + (int64_t)ghost * s[ax]] = (fa.bc == NOSLIP) ? -in : in;
+    }
+  }
+}
+
+// ---- special boundary conditions (discretization.c:364-389) ----
+__global__ void k_lid(Dims g, double twice_lid, double *__restrict__ u)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int k = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (i >= g.imax || k >= g.kmax) return;
+  const int64_t c = (int64_t)k * g.sk + (int64_t)g.jmax * g.sj + i;
+  u[c + g.sj] = twice_lid - u[c];
+}
+
+__global__ void k_inflow(Dims g, double inflow, double *__restrict__ u)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int k = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (j > g.jmax || k > g.kmax) return;
+  u[(int64_t)k * g.sk + (int64_t)j * g.sj] = inflow;
+}
+
+// ---- F, G, H (discretization.c:455-652) ----
+struct FghArgs {
+  Dims g;
+  double c1x, c1y, c1z;  // 0.25 / h
+  double c2x, c2y, c2z;  // gamma * 0.25 / h
+  double ex, ey, ez;     // 1 / h^2
+  double iRe, dt, gx, gy, gz;
+};
+
+// donor-cell convective difference d(c q)/ds: cp, cm are the doubled
+// transport velocities on the + and - side, q/qp/qm the transported quantity
+__device__ __forceinline__ double donor(
+    double c1, double c2, double cp, double cm, double q, double qp, double qm)
+{
+  return c1 * (cp * (q + qp) - cm * (q + qm)) + c2 * (fabs(cp) * (q - qp) + fabs(cm) * (q - qm));
+}
+
+__device__ __forceinline__ double second(double e, double qp, double q, double qm)
+{
+  return e * (qp - 2.0 * q + qm);
+}
+
+__global__ void __launch_bounds__(kBlock) k_fgh(FghArgs A, const double *__restrict__ u,
+    const double *__restrict__ v, const double *__restrict__ w, double *__restrict__ f,
+    double *__restrict__ gg, double *__restrict__ h)
+{
+  const Dims &g = A.g;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
+  if (i > g.imax || j > g.jmax || k > g.kmax) return;
+  const int sj = g.sj, sk = g.sk;
+  const int64_t c = (int64_t)k * sk + (int64_t)j * sj + i;
+
+  // F on the +x face; the wall face F(imax) carries U itself
+  if (i == g.imax) {
+    f[c] = u[c];
+  } else {
+    const double uc = u[c], ue = u[c + 1], uw = u[c - 1];
+    const double un = u[c + sj], us = u[c - sj], ut = u[c + sk], ub = u[c - sk];
+    const double cx = donor(A.c1x, A.c2x, uc + ue, uc + uw, uc, ue, uw);
+    const double cy = donor(A.c1y, A.c2y, v[c] + v[c + 1], v[c - sj] + v[c + 1 - sj], uc, un, us);
+    const double cz = donor(A.c1z, A.c2z, w[c] + w[c + 1], w[c - sk] + w[c + 1 - sk], uc, ut, ub);
+    const double lap = second(A.ex, ue, uc, uw) + second(A.ey, un, uc, us) + second(A.ez, ut, uc, ub);
+    f[c] = uc + A.dt * (A.iRe * lap - cx - cy - cz + A.gx);
+  }
+  // G on the +y face
+  if (j == g.jmax) {
+    gg[c] = v[c];
+  } else {
+    const double vc = v[c], ve = v[c + 1], vw = v[c - 1];
+    const double vn = v[c + sj], vs = v[c - sj], vt = v[c + sk], vb = v[c - sk];
+    const double cx = donor(A.c1x, A.c2x, u[c] + u[c + sj], u[c - 1] + u[c - 1 + sj], vc, ve, vw);
+    const double cy = donor(A.c1y, A.c2y, vc + vn, vc + vs, vc, vn, vs);
+    // reference quirk kept for parity (discretization.c:543-550): the "minus"
+    // half uses V(i,j,k+1) where the textbook stencil has V(i,j,k-1)
+    const double cz = donor(A.c1z, A.c2z, w[c] + w[c + sj], w[c - sk] + w[c + sj - sk], vc, vt, vt);
+    const double lap = second(A.ex, ve, vc, vw) + second(A.ey, vn, vc, vs) + second(A.ez, vt, vc, vb);
+    gg[c] = vc + A.dt * (A.iRe * lap - cx - cy - cz + A.gy);
+  }
+  // H on the +z face
+  if (k == g.kmax) {
+    h[c] = w[c];
+  } else {
+    const double wc = w[c], we = w[c + 1], ww = w[c - 1];
+    const double wn = w[c + sj], ws = w[c - sj], wt = w[c + sk], wb = w[c - sk];
+    const double cx = donor(A.c1x, A.c2x, u[c] + u[c + sk], u[c - 1] + u[c - 1 + sk], wc, we, ww);
+    const double cy = donor(A.c1y, A.c2y, v[c] + v[c + sk], v[c - sj + sk] + v[c - sj], wc, wn, ws);
+    const double cz = donor(A.c1z, A.c2z, wc + wt, wc + wb, wc, wt, wb);
+    const double lap = second(A.ex, we, wc, ww) + second(A.ey, wn, wc, ws) + second(A.ez, wt, wc, wb);
+    h[c] = wc + A.dt * (A.iRe * lap - cx - cy - cz + A.gz);
+  }
+  // low wall faces F(0), G(0), H(0) carry the velocity (discretization.c:601-643)
+  if (i == 1) f[c - 1] = u[c - 1];
+  if (j == 1) gg[c - sj] = v[c - sj];
+  if (k == 1) h[c - sk] = w[c - sk];
+}
+
+// ---- RHS (discretization.c:334-362) ----
+__global__ void __launch_bounds__(kBlock) k_rhs(Dims g, double ix, double iy, double iz,
+    double idt, const double *__restrict__ f, const double *__restrict__ gg,
+    const double *__restrict__ h, double *__restrict__ rhs)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
+  if (i > g.imax || j > g.jmax || k > g.kmax) return;
+  const int64_t c = (int64_t)k * g.sk + (int64_t)j * g.sj + i;
+  rhs[c] = ((f[c] - f[c - 1]) * ix + (gg[c] - gg[c - g.sj]) * iy + (h[c] - h[c - g.sk]) * iz) * idt;
+}
+
+// ---- adaptUV (discretization.c:654-681) ----
+__global__ void __launch_bounds__(kBlock) k_adapt(Dims g, double fx, double fy, double fz,
+    const double *__restrict__ f, const double *__restrict__ gg, const double *__restrict__ h,
+    const double *__restrict__ p, double *__restrict__ u, double *__restrict__ v,
+    double *__restrict__ w)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
+  if (i > g.imax || j > g.jmax || k > g.kmax) return;
+  const int64_t c = (int64_t)k * g.sk + (int64_t)j * g.sj + i;
+  const double pc = p[c];
+  u[c] = f[c] - (p[c + 1] - pc) * fx;
+  v[c] = gg[c] - (p[c + g.sj] - pc) * fy;
+  w[c] = h[c] - (p[c + g.sk] - pc) * fz;
+}
+
+// ---- normalizePressure (discretization.c:403-429) ----
+// Interior sum (block partials folded by the last block), then the mean is
+// subtracted by a second kernel that reads it from device memory.
+__global__ void __launch_bounds__(kBlock) k_interior_sum(Dims g, const double *__restrict__ p,
+    double *__restrict__ partials, unsigned *ticket, double *__restrict__ out)
+{
+  const int64_t ncell = (int64_t)g.imax * g.jmax * g.kmax;
+  double s = 0.0;
+  for (int64_t q = blockIdx.x * (int64_t)kBlock + threadIdx.x; q < ncell;
+       q += (int64_t)gridDim.x * kBlock) {
+    const int i = (int)(q % g.imax) + 1;
+    const int64_t r = q / g.imax;
+    const int j = (int)(r % g.jmax) + 1;
+    const int k = (int)(r / g.jmax) + 1;
+    s += p[(int64_t)k * g.sk + (int64_t)j * g.sj + i];
+  }
+  __shared__ double sm[kBlock / 32];
+  s = block_reduce_sum<kBlock>(s, sm);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = s;
+    last = ticket_is_last(ticket);
+  }
+  __syncthreads();
+  if (!last) return;
+  double t = 0.0;
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += kBlock) t += ld_cg(partials + q);
+  t = block_reduce_sum<kBlock>(t, sm);
+  if (threadIdx.x == 0) {
+    out[0] = t;
+    out[1] = t / (double)ncell;
+    *ticket = 0;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) k_subtract_mean(Dims g, double *__restrict__ p,
+    const double *__restrict__ mean)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
+  if (i > g.imax || j > g.jmax || k > g.kmax) return;
+  const int64_t c = (int64_t)k * g.sk + (int64_t)j * g.sj + i;
+  p[c] = p[c] - mean[0];
+}
+
+dim3 cell_grid(const Dims &g, dim3 blk)
+{
+  return dim3((g.imax + blk.x - 1) / blk.x, (g.jmax + blk.y - 1) / blk.y,
+      (g.kmax + blk.z - 1) / blk.z);
+}
+
+const dim3 kCellBlock(64, 2, 2);
+
+bool launched(const char *what) { return cuda_ok(cudaGetLastError(), what); }
+
+}  // namespace
+
+// ---- launchers ----
+
+bool launch_max3(const Dims &g, const double *u, const double *v, const double *w,
+    ReduceScratch &red, double *d_out3)
+{
+  int blocks = 4 * sm_count();
+  if (!reduce_scratch_alloc(red, 3 * blocks)) return false;
+  k_max3<<<blocks, kBlock, 0, stream()>>>(u, v, w, g.padded, red.partials, red.ticket, d_out3);
+  return launched("k_max3");
+}
+
+bool launch_bc(const Dims &g, const int bc[6], int problem, double lid, double inflow,
+    double *u, double *v, double *w)
+{
+  // reference order: top, bottom, left, right, front, back (discretization.c:129-331)
+  static const int order[6][3] = { // axis, high, slot in bc[] (left,right,bottom,top,front,back)
+    { 1, 1, 3 }, { 1, 0, 2 }, { 0, 0, 0 }, { 0, 1, 1 }, { 2, 0, 4 }, { 2, 1, 5 } };
+  (void)problem;
+  (void)lid;
+  (void)inflow;
+  const int n[3] = { g.imax, g.jmax, g.kmax };
+  for (int f = 0; f < 6; f++) {
+    FaceArgs fa{ g, order[f][0], order[f][1], bc[order[f][2]] };
+    if (fa.bc != NOSLIP && fa.bc != SLIP && fa.bc != OUTFLOW) continue;  // periodic: no-op
+    const int a1 = (fa.axis == 0) ? 1 : 0, a2 = (fa.axis == 2) ? 1 : 2;
+    dim3 blk(32, 8);
+    dim3 grd((n[a1] + 31) / 32, (n[a2] + 7) / 8);
+    k_face<<<grd, blk, 0, stream()>>>(fa, u, v, w);
+    if (!launched("k_face")) return false;
+  }
+  return true;
+}
+
+bool launch_special(const Dims &g, int problem, double lid, double inflow, double *u)
+{
+  dim3 blk(32, 8);
+  if (problem == PROBLEM_DCAVITY) {
+    if (g.imax < 2 || g.kmax < 2) return true;
+    dim3 grd((g.imax - 1 + 31) / 32, (g.kmax - 1 + 7) / 8);
+    k_lid<<<grd, blk, 0, stream()>>>(g, 2.0 * lid, u);
+    return launched("k_lid");
+  }
+  if (problem == PROBLEM_CANAL) {
+    dim3 grd((g.jmax + 31) / 32, (g.kmax + 7) / 8);
+    k_inflow<<<grd, blk, 0, stream()>>>(g, inflow, u);
+    return launched("k_inflow");
+  }
+  return true;
+}
+
+bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, double gz,
+    double dt, double dx, double dy, double dz, const double *u, const double *v,
+    const double *w, double *f, double *gg, double *h)
+{
+  FghArgs A;
+  A.g = g;
+  const double ix = 1.0 / dx, iy = 1.0 / dy, iz = 1.0 / dz;
+  A.c1x = ix * 0.25;
+  A.c1y = iy * 0.25;
+  A.c1z = iz * 0.25;
+  A.c2x = gamma * ix * 0.25;
+  A.c2y = gamma * iy * 0.25;
+  A.c2z = gamma * iz * 0.25;
+  A.ex = ix * ix;
+  A.ey = iy * iy;
+  A.ez = iz * iz;
+  A.iRe = 1.0 / re;
+  A.dt = dt;
+  A.gx = gx;
+  A.gy = gy;
+  A.gz = gz;
+  k_fgh<<<cell_grid(g, kCellBlock), kCellBlock, 0, stream()>>>(A, u, v, w, f, gg, h);
+  return launched("k_fgh");
+}
+
+bool launch_rhs(const Dims &g, double dt, double dx, double dy, double dz, const double *f,
+    const double *gg, const double *h, double *rhs)
+{
+  k_rhs<<<cell_grid(g, kCellBlock), kCellBlock, 0, stream()>>>(
+      g, 1.0 / dx, 1.0 / dy, 1.0 / dz, 1.0 / dt, f, gg, h, rhs);
+  return launched("k_rhs");
+}
+
+bool launch_interior_sum(const Dims &g, const double *p, ReduceScratch &red, double *d_out)
+{
+  int blocks = 4 * sm_count();
+  if (!reduce_scratch_alloc(red, 3 * blocks)) return false;
+  k_interior_sum<<<blocks, kBlock, 0, stream()>>>(g, p, red.partials, red.ticket, d_out);
+  return launched("k_interior_sum");
+}
+
+bool launch_subtract_mean(const Dims &g, double *p, const double *d_mean)
+{
+  k_subtract_mean<<<cell_grid(g, kCellBlock), kCellBlock, 0, stream()>>>(g, p, d_mean);
+  return launched("k_subtract_mean");
+}
+
+bool launch_adapt_uv(const Dims &g, double dt, double dx, double dy, double dz,
+    const double *f, const double *gg, const double *h, const double *p, double *u, double *v,
+    double *w)
+{
+  k_adapt<<<cell_grid(g, kCellBlock), kCellBlock, 0, stream()>>>(
+      g, dt / dx, dt / dy, dt / dz, f, gg, h, p, u, v, w);
+  return launched("k_adapt");
+}
+
+bool launch_fill(double *a, int64_t n, double value)
+{
+  k_fill<<<4 * sm_count(), kBlock, 0, stream()>>>(a, n, value);
+  return launched("k_fill");
+}
+
+int problem_code(const char *name)
+{
+  if (name == nullptr) return PROBLEM_NONE;
+  if (strcmp(name, "dcavity") == 0) return PROBLEM_DCAVITY;
+  if (strcmp(name, "canal") == 0) return PROBLEM_CANAL;
+  return PROBLEM_NONE;
+}
+
+}  // namespace nusif
+
+using namespace nusif;
+
+namespace {
+
+DiscState *need_state(const Discretization *d, const char *what)
+{
+  DiscState *st = disc_state(d);
+  if (!st) fail(NUSIF_ERR_STATE, "%s: discretization not initialised by initDiscretization", what);
+  return st;
+}
+
+bool verbose()
+{
+  const char *v = getenv("NUSIF_VERBOSE");
+  return v && v[0] && v[0] != '0';
+}
+
+// printConfig, reference src/discretization.c:16-47 (printed when NUSIF_VERBOSE is set)
+void print_config(const Discretization *s)
+{
+  printf("Parameters for #%s#\n", s->problem);
+  printf("BC Left:%d Right:%d Bottom:%d Top:%d Front:%d Back:%d\n", s->bcLeft, s->bcRight,
+      s->bcBottom, s->bcTop, s->bcFront, s->bcBack);
+  printf("\tReynolds number: %.2f\n", s->re);
+  printf("\tGx Gy: %.2f %.2f %.2f\n", s->gx, s->gy, s->gz);
+  printf("Geometry data:\n");
+  printf("\tDomain box size (x, y, z): %.2f, %.2f, %.2f\n", s->grid.xlength, s->grid.ylength,
+      s->grid.zlength);
+  printf("\tCells (x, y, z): %d, %d, %d\n", s->grid.imax, s->grid.jmax, s->grid.kmax);
+  printf("\tCell size (dx, dy, dz): %f, %f, %f\n", s->grid.dx, s->grid.dy, s->grid.dz);
+  printf("Timestep parameters:\n");
+  printf("\tDefault stepsize: %.2f, Final time %.2f\n", s->dt, s->te);
+  printf("\tdt bound: %.6f\n", s->dtBound);
+  printf("\tTau factor: %.2f\n", s->tau);
+  printf("Iterative parameters:\n");
+  printf("\tMax iterations: %d\n", s->itermax);
+  printf("\tepsilon (stopping tolerance) : %f\n", s->eps);
+  printf("\tgamma factor: %f\n", s->gamma);
+  printf("\tomega (SOR relaxation): %f\n", s->omega);
+}
+
+}  // namespace
+
+extern "C" {
+
+// initDiscretization, reference src/discretization.c:49-117
+void initDiscretization(Discretization *s, Parameter *params)
+{
+  if (!s || !params) {
+    fail(NUSIF_ERR_ARG, "initDiscretization: null argument");
+    return;
+  }
+  if (params->imax < 1 || params->jmax < 1 || params->kmax < 1) {
+    fail(NUSIF_ERR_ARG, "initDiscretization: grid %d x %d x %d is empty", params->imax,
+        params->jmax, params->kmax);
+    return;
+  }
+  const int64_t padded = (int64_t)(params->imax + 2) * (params->jmax + 2) * (params->kmax + 2);
+  if (padded >= ((int64_t)1 << 31)) {
+    fail(NUSIF_ERR_ARG, "initDiscretization: %lld padded cells exceed the 2^31 index range",
+        (long long)padded);
+    return;
+  }
+  if (disc_state(s)) nusifFreeDiscretization(s);
+
+  s->problem = params->name;
+  s->bcLeft = params->bcLeft;
+  s->bcRight = params->bcRight;
+  s->bcBottom = params->bcBottom;
+  s->bcTop = params->bcTop;
+  s->bcFront = params->bcFront;
+  s->bcBack = params->bcBack;
+
+  s->grid.imax = params->imax;
+  s->grid.jmax = params->jmax;
+  s->grid.kmax = params->kmax;
+  s->grid.xlength = params->xlength;
+  s->grid.ylength = params->ylength;
+  s->grid.zlength = params->zlength;
+  s->grid.dx = params->xlength / params->imax;
+  s->grid.dy = params->ylength / params->jmax;
+  s->grid.dz = params->zlength / params->kmax;
+
+  s->eps = params->eps;
+  s->omega = params->omg;
+  s->itermax = params->itermax;
+  s->re = params->re;
+  s->gx = params->gx;
+  s->gy = params->gy;
+  s->gz = params->gz;
+  s->dt = params->dt;
+  s->te = params->te;
+  s->tau = params->tau;
+  s->gamma = params->gamma;
+
+  DiscState *st = disc_state_create(s);
+  st->dims = make_dims(params->imax, params->jmax, params->kmax);
+  const Extras *x = extras_for(params, false);
+  st->ext = x ? *x : Extras();
+
+  const size_t bytes = sizeof(double) * (size_t)padded;
+  double **fields[8] = { &s->u, &s->v, &s->w, &s->p, &s->rhs, &s->f, &s->g, &s->h };
+  for (int q = 0; q < 8; q++) {
+    *fields[q] = nullptr;
+    if (!cuda_ok(cudaMalloc(fields[q], bytes), "cudaMalloc(field)")) return;
+  }
+  if (!cuda_ok(cudaMalloc(&st->d_scalars, 8 * sizeof(double)), "cudaMalloc(scalars)")) return;
+  if (!cuda_ok(cudaMallocHost(&st->h_scalars, 8 * sizeof(double)), "cudaMallocHost(scalars)"))
+    return;
+  const double init[4] = { params->u_init, params->v_init, params->w_init, params->p_init };
+  for (int q = 0; q < 4; q++)
+    if (!launch_fill(*fields[q], padded, init[q])) return;
+  for (int q = 4; q < 8; q++)
+    if (!cuda_ok(cudaMemsetAsync(*fields[q], 0, bytes, stream()), "cudaMemsetAsync(field)"))
+      return;
+  cuda_ok(cudaStreamSynchronize(stream()), "initDiscretization sync");
+
+  const double dx = s->grid.dx, dy = s->grid.dy, dz = s->grid.dz;
+  const double invSqrSum = 1.0 / (dx * dx) + 1.0 / (dy * dy) + 1.0 / (dz * dz);
+  s->dtBound = 0.5 * s->re * 1.0 / invSqrSum;
+  if (verbose()) print_config(s);
+}
+
+// computeTimestep, reference src/discretization.c:431-453: the three maxima
+// come from the device, the dt arithmetic stays on the host.
+void computeTimestep(Discretization *s)
+{
+  DiscState *st = need_state(s, "computeTimestep");
+  if (!st) return;
+  if (!launch_max3(st->dims, s->u, s->v, s->w, st->red, st->d_scalars)) return;
+  if (!cuda_ok(cudaMemcpyAsync(st->h_scalars, st->d_scalars, 3 * sizeof(double),
+                   cudaMemcpyDeviceToHost, stream()),
+          "computeTimestep copy"))
+    return;
+  if (!cuda_ok(cudaStreamSynchronize(stream()), "computeTimestep sync")) return;
+  const double umax = st->h_scalars[0], vmax = st->h_scalars[1], wmax = st->h_scalars[2];
+  double dt = s->dtBound;
+  const double dx = s->grid.dx, dy = s->grid.dy, dz = s->grid.dz;
+  if (umax > 0) dt = (dt > dx / umax) ? dx / umax : dt;
+  if (vmax > 0) dt = (dt > dy / vmax) ? dy / vmax : dt;
+  if (wmax > 0) dt = (dt > dz / wmax) ? dz / wmax : dt;
+  s->dt = dt * s->tau;
+}
+
+void setBoundaryConditions(Discretization *s)
+{
+  DiscState *st = need_state(s, "setBoundaryConditions");
+  if (!st) return;
+  const int bc[6] = { s->bcLeft, s->bcRight, s->bcBottom, s->bcTop, s->bcFront, s->bcBack };
+  launch_bc(st->dims, bc, PROBLEM_NONE, 0.0, 0.0, s->u, s->v, s->w);
+}
+
+// the problem is matched by name at every call, as in the reference
+void setSpecialBoundaryCondition(Discretization *s)
+{
+  DiscState *st = need_state(s, "setSpecialBoundaryCondition");
+  if (!st) return;
+  launch_special(st->dims, problem_code(s->problem), st->ext.lid, st->ext.inflow, s->u);
+}
+
+void computeFG(Discretization *s)
+{
+  DiscState *st = need_state(s, "computeFG");
+  if (!st) return;
+  launch_fgh(st->dims, s->re, s->gamma, s->gx, s->gy, s->gz, s->dt, s->grid.dx, s->grid.dy,
+      s->grid.dz, s->u, s->v, s->w, s->f, s->g, s->h);
+}
+
+void computeRHS(Discretization *s)
+{
+  DiscState *st = need_state(s, "computeRHS");
+  if (!st) return;
+  launch_rhs(st->dims, s->dt, s->grid.dx, s->grid.dy, s->grid.dz, s->f, s->g, s->h, s->rhs);
+}
+
+void normalizePressure(Discretization *s)
+{
+  DiscState *st = need_state(s, "normalizePressure");
+  if (!st) return;
+  if (!launch_interior_sum(st->dims, s->p, st->red, st->d_scalars + 3)) return;
+  launch_subtract_mean(st->dims, s->p, st->d_scalars + 4);
+}
+
+void adaptUV(Discretization *s)
+{
+  DiscState *st = need_state(s, "adaptUV");
+  if (!st) return;
+  launch_adapt_uv(st->dims, s->dt, s->grid.dx, s->grid.dy, s->grid.dz, s->f, s->g, s->h, s->p,
+      s->u, s->v, s->w);
+}
+
+void nusifFreeDiscretization(Discretization *s)
+{
+  DiscState *st = disc_state(s);
+  if (!st) return;
+  cudaStreamSynchronize(stream());
+  double **fields[8] = { &s->u, &s->v, &s->w, &s->p, &s->rhs, &s->f, &s->g, &s->h };
+  for (int q = 0; q < 8; q++) {
+    if (*fields[q]) cudaFree(*fields[q]);
+    *fields[q] = nullptr;
+  }
+  if (st->d_scalars) cudaFree(st->d_scalars);
+  if (st->h_scalars) cudaFreeHost(st->h_scalars);
+  reduce_scratch_free(st->red);
+  disc_state_erase(s);
+}
+
+}  // extern "C"

@@ -1,0 +1,91 @@
+// Internal declarations of the GB300 NuSiF library (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "nusif_gb300.h"
+
+namespace nusif {
+
+// ---- error handling (runtime.cpp) ----
+void fail(int code, const char *fmt, ...);  // records or exits per error mode
+bool cuda_ok(cudaError_t e, const char *what);  // false after recording a failure
+bool has_error();                              // an error is pending (record mode)
+cudaStream_t stream();
+
+// ---- problem kinds and solver kinds ----
+enum Problem { PROBLEM_NONE = 0, PROBLEM_DCAVITY = 1, PROBLEM_CANAL = 2 };
+enum SolverKind { SOLVER_RB = 0, SOLVER_MG_REF = 1, SOLVER_MG = 2, SOLVER_MG_MIXED = 3 };
+
+// Extension settings carried beside a Parameter (keys this library adds).
+struct Extras {
+  int solver = -1;          // -1: not set (environment, then rb)
+  double lid = 1.0;         // dcavity lid speed (reference hard-codes 1)
+  double inflow = 2.0;      // canal inflow speed (reference hard-codes 2.0)
+  double rtol = 1e-6;       // relative residual target of the V-cycle solvers
+  int mg_levels = 0;        // 0: coarsen while every axis stays even and >= 8
+  int mg_pre = 2, mg_post = 2;
+  int mg_coarse_sweeps = 64;
+  int mg_maxcycles = 100;
+};
+Extras *extras_for(const Parameter *p, bool create);
+
+// Grid geometry shared by all kernels.
+struct Dims {
+  int imax, jmax, kmax;
+  int sj, sk;      // strides of j and k in the padded layout
+  int64_t padded;  // (imax+2)(jmax+2)(kmax+2)
+};
+inline Dims make_dims(int imax, int jmax, int kmax)
+{
+  Dims d;
+  d.imax = imax;
+  d.jmax = jmax;
+  d.kmax = kmax;
+  d.sj = imax + 2;
+  d.sk = (imax + 2) * (jmax + 2);
+  d.padded = (int64_t)(imax + 2) * (jmax + 2) * (kmax + 2);
+  return d;
+}
+
+// Reduction scratch: per-block partials plus a ticket counter, so that the
+// last block to finish folds the partials in a fixed order (deterministic,
+// no spin-waits).
+struct ReduceScratch {
+  double *partials = nullptr;   // device
+  unsigned *ticket = nullptr;   // device, returns to 0 after every use
+  int capacity = 0;
+};
+bool reduce_scratch_alloc(ReduceScratch &r, int capacity);
+void reduce_scratch_free(ReduceScratch &r);
+
+// Device state of one Discretization (kept beside the reference struct).
+struct DiscState {
+  Dims dims;
+  int problem = PROBLEM_NONE;
+  Extras ext;
+  ReduceScratch red;
+  double *d_scalars = nullptr;  // device: [0..2] max |u|,|v|,|w|, [3] sum p
+  double *h_scalars = nullptr;  // pinned host mirror
+};
+DiscState *disc_state(const Discretization *d);
+
+// ---- kernels launched by the discretization entry points (discretization.cu) ----
+bool launch_max3(const Dims &g, const double *u, const double *v, const double *w,
+    ReduceScratch &red, double *d_out3);
+bool launch_bc(const Dims &g, const int bc[6], int problem, double lid, double inflow,
+    double *u, double *v, double *w);
+bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, double gz,
+    double dt, double dx, double dy, double dz, const double *u, const double *v,
+    const double *w, double *f, double *gg, double *h);
+bool launch_rhs(const Dims &g, double dt, double dx, double dy, double dz, const double *f,
+    const double *gg, const double *h, double *rhs);
+bool launch_interior_sum(const Dims &g, const double *p, ReduceScratch &red, double *d_out);
+bool launch_subtract_mean(const Dims &g, double *p, const double *d_sum, double ncell);
+bool launch_adapt_uv(const Dims &g, double dt, double dx, double dy, double dz,
+    const double *f, const double *gg, const double *h, const double *p, double *u, double *v,
+    double *w);
+
+}  // namespace nusif

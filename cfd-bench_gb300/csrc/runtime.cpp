@@ -1,0 +1,173 @@
+// Runtime of the GB300 NuSiF library: error reporting, the launch stream,
+// field upload/download and the side tables that hold device state beside the
+// reference structs (whose layouts have no room for it).
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+
+#include "nusif_internal.h"
+
+namespace nusif {
+
+static int g_error_mode = NUSIF_ERRORS_EXIT;
+static int g_error_code = 0;
+static std::string g_error_msg;
+static cudaStream_t g_stream = nullptr;
+
+void fail(int code, const char *fmt, ...)
+{
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (g_error_mode == NUSIF_ERRORS_EXIT) {
+    fprintf(stderr, "Error: %s\n", buf);
+    exit(EXIT_FAILURE);
+  }
+  if (g_error_code == 0) {  // keep the first failure of a call chain
+    g_error_code = code;
+    g_error_msg = buf;
+  }
+}
+
+bool cuda_ok(cudaError_t e, const char *what)
+{
+  if (e == cudaSuccess) return true;
+  fail(NUSIF_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return false;
+}
+
+bool has_error() { return g_error_code != 0; }
+
+cudaStream_t stream() { return g_stream; }
+
+bool reduce_scratch_alloc(ReduceScratch &r, int capacity)
+{
+  if (r.capacity >= capacity) return true;
+  reduce_scratch_free(r);
+  if (!cuda_ok(cudaMalloc(&r.partials, sizeof(double) * (size_t)capacity), "cudaMalloc(partials)"))
+    return false;
+  if (!cuda_ok(cudaMalloc(&r.ticket, sizeof(unsigned) * 4), "cudaMalloc(ticket)")) return false;
+  if (!cuda_ok(cudaMemset(r.ticket, 0, sizeof(unsigned) * 4), "cudaMemset(ticket)")) return false;
+  r.capacity = capacity;
+  return true;
+}
+
+void reduce_scratch_free(ReduceScratch &r)
+{
+  if (r.partials) cudaFree(r.partials);
+  if (r.ticket) cudaFree(r.ticket);
+  r = ReduceScratch();
+}
+
+// ---- side tables ----
+static std::unordered_map<const void *, DiscState *> &disc_table()
+{
+  static std::unordered_map<const void *, DiscState *> t;
+  return t;
+}
+
+DiscState *disc_state(const Discretization *d)
+{
+  auto &t = disc_table();
+  auto it = t.find(d);
+  return it == t.end() ? nullptr : it->second;
+}
+
+DiscState *disc_state_create(const Discretization *d)
+{
+  auto &t = disc_table();
+  auto it = t.find(d);
+  if (it != t.end()) return it->second;
+  DiscState *s = new DiscState();
+  t[d] = s;
+  return s;
+}
+
+void disc_state_erase(const Discretization *d)
+{
+  auto &t = disc_table();
+  auto it = t.find(d);
+  if (it == t.end()) return;
+  delete it->second;
+  t.erase(it);
+}
+
+static double *field_ptr(const Discretization *d, int which)
+{
+  switch (which) {
+  case NUSIF_U: return d->u;
+  case NUSIF_V: return d->v;
+  case NUSIF_W: return d->w;
+  case NUSIF_P: return d->p;
+  case NUSIF_RHS: return d->rhs;
+  case NUSIF_F: return d->f;
+  case NUSIF_G: return d->g;
+  case NUSIF_H: return d->h;
+  default: return nullptr;
+  }
+}
+
+}  // namespace nusif
+
+using namespace nusif;
+
+extern "C" {
+
+void nusifSetErrorMode(int mode) { g_error_mode = mode; }
+
+int nusifGetLastError(char *msg, int len)
+{
+  int code = g_error_code;
+  if (msg && len > 0) {
+    strncpy(msg, g_error_msg.c_str(), (size_t)len - 1);
+    msg[len - 1] = '\0';
+  }
+  g_error_code = 0;
+  g_error_msg.clear();
+  return code;
+}
+
+void nusifSetStream(void *s) { g_stream = (cudaStream_t)s; }
+void *nusifGetStream(void) { return (void *)g_stream; }
+
+int nusifDownloadField(const Discretization *d, int which, double *host)
+{
+  DiscState *st = disc_state(d);
+  double *src = field_ptr(d, which);
+  if (!st || !src || !host) {
+    fail(NUSIF_ERR_ARG, "nusifDownloadField: unknown discretization or field %d", which);
+    return NUSIF_ERR_ARG;
+  }
+  size_t bytes = sizeof(double) * (size_t)st->dims.padded;
+  if (!cuda_ok(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, g_stream),
+          "download field"))
+    return NUSIF_ERR_CUDA;
+  if (!cuda_ok(cudaStreamSynchronize(g_stream), "download field sync")) return NUSIF_ERR_CUDA;
+  return NUSIF_OK;
+}
+
+int nusifUploadField(Discretization *d, int which, const double *host)
+{
+  DiscState *st = disc_state(d);
+  double *dst = field_ptr(d, which);
+  if (!st || !dst || !host) {
+    fail(NUSIF_ERR_ARG, "nusifUploadField: unknown discretization or field %d", which);
+    return NUSIF_ERR_ARG;
+  }
+  size_t bytes = sizeof(double) * (size_t)st->dims.padded;
+  if (!cuda_ok(cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, g_stream),
+          "upload field"))
+    return NUSIF_ERR_CUDA;
+  if (!cuda_ok(cudaStreamSynchronize(g_stream), "upload field sync")) return NUSIF_ERR_CUDA;
+  return NUSIF_OK;
+}
+
+const char *nusifVersion(void) { return "nusif-gb300 1.0 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,54 @@
+// Solver-side internal declarations (not part of the C ABI).
+#pragma once
+
+#include "nusif_internal.h"
+
+namespace nusif {
+
+// Convergence state of one solve, kept in device memory and mirrored in
+// pinned host memory.
+struct SolveState {
+  double res;     // carried mean-square residual (rb) / residual (mg-ref)
+  double epssq;   // eps^2
+  double ncell;   // imax*jmax*kmax
+  int it;         // iterations done
+  int itermax;
+  int done;       // set by the device when the loop condition fails
+  int pad;
+};
+
+struct SorArgs {
+  Dims g;
+  double idx2, idy2, idz2, diag, factor;
+  int kb;  // k planes per block
+};
+
+SorArgs make_sor_args(const Dims &g, double dx, double dy, double dz, double omega);
+dim3 sor_grid(const SorArgs &A);
+int sor_blocks(const SorArgs &A);
+bool launch_rb_iteration(const SorArgs &A, double *p, const double *rhs, SolveState *st,
+    ReduceScratch &red);
+bool launch_sor_sweep(const SorArgs &A, double *p, const double *rhs, bool ghosts);
+bool launch_residual_ref(const SorArgs &A, const double *p, const double *rhs, SolveState *st,
+    ReduceScratch &red);
+bool launch_pressure_ghosts(const Dims &g, double *p);
+
+struct MgHierarchy;  // multigrid.cu
+
+struct SolverState {
+  int kind = SOLVER_RB;
+  Extras ext;
+  SolveState *d_state = nullptr;
+  SolveState *h_state = nullptr;  // pinned
+  ReduceScratch red;
+  int last_iterations = 0;
+  MgHierarchy *mg = nullptr;
+};
+
+SolverState *solver_state(const Solver *s);
+
+bool mg_setup(Solver *s, Discretization *d, SolverState *ss);
+double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs);
+void mg_free(Solver *s, SolverState *ss);
+
+}  // namespace nusif

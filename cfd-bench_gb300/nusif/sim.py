@@ -1,0 +1,164 @@
+"""Host driver over the C ABI: the reference time loop (src/main.c:53-88).
+
+``Simulation`` owns one Parameter / Discretization / Solver triple of the
+library and advances it with exactly the reference's call order. Every call
+goes through the shared library; errors raise ``NusifError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import tempfile
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+from . import abi
+from .params import write_par
+
+# keys the reference parser knows (src/parameter.c:65-95); the rest are extensions
+REFERENCE_KEYS = {
+    "xlength", "ylength", "zlength", "imax", "jmax", "kmax", "itermax", "levels",
+    "presmooth", "postsmooth", "eps", "omg", "re", "tau", "gamma", "dt", "te",
+    "gx", "gy", "gz", "name", "bcLeft", "bcRight", "bcBottom", "bcTop", "bcFront",
+    "bcBack", "u_init", "v_init", "w_init", "p_init",
+}
+
+
+@dataclass
+class StepInfo:
+    nt: int        # steps done after this one
+    t: float       # time after this step
+    dt: float      # step size used
+    res: float     # value solve() returned
+    it: int        # solver iterations (RB) / V-cycles (MG); 0 for mg-ref
+
+
+class Simulation:
+    """One NuSiF case on the GPU, driven through the C ABI."""
+
+    def __init__(self, par: str | Path | dict):
+        self.lib = abi.load_library()
+        lib = self.lib
+        self._tmp = None
+        if isinstance(par, dict):
+            self._tmp = tempfile.TemporaryDirectory(prefix="nusif_")
+            par = write_par(Path(self._tmp.name) / "case.par", par)
+        self.par_path = str(par)
+        self.param = abi.Parameter()
+        lib.initParameter(C.byref(self.param))
+        lib.readParameter(C.byref(self.param), self.par_path.encode())
+        abi.check(lib)
+        self.d = abi.Discretization()
+        lib.initDiscretization(C.byref(self.d), C.byref(self.param))
+        abi.check(lib)
+        self.s = abi.Solver()
+        lib.initSolver(C.byref(self.s), C.byref(self.d), C.byref(self.param))
+        abi.check(lib)
+        self.t = 0.0
+        self.nt = 0
+        self._closed = False
+
+    # ---- geometry ----
+    @property
+    def dims(self) -> tuple[int, int, int]:
+        g = self.d.grid
+        return g.imax, g.jmax, g.kmax
+
+    @property
+    def padded_shape(self) -> tuple[int, int, int]:
+        i, j, k = self.dims
+        return (k + 2, j + 2, i + 2)
+
+    @property
+    def dt(self) -> float:
+        return self.d.dt
+
+    @property
+    def te(self) -> float:
+        return self.d.te
+
+    # ---- fields ----
+    def field(self, name: str) -> np.ndarray:
+        out = np.empty(self.padded_shape, dtype=np.float64)
+        self.lib.nusifDownloadField(C.byref(self.d), abi.FIELD_INDEX[name],
+                                    out.ctypes.data_as(abi.c_double_p))
+        abi.check(self.lib)
+        return out
+
+    def set_field(self, name: str, arr: np.ndarray) -> None:
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(self.padded_shape)
+        self.lib.nusifUploadField(C.byref(self.d), abi.FIELD_INDEX[name],
+                                  a.ctypes.data_as(abi.c_double_p))
+        abi.check(self.lib)
+
+    # ---- reference operators, one C-ABI call each ----
+    def _call(self, name: str) -> None:
+        getattr(self.lib, name)(C.byref(self.d))
+        abi.check(self.lib)
+
+    def compute_timestep(self): self._call("computeTimestep")
+    def set_boundary_conditions(self): self._call("setBoundaryConditions")
+    def set_special_boundary_condition(self): self._call("setSpecialBoundaryCondition")
+    def compute_fg(self): self._call("computeFG")
+    def compute_rhs(self): self._call("computeRHS")
+    def normalize_pressure(self): self._call("normalizePressure")
+    def adapt_uv(self): self._call("adaptUV")
+
+    def solve(self) -> float:
+        res = self.lib.solve(C.byref(self.s), self.d.p, self.d.rhs)
+        abi.check(self.lib)
+        return res
+
+    @property
+    def iterations(self) -> int:
+        return self.lib.nusifSolverIterations(C.byref(self.s))
+
+    # ---- the time loop body, reference src/main.c:61-79 ----
+    def step(self) -> StepInfo:
+        if self.d.tau > 0.0:
+            self.compute_timestep()
+        self.set_boundary_conditions()
+        self.set_special_boundary_condition()
+        self.compute_fg()
+        self.compute_rhs()
+        if self.nt % 100 == 0:
+            self.normalize_pressure()
+        res = self.solve()
+        it = self.iterations
+        self.adapt_uv()
+        dt = self.d.dt
+        self.t += dt
+        self.nt += 1
+        return StepInfo(self.nt, self.t, dt, res, it)
+
+    def run(self, max_steps: int | None = None, callback=None) -> list[StepInfo]:
+        """``while (t <= te)`` (src/main.c:60), optionally capped at max_steps."""
+        out = []
+        while self.t <= self.te and (max_steps is None or len(out) < max_steps):
+            info = self.step()
+            out.append(info)
+            if callback:
+                callback(self, info)
+        return out
+
+    def close(self) -> None:
+        if self._closed:
+            return
+        self.lib.nusifFreeSolver(C.byref(self.s))
+        self.lib.nusifFreeDiscretization(C.byref(self.d))
+        self._closed = True
+        if self._tmp is not None:
+            self._tmp.cleanup()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,175 @@
+/*
+ * nusif_gb300.h -- C ABI of the GB300 (sm_103a) NuSiF hot-path library.
+ *
+ * The library replaces the reference objects parameter.o, discretization.o
+ * and solver-{rb,mg}.o of HPC-Dwarfs/CFD-Bench ("NuSiF", src/). The entry
+ * points below have the reference names, signatures, argument meaning and
+ * error behaviour; the structs have the reference member order and types, so
+ * an unchanged src/main.c links against the library.
+ *
+ * Differences a caller must know:
+ *  - The field pointers in Discretization (p, rhs, f, g, h, u, v, w) are
+ *    DEVICE pointers to FP64 arrays in the reference layout
+ *    ((imax+2)(jmax+2)(kmax+2) doubles, i fastest, one ghost layer;
+ *    src/util.h:19-34). Read them on the host with nusifDownloadField().
+ *  - All scalar time-step logic (dt, dtBound, t) stays on the host in the
+ *    reference's own expressions.
+ *  - Errors: by default a failing call prints to stderr and exits with
+ *    EXIT_FAILURE, as the reference does (src/allocate.c:18-31,
+ *    src/parameter.c:38-41). nusifSetErrorMode(NUSIF_ERRORS_RECORD) makes
+ *    calls return instead and report through nusifGetLastError().
+ *  - Single host thread, no reentrancy (as the reference).
+ */
+#ifndef NUSIF_GB300_H
+#define NUSIF_GB300_H
+
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define NUSIF_API __attribute__((visibility("default")))
+#else
+#define NUSIF_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- reference types (layouts identical to the sequential reference build) ---- */
+
+/* src/grid.h:8-12 */
+typedef struct {
+  double dx, dy, dz;
+  int imax, jmax, kmax;
+  double xlength, ylength, zlength;
+} Grid;
+
+/* src/comm.h:33-44, sequential build (no MPI members) */
+typedef struct {
+  int rank;
+  int size;
+  int neighbours[6];
+  int coords[3], dims[3];
+  int imaxLocal, jmaxLocal, kmaxLocal;
+} CommType;
+
+/* src/parameter.h:8-19 */
+typedef struct {
+  int imax, jmax, kmax;
+  double xlength, ylength, zlength;
+  int itermax;
+  double eps, omg;
+  double re, tau, gamma;
+  double te, dt;
+  double gx, gy, gz;
+  char *name;
+  int bcLeft, bcRight, bcBottom, bcTop, bcFront, bcBack;
+  double u_init, v_init, w_init, p_init;
+  int levels, presmooth, postsmooth;
+} Parameter;
+
+/* src/discretization.h:12 */
+enum BC { NOSLIP = 1, SLIP, OUTFLOW, PERIODIC };
+
+/* src/discretization.h:14-32; field pointers are device pointers */
+typedef struct {
+  Grid grid;
+  double *p, *rhs;
+  double *f, *g, *h;
+  double *u, *v, *w;
+  double eps, omega;
+  double re, tau, gamma;
+  double gx, gy, gz;
+  int itermax;
+  double dt, te;
+  double dtBound;
+  char *problem;
+  int bcLeft, bcRight, bcBottom, bcTop, bcFront, bcBack;
+  CommType comm;
+} Discretization;
+
+/* src/solver.h:12-33 */
+typedef struct {
+  Grid *grid;
+  double *p, *rhs;
+  double *f, *g, *h;
+  double *u, *v, *w;
+  double eps, omega;
+  double re, tau, gamma;
+  double gx, gy, gz;
+  int itermax;
+  double dt, te;
+  double dtBound;
+  char *problem;
+  int bcLeft, bcRight, bcBottom, bcTop, bcFront, bcBack;
+  double **r, **e;
+  int levels, presmooth, postsmooth;
+  CommType *comm;
+} Solver;
+
+/* ---- reference entry points ---- */
+
+/* src/parameter.h:22-24 (parameter.c:13-30, 32-98, 100-131). Same parsing
+ * rules: text after '#' dropped, split on spaces only, keys matched by prefix
+ * of the key's length, atoi/atof/strdup. Extra keys of this library (solver,
+ * lid, inflow, rtol, mg_*) are stored beside the struct, keyed by its address. */
+NUSIF_API void initParameter(Parameter *param);
+NUSIF_API void readParameter(Parameter *param, const char *filename);
+NUSIF_API void printParameter(Parameter *param);
+
+/* src/discretization.h:34-41 */
+NUSIF_API void initDiscretization(Discretization *d, Parameter *params); /* discretization.c:49-117 */
+NUSIF_API void computeTimestep(Discretization *d);                       /* discretization.c:431-453 */
+NUSIF_API void setBoundaryConditions(Discretization *d);                 /* discretization.c:119-332 */
+NUSIF_API void setSpecialBoundaryCondition(Discretization *d);           /* discretization.c:364-389 */
+NUSIF_API void computeFG(Discretization *d);                             /* discretization.c:455-652 */
+NUSIF_API void computeRHS(Discretization *d);                            /* discretization.c:334-362 */
+NUSIF_API void normalizePressure(Discretization *d);                     /* discretization.c:403-429 */
+NUSIF_API void adaptUV(Discretization *d);                               /* discretization.c:654-681 */
+
+/* src/solver.h:35-36. The solver kind is chosen at run time (the reference
+ * picks solver-rb.o or solver-mg.o at link time, Makefile:19-21): the .par key
+ * "solver" (rb | mg-ref | mg | mg-mixed), else the environment variable
+ * NUSIF_SOLVER, else rb.
+ *   rb       red-black SOR, solver-rb.c:27-172 (residual recurrence kept)
+ *   mg-ref   the reference multigrid as it behaves, solver-mg.c:299-402
+ *   mg       FP64 geometric V-cycles (full weighting, trilinear prolongation,
+ *            red-black Gauss-Seidel) to a relative residual (key rtol)
+ *   mg-mixed FP32 V-cycles inside FP64 iterative refinement, same stopping rule
+ * solve() returns what the reference returns: the mean-square residual
+ * (rb, mg-ref) or, for mg and mg-mixed, the final relative residual. */
+NUSIF_API void initSolver(Solver *s, Discretization *d, Parameter *p); /* solver-rb.c:17-25, solver-mg.c:356-389 */
+NUSIF_API double solve(Solver *s, double *p, const double *rhs);     /* solver-rb.c:27-172, solver-mg.c:391-402 */
+
+/* ---- extensions (no reference counterpart) ---- */
+
+enum { NUSIF_ERRORS_EXIT = 0, NUSIF_ERRORS_RECORD = 1 };
+enum { NUSIF_OK = 0, NUSIF_ERR_CUDA = 1, NUSIF_ERR_ARG = 2, NUSIF_ERR_IO = 3,
+       NUSIF_ERR_STATE = 4, NUSIF_ERR_DEVICE = 5 };
+/* field selectors for upload/download */
+enum { NUSIF_U = 0, NUSIF_V, NUSIF_W, NUSIF_P, NUSIF_RHS, NUSIF_F, NUSIF_G, NUSIF_H };
+
+NUSIF_API void nusifSetErrorMode(int mode);
+/* last error code (0 = none) and message; clears it */
+NUSIF_API int nusifGetLastError(char *msg, int len);
+/* CUDA stream (cudaStream_t) every later call launches on; NULL = legacy default stream */
+NUSIF_API void nusifSetStream(void *stream);
+NUSIF_API void *nusifGetStream(void);
+/* copies between a host array of (imax+2)(jmax+2)(kmax+2) doubles and a field */
+NUSIF_API int nusifDownloadField(const Discretization *d, int which, double *host);
+NUSIF_API int nusifUploadField(Discretization *d, int which, const double *host);
+/* iteration count of the last solve() (the reference prints it under VERBOSE,
+ * solver-rb.c:163-166); V-cycles for mg and mg-mixed */
+NUSIF_API int nusifSolverIterations(const Solver *s);
+/* set an extension key on a Parameter, as a .par line "key value" would */
+NUSIF_API int nusifParameterSet(Parameter *param, const char *key, const char *value);
+/* release device memory of a discretization / solver (the reference never frees) */
+NUSIF_API void nusifFreeDiscretization(Discretization *d);
+NUSIF_API void nusifFreeSolver(Solver *s);
+/* library version string */
+NUSIF_API const char *nusifVersion(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NUSIF_GB300_H */

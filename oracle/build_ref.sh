@@ -1,0 +1,54 @@
+#!/usr/bin/env bash
+# Builds the reference NuSiF sources, where they lie, into oracle/_ref/ --
+# test infrastructure only (the checker and the CPU baseline), never the product.
+#
+#   oracle/build_ref.sh [REFERENCE_ROOT]      (default: /root/reference)
+#
+# Outputs (git-ignored; nothing is written into the reference tree):
+#   _ref/libnusif_ref_rb.so   reference objects + oracle/ref_driver.c, SOLVER=rb
+#   _ref/libnusif_ref_mg.so   the same with SOLVER=mg
+#   _ref/NusifSolver-rb, _ref/NusifSolver-mg   the reference program itself
+#
+# Flags follow the reference's sequential GCC build (config.mk, mk/include_GCC.mk:
+# -O3 -ffast-math -std=c99 -D_GNU_SOURCE -DARRAY_ALIGNMENT=64 -DVERBOSE), minus
+# -DPROFILING, whose sequential build crashes at exit (src/profiler.c:104-108).
+# The libraries are built twice: "strict" (-O2, no fast-math, no FMA contraction)
+# pins the oracle bit-for-bit; "fast" keeps the reference's own flags for timing.
+set -euo pipefail
+REF="${1:-/root/reference}"
+HERE="$(cd "$(dirname "$0")" && pwd)"
+OUT="$HERE/_ref"
+SRC="$REF/src"
+if [ ! -f "$SRC/solver-rb.c" ]; then
+  echo "build_ref: reference sources not found under $SRC" >&2
+  exit 2
+fi
+mkdir -p "$OUT"
+CC="${CC:-gcc}"
+COMMON="-std=c99 -D_GNU_SOURCE -DARRAY_ALIGNMENT=64 -DVERBOSE -U_FORTIFY_SOURCE -D_FORTIFY_SOURCE=0 -I$SRC"
+FAST="-O3 -ffast-math"
+STRICT="-O2 -ffp-contract=off"
+LIBSRC="allocate.c comm.c discretization.c parameter.c profiler.c progress.c timing.c"
+
+build_lib() { # $1 solver, $2 flavour-name, $3 opt flags
+  local solver="$1" flav="$2" opt="$3" objs=()
+  local tmp="$OUT/obj-$solver-$flav"
+  mkdir -p "$tmp"
+  for f in $LIBSRC solver-$solver.c; do
+    "$CC" $COMMON $opt -fPIC -fvisibility=hidden -Dprintf=refdrv_printf \
+      -c "$SRC/$f" -o "$tmp/${f%.c}.o"
+    objs+=("$tmp/${f%.c}.o")
+  done
+  "$CC" $COMMON $opt -fPIC -c "$HERE/ref_driver.c" -o "$tmp/ref_driver.o"
+  "$CC" -shared -o "$OUT/libnusif_ref_${solver}${flav:+_$flav}.so" "${objs[@]}" "$tmp/ref_driver.o" -lm
+  rm -rf "$tmp"
+}
+
+for solver in rb mg; do
+  build_lib "$solver" "" "$STRICT"
+  build_lib "$solver" "fast" "$FAST"
+  # the reference program itself, with its own flags
+  "$CC" $COMMON $FAST -o "$OUT/NusifSolver-$solver" \
+    $(for f in $LIBSRC main.c vtkWriter-seq.c solver-$solver.c; do echo "$SRC/$f"; done) -lm
+done
+echo "build_ref: wrote $(ls "$OUT" | tr '\n' ' ')"

@@ -1,0 +1,182 @@
+"""Per-operator parity of the CUDA library (through the C ABI) against the
+golden vectors of the reference and against the CPU oracle on seeded random
+fields at small, odd and ragged sizes.
+
+Tolerances: the GPU evaluates the reference's FP64 expressions with fused
+multiply-adds and reordered sums, so results may differ in the last bits.
+Boundary copies are exact; arithmetic operators must agree to 1e-13 of the
+field's magnitude; the red-black solve must give the same iteration count and
+fields to 1e-11.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_values, load_golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+NAMES = ("u", "v", "w", "p", "rhs", "f", "g", "h")
+TOL = 1e-13
+
+
+def _sim(vals):
+    from nusif import Simulation
+    return Simulation(vals)
+
+
+def _upload(sim, arrays):
+    for f, a in arrays.items():
+        sim.set_field(f, a)
+
+
+def test_operators_match_golden(nusif_lib):
+    z = load_golden("kat_ops.npz")
+    v = golden_values(z)
+    inputs = {f: z[f"in_{f}"] for f in NAMES}
+    with _sim(v) as sim:
+        assert sim.d.dtBound == pytest.approx(float(z["dtbound"]), rel=1e-15)
+
+        def run(op):
+            _upload(sim, inputs)
+            sim.d.dt = float(z["dt_in"])
+            getattr(sim, op)()
+
+        run("compute_timestep")
+        assert sim.d.dt == pytest.approx(float(z["timestep_dt"]), rel=1e-15)
+        run("set_boundary_conditions")
+        for f in "uvw":
+            np.testing.assert_array_equal(sim.field(f), z[f"bc_out_{f}"])
+        run("set_special_boundary_condition")
+        np.testing.assert_array_equal(sim.field("u"), z["special_out_u"])
+        run("compute_fg")
+        for f in "fgh":
+            assert rel_err(sim.field(f), z[f"fg_out_{f}"]) < TOL, f
+        run("compute_rhs")
+        assert rel_err(sim.field("rhs"), z["rhs_out_rhs"]) < TOL
+        run("normalize_pressure")
+        assert rel_err(sim.field("p"), z["normalize_out_p"]) < TOL
+        run("adapt_uv")
+        for f in "uvw":
+            assert rel_err(sim.field(f), z[f"adapt_out_{f}"]) < TOL, f
+        _upload(sim, inputs)
+        res = sim.solve()
+        assert sim.iterations == int(z["solve_it"])
+        assert res == pytest.approx(float(z["solve_res"]), rel=1e-11)
+        assert rel_err(sim.field("p"), z["solve_out_p"]) < 1e-11
+
+
+SIZES = [(5, 5, 5), (8, 8, 8), (17, 9, 13), (33, 33, 33), (64, 3, 7), (1, 4, 6)]
+BCS = [(1, 1, 1, 1, 1, 1), (2, 3, 2, 1, 3, 4), (3, 3, 1, 1, 2, 2)]
+
+
+def _case(dims, bc, name="dcavity", **over):
+    from nusif.params import cavity
+    keys = ("bcLeft", "bcRight", "bcBottom", "bcTop", "bcFront", "bcBack")
+    return cavity(dims, xlength=1.1, ylength=0.8, zlength=1.3, name=name, re=300.0,
+                  gamma=0.85, gx=0.05, gy=-0.1, gz=0.02, tau=0.5, te=1e9, omg=1.7,
+                  eps=1e-6, itermax=25, **dict(zip(keys, bc)), **over)
+
+
+@pytest.mark.parametrize("dims", SIZES)
+@pytest.mark.parametrize("bci", range(len(BCS)))
+def test_operators_match_oracle_random(nusif_lib, oracle_mod, dims, bci):
+    o = oracle_mod
+    name = "canal" if bci == 2 else "dcavity"
+    v = _case(dims, BCS[bci], name=name, lid=1.25, inflow=0.75)
+    rng = np.random.default_rng(abs(hash((dims, bci))) % (2 ** 32))
+    with _sim(v) as sim:
+        shape = sim.padded_shape
+        inputs = {f: rng.standard_normal(shape) for f in NAMES}
+        g = o.grid(*dims, v["xlength"], v["ylength"], v["zlength"])
+        dt = 0.0123
+
+        def gpu(op):
+            _upload(sim, inputs)
+            sim.d.dt = dt
+            getattr(sim, op)()
+
+        def cpu():
+            return {f: inputs[f].copy() for f in NAMES}
+
+        gpu("compute_timestep")
+        a = cpu()
+        assert sim.d.dt == o.op_timestep(g, sim.d.dtBound, a["u"], a["v"], a["w"], v["tau"])
+
+        gpu("set_boundary_conditions")
+        a = cpu()
+        o.op_set_bc(g, [v[k] for k in o.BC_ORDER], a["u"], a["v"], a["w"])
+        for f in "uvw":
+            np.testing.assert_array_equal(sim.field(f), a[f])
+
+        gpu("set_special_boundary_condition")
+        a = cpu()
+        o.op_special_bc(g, name, a["u"], lid=1.25, inflow=0.75)
+        np.testing.assert_array_equal(sim.field("u"), a["u"])
+
+        gpu("compute_fg")
+        a = cpu()
+        o.op_fgh(g, v["re"], v["gamma"], v["gx"], v["gy"], v["gz"], dt, a["u"], a["v"],
+                 a["w"], a["f"], a["g"], a["h"])
+        for f in "fgh":
+            assert rel_err(sim.field(f), a[f]) < TOL, f
+
+        gpu("compute_rhs")
+        a = cpu()
+        o.op_rhs(g, dt, a["f"], a["g"], a["h"], a["rhs"])
+        assert rel_err(sim.field("rhs"), a["rhs"]) < TOL
+
+        gpu("normalize_pressure")
+        a = cpu()
+        o.op_normalize(g, a["p"])
+        assert rel_err(sim.field("p"), a["p"]) < TOL
+
+        gpu("adapt_uv")
+        a = cpu()
+        o.op_adapt(g, dt, a["f"], a["g"], a["h"], a["p"], a["u"], a["v"], a["w"])
+        for f in "uvw":
+            assert rel_err(sim.field(f), a[f]) < TOL, f
+
+        # untouched fields stay untouched (no stray writes)
+        for f in ("f", "g", "h", "rhs", "p"):
+            np.testing.assert_array_equal(sim.field(f), inputs[f])
+
+
+@pytest.mark.parametrize("dims", [(8, 8, 8), (17, 9, 13), (33, 33, 33), (2, 5, 3)])
+def test_rb_solve_matches_oracle(nusif_lib, oracle_mod, dims):
+    o = oracle_mod
+    v = _case(dims, BCS[0], itermax=60, eps=1e-9)
+    rng = np.random.default_rng(7)
+    with _sim(v) as sim:
+        g = o.grid(*dims, v["xlength"], v["ylength"], v["zlength"])
+        p = rng.standard_normal(sim.padded_shape)
+        rhs = rng.standard_normal(sim.padded_shape)
+        sim.set_field("p", p)
+        sim.set_field("rhs", rhs)
+        res = sim.solve()
+        pc = p.copy()
+        it, res_c = o.op_solve_rb(g, v["eps"], v["omg"], v["itermax"], pc, rhs)
+        assert sim.iterations == it
+        assert res == pytest.approx(res_c, rel=1e-11)
+        assert rel_err(sim.field("p"), pc) < 1e-11
+        np.testing.assert_array_equal(sim.field("rhs"), rhs)
+
+
+@pytest.mark.parametrize("levels,pre,post", [(3, 5, 3), (1, 4, 2), (2, 0, 2)])
+def test_mg_ref_solve_matches_oracle(nusif_lib, oracle_mod, levels, pre, post):
+    o = oracle_mod
+    dims = (12, 10, 9)
+    v = _case(dims, BCS[0], solver="mg-ref", levels=levels, presmooth=pre, postsmooth=post)
+    rng = np.random.default_rng(11)
+    with _sim(v) as sim:
+        g = o.grid(*dims, v["xlength"], v["ylength"], v["zlength"])
+        p = rng.standard_normal(sim.padded_shape)
+        rhs = rng.standard_normal(sim.padded_shape)
+        sim.set_field("p", p)
+        sim.set_field("rhs", rhs)
+        res = sim.solve()
+        pc = p.copy()
+        res_c = o.op_solve_mg_ref(g, v["omg"], levels, pre, post, pc, rhs)
+        assert res == pytest.approx(res_c, rel=1e-12)
+        assert rel_err(sim.field("p"), pc) < 1e-12
