@@ -1,0 +1,407 @@
+"""Benchmark of the NuSiF per-timestep hot path on GB300.
+
+Workload: the 3D lid-driven cavity at 256^3 cells (Re 1000, tau 0.5,
+donor-cell gamma 0.9), one time step per "step": CFL reduction, velocity
+boundary conditions, F/G/H, RHS, pressure solve, velocity update, all
+through the library's C ABI (reference src/main.c:61-79). The pressure solve
+is selected with --solver:
+  mg-mixed  FP32 V-cycles in FP64 iterative refinement to 1e-6 relative residual
+  mg        FP64 V-cycles to 1e-6 relative residual
+  rb        the reference's red-black SOR (omega 1.7, eps 1e-6, itermax 10000)
+
+Output: one JSON line (rank 0). ``value`` is device-timed ms per time step with
+the state resident in HBM (8 FP64 fields of 137 MB: inputs far larger than
+L2, so no flush is needed); ``e2e`` is the same step through the C ABI with
+u, v, w, p uploaded from and downloaded to pinned host buffers every step.
+
+``--impl reference`` times the reference's CPU implementation of the same
+step on this machine's host cores (the reference compiled from source in
+oracle/_ref when present, else the oracle's C restatement built with the
+reference's flags), on a bounded sample scaled to one time step.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "cfd-bench_gb300"))
+
+METRIC = "ms/timestep at 256^3 to 1e-6 residual: learned+FP32-MG vs FP64 MG; HBM GB/s"
+UNIT = "ms/timestep"
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+TRAFFIC = ROOT / "profiles" / "traffic.json"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--solver", default=os.environ.get("NUSIF_BENCH_SOLVER", "auto"))
+    ap.add_argument("--n", type=int, default=256, help="cells per axis of the cavity")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def hbm_peak():
+    try:
+        d = json.loads(PEAKS.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def bench_case(n: int, solver: str) -> dict:
+    from nusif.params import config2
+    vals = config2(solver=solver)
+    vals.update(imax=n, jmax=n, kmax=n)
+    return vals
+
+
+def pick_solver(requested: str) -> str:
+    if requested != "auto":
+        return requested
+    return "mg-mixed" if os.environ.get("NUSIF_BENCH_HAS_MG", "1") == "1" else "rb"
+
+
+# ---------------------------------------------------------------- GPU arm
+
+def run_gpu(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    import nusif
+    from nusif import abi
+
+    torch.cuda.set_device(local)
+    if world > 1 and not torch.distributed.is_initialized():
+        torch.distributed.init_process_group("nccl")
+    stream = torch.cuda.current_stream()
+    lib = nusif.load_library()
+    lib.nusifSetStream(C.c_void_p(stream.cuda_stream))
+
+    solver = pick_solver(args.solver)
+    vals = bench_case(args.n, solver)
+    try:
+        sim = nusif.Simulation(vals)
+    except nusif.NusifError:
+        if args.solver != "auto":
+            raise
+        solver = "rb"
+        vals = bench_case(args.n, solver)
+        sim = nusif.Simulation(vals)
+    i, j, k = sim.dims
+    ncell = i * j * k
+    padded = (i + 2) * (j + 2) * (k + 2)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        sim.step()
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = lib.nusifLaunchCount()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    infos = [sim.step() for _ in range(args.steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    launches = lib.nusifLaunchCount() - launches0
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_per_step = ms / args.steps
+    iters = [inf.it for inf in infos]
+    ress = [inf.res for inf in infos]
+
+    # ---- dominant kernel, timed live: the pressure smoother / SOR sweep ----
+    roof = dominant_kernel_roofline(sim, solver, stream, ncell, padded)
+
+    # ---- e2e: same step through the C ABI with host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(sim, args, stream, padded)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(vals, solver, iters)
+
+    sim.close()
+    if rank != 0:
+        return None
+    out = {
+        "metric": METRIC,
+        "value": ms_per_step / world,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64" if solver in ("rb", "mg", "mg-ref") else "f64+f32",
+        "data": "synthetic: lid-driven cavity from rest, no dataset",
+        "config": {"workload": f"lid-driven cavity {i}x{j}x{k}, Re 1000, tau 0.5, "
+                               f"solver {solver}",
+                   "cells": ncell, "solver": solver,
+                   "tolerance": "rtol 1e-6" if solver.startswith("mg") else "eps 1e-6 (RMS), itermax 10000",
+                   "l2": "no flush: 8 FP64 fields of %.0f MB each, far larger than L2" % (padded * 8 / 1e6),
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "solver_iterations_per_step": iters,
+        "residual_per_step": ress,
+        "roofline": roof,
+        "e2e": e2e,
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    return out
+
+
+def dominant_kernel_roofline(sim, solver, stream, ncell, padded):
+    """Average launch duration of the pressure smoother, from CUDA events."""
+    import torch
+    peak, src = hbm_peak()
+    s = sim.s
+    saved = (s.eps, s.itermax)
+    n_it = 40
+    if solver == "rb":
+        s.eps, s.itermax = 0.0, n_it
+        # warm the chunk size, then time exactly n_it iterations (2 launches each)
+        sim.solve()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.solve()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        s.eps, s.itermax = saved
+        launches = 2 * n_it
+        per_launch_ms = e0.elapsed_time(e1) / launches
+        kernel = "k_sor_pass (one colour of a red-black SOR iteration, FP64)"
+        # algorithmic bytes: p read + p write + rhs read = 24 B per cell per iteration
+        bytes_per_launch = 12.0 * ncell
+    else:
+        return {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
+                "traffic": None, "kernel": "multigrid smoother", "peak_source": src}
+    achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
+    traffic = None
+    try:
+        tr = json.loads(TRAFFIC.read_text())
+        entry = tr.get("k_sor_pass")
+        if entry:
+            traffic = entry["bytes_per_cell_per_launch"] * ncell
+    except Exception:
+        pass
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
+            "launch_ms": per_launch_ms, "algorithmic_bytes_per_launch": bytes_per_launch,
+            "peak_source": src,
+            "note": "FP64-pipe bound on GB300 (about 1.2 TFLOP/s FP64): see fp64 fields",
+            "fp64_instr_per_cell": 10,
+            "fp64_tflops_equiv": 20.0 * ncell / 2 / (per_launch_ms * 1e-3) / 1e12}
+
+
+def run_e2e(sim, args, stream, padded):
+    import numpy as np
+    import torch
+    from nusif import abi
+    host = {f: torch.empty(padded, dtype=torch.float64, pin_memory=True) for f in "uvwp"}
+    for f in "uvwp":
+        host[f].numpy()[:] = sim.field(f).reshape(-1)
+    lib = sim.lib
+    ptrs = {f: C.cast(host[f].data_ptr(), abi.c_double_p) for f in "uvwp"}
+    idx = abi.FIELD_INDEX
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for f in "uvwp":
+            lib.nusifUploadField(C.byref(sim.d), idx[f], ptrs[f])
+        sim.step()
+        for f in "uvwp":
+            lib.nusifDownloadField(C.byref(sim.d), idx[f], ptrs[f])
+    torch.cuda.synchronize()
+    abi.check(lib)
+    ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    return {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 4 * 8 * padded,
+            "d2h_bytes_per_step": 4 * 8 * padded,
+            "path": "C ABI: nusifUploadField x4, reference step calls, nusifDownloadField x4"}
+
+
+# ---------------------------------------------------------------- CPU side
+
+def cpu_step_estimate(vals, iters_per_step, fast=True):
+    """One time step of the reference algorithm on one host core, estimated
+    from a bounded sample: the non-solver operators once, plus a fixed number
+    of red-black iterations scaled to the per-step iteration count."""
+    import numpy as np
+    import oracle
+    kind = "port"
+    run = oracle.OracleRun(dict(vals, itermax=1), "rb", fast=fast)
+    lib = run.lib
+    st = run.st
+    g = st.g
+    n = int(np.prod(run.shape))
+    t0 = time.perf_counter()
+    # non-solver part of src/main.c:61-72,72: CFL, BCs, F/G/H, RHS, adaptUV
+    dt = lib.or_timestep(st.dtBound, g.dx, g.dy, g.dz, lib.or_max_abs(st.u, n),
+                         lib.or_max_abs(st.v, n), lib.or_max_abs(st.w, n), st.c.tau)
+    lib.or_set_bc(C.byref(g), st.c.bc, st.u, st.v, st.w)
+    lib.or_special_bc(C.byref(g), st.c.problem, C.c_double(st.c.lid), C.c_double(st.c.inflow), st.u)
+    d = C.c_double
+    lib.or_compute_fgh(C.byref(g), d(st.c.re), d(st.c.gamma), d(st.c.gx), d(st.c.gy), d(st.c.gz),
+                       d(dt), st.u, st.v, st.w, st.f, st.gf, st.h)
+    lib.or_compute_rhs(C.byref(g), d(dt), st.f, st.gf, st.h, st.rhs)
+    lib.or_adapt_uv(C.byref(g), d(dt), st.f, st.gf, st.h, st.p, st.u, st.v, st.w)
+    t_ns = time.perf_counter() - t0
+    sample_it = 8
+    res = C.c_double()
+    t0 = time.perf_counter()
+    lib.or_solve_rb(C.byref(g), 0.0, st.c.omega, sample_it, st.p, st.rhs, C.byref(res))
+    t_it = (time.perf_counter() - t0) / sample_it
+    run.close()
+    per_step = t_ns + iters_per_step * t_it
+    return per_step * 1e3, t_ns, t_it, kind, sample_it
+
+
+def cpu_baseline(vals, solver, gpu_iters):
+    import oracle
+    it = float(sum(gpu_iters)) / max(len(gpu_iters), 1) if solver == "rb" else float(vals["itermax"])
+    ms, t_ns, t_it, kind, sample_it = cpu_step_estimate(vals, it)
+    return {"value": ms, "unit": UNIT, "cores": 1, "kind": kind,
+            "sample": (f"one pass of the non-solver operators ({t_ns:.2f} s) plus {sample_it} "
+                       f"red-black SOR iterations ({t_it * 1e3:.1f} ms each) at "
+                       f"{vals['imax']}^3 on one host core, scaled to {it:.0f} iterations per "
+                       f"step (the reference's red-black solve for this case)")}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    solver = pick_solver(args.solver)
+    vals = bench_case(args.n, solver)
+    it = float(vals["itermax"])
+    samples = []
+    for s in range(args.warmup + args.steps):
+        ms, t_ns, t_it, kind, sample_it = cpu_step_estimate(vals, it)
+        if s >= args.warmup:
+            samples.append(ms)
+    ms = sum(samples) / len(samples)
+    n = vals["imax"]
+    return {
+        "impl": "reference",
+        "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: lid-driven cavity from rest, no dataset",
+        "config": {"workload": f"lid-driven cavity {n}x{n}x{n}, Re 1000, tau 0.5, "
+                               f"reference red-black SOR solve (omega 1.7, eps 1e-6, itermax 10000)",
+                   "cells": n ** 3, "solver": "rb (reference)"},
+        "cpu_baseline": {"value": ms, "unit": UNIT, "cores": 1, "kind": kind,
+                         "sample": (f"per step: the non-solver operators once plus {sample_it} "
+                                    f"red-black iterations, scaled to {it:.0f} iterations "
+                                    f"(the reference's own C code path compiled with "
+                                    f"-O3 -ffast-math, sequential)")},
+        "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        out = run_gpu(args, rank, world, local)
+    if out is not None and rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

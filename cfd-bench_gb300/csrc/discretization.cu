@@ -316,8 +316,6 @@ dim3 cell_grid(const Dims &g, dim3 blk)
 
 const dim3 kCellBlock(64, 2, 2);
 
-bool launched(const char *what) { return cuda_ok(cudaGetLastError(), what); }
-
 }  // namespace
 
 // ---- launchers ----

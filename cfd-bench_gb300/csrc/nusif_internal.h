@@ -14,6 +14,8 @@ void fail(int code, const char *fmt, ...);  // records or exits per error mode
 bool cuda_ok(cudaError_t e, const char *what);  // false after recording a failure
 bool has_error();                              // an error is pending (record mode)
 cudaStream_t stream();
+// after every kernel launch: counts it and checks the launch error
+bool launched(const char *what);
 
 // ---- problem kinds and solver kinds ----
 enum Problem { PROBLEM_NONE = 0, PROBLEM_DCAVITY = 1, PROBLEM_CANAL = 2 };

@@ -46,6 +46,14 @@ bool has_error() { return g_error_code != 0; }
 
 cudaStream_t stream() { return g_stream; }
 
+static unsigned long long g_launches = 0;
+
+bool launched(const char *what)
+{
+  g_launches++;
+  return cuda_ok(cudaGetLastError(), what);
+}
+
 bool reduce_scratch_alloc(ReduceScratch &r, int capacity)
 {
   if (r.capacity >= capacity) return true;
@@ -167,6 +175,8 @@ int nusifUploadField(Discretization *d, int which, const double *host)
   if (!cuda_ok(cudaStreamSynchronize(g_stream), "upload field sync")) return NUSIF_ERR_CUDA;
   return NUSIF_OK;
 }
+
+unsigned long long nusifLaunchCount(void) { return g_launches; }
 
 const char *nusifVersion(void) { return "nusif-gb300 1.0 (sm_103a)"; }
 

@@ -212,8 +212,6 @@ int sor_blocks(const SorArgs &A)
   return (int)(gr.x * gr.y * gr.z);
 }
 
-static bool launched(const char *what) { return cuda_ok(cudaGetLastError(), what); }
-
 bool launch_rb_iteration(const SorArgs &A, double *p, const double *rhs, SolveState *st,
     ReduceScratch &red)
 {

@@ -94,6 +94,7 @@ SIGNATURES = [
     ("nusifParameterSet", C.c_int, [C.POINTER(Parameter), C.c_char_p, C.c_char_p]),
     ("nusifFreeDiscretization", None, [C.POINTER(Discretization)]),
     ("nusifFreeSolver", None, [C.POINTER(Solver)]),
+    ("nusifLaunchCount", C.c_ulonglong, []),
     ("nusifVersion", C.c_char_p, []),
 ]
 

@@ -166,6 +166,8 @@ NUSIF_API int nusifParameterSet(Parameter *param, const char *key, const char *v
 /* release device memory of a discretization / solver (the reference never frees) */
 NUSIF_API void nusifFreeDiscretization(Discretization *d);
 NUSIF_API void nusifFreeSolver(Solver *s);
+/* kernels this library launched since it was loaded (observability) */
+NUSIF_API unsigned long long nusifLaunchCount(void);
 /* library version string */
 NUSIF_API const char *nusifVersion(void);
 

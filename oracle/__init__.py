@@ -24,6 +24,8 @@ REF_DIR = HERE / "_ref"
 LIB_STRICT = HERE / "liboracle.so"
 LIB_FAST = HERE / "liboracle_fast.so"
 SRC = HERE / "nusif_oracle.c"
+SOURCES = [SRC, HERE / "nusif_oracle_mg.c"]
+DEPS = SOURCES + [HERE / "nusif_oracle.h", HERE / "nusif_oracle_mg.inc"]
 
 # strict: no fast-math, no FMA contraction (bit-for-bit pin against the
 # reference's strict build); fast: the reference's own -O3 -ffast-math
@@ -39,11 +41,11 @@ def build(force: bool = False) -> None:
     cc = os.environ.get("CC", "gcc")
     for lib, opt in FLAGS.items():
         if not force and lib.exists() and lib.stat().st_mtime >= max(
-                SRC.stat().st_mtime, (HERE / "nusif_oracle.h").stat().st_mtime):
+                d.stat().st_mtime for d in DEPS):
             continue
         tmp = lib.with_suffix(".so.tmp")
-        subprocess.run([cc, "-std=c99", "-shared", "-fPIC", *opt, "-o", str(tmp), str(SRC), "-lm"],
-                       check=True)
+        subprocess.run([cc, "-std=c99", "-shared", "-fPIC", *opt, "-o", str(tmp),
+                        *map(str, SOURCES), "-lm"], check=True)
         os.replace(tmp, lib)
 
 
@@ -96,6 +98,11 @@ def load(fast: bool = False) -> C.CDLL:
     lib.or_solve_mg_ref.restype = C.c_double
     lib.or_solve_mg_ref.argtypes = [C.POINTER(OrGrid), C.c_double, C.c_int, C.c_int, C.c_int,
                                     d_p, d_p]
+    lib.or_mg_solve.restype = C.c_int
+    lib.or_mg_solve.argtypes = [C.POINTER(OrGrid), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                C.c_int, C.c_double, d_p, d_p, d_p]
+    lib.or_mg_levels.restype = C.c_int
+    lib.or_mg_levels.argtypes = [C.POINTER(OrGrid), C.c_int, C.POINTER(C.c_int)]
     lib.or_state_init.argtypes = [C.POINTER(OrState), C.POINTER(OrCase)]
     lib.or_state_step.argtypes = [C.POINTER(OrState), d_p]
     lib.or_state_step.restype = C.c_int
@@ -286,3 +293,18 @@ def op_solve_rb(g: OrGrid, eps, omega, itermax, p, rhs):
 def op_solve_mg_ref(g: OrGrid, omega, levels, presmooth, postsmooth, p, rhs) -> float:
     return load().or_solve_mg_ref(C.byref(g), omega, levels, presmooth, postsmooth, ptr(p),
                                   ptr(rhs))
+
+
+def op_mg_solve(g: OrGrid, mode: str, p, rhs, rtol=1e-6, pre=2, post=2, coarse_sweeps=64,
+                maxcycles=100, level_cap=0):
+    """The library's corrected V-cycle solvers ("mg": FP64, "mg-mixed": FP32 in FP64)."""
+    rel = C.c_double()
+    cyc = load().or_mg_solve(C.byref(g), {"mg": 0, "mg-mixed": 1}[mode], level_cap, pre, post,
+                             coarse_sweeps, maxcycles, rtol, ptr(p), ptr(rhs), C.byref(rel))
+    return cyc, rel.value
+
+
+def op_mg_levels(g: OrGrid, cap: int = 0):
+    dims = (C.c_int * 48)()
+    n = load().or_mg_levels(C.byref(g), cap, dims)
+    return [tuple(dims[3 * l:3 * l + 3]) for l in range(n)]

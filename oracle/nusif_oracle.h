@@ -64,6 +64,13 @@ void or_pressure_ghosts(const OrGrid *g, double *p);
 double or_solve_mg_ref(const OrGrid *g, double omega, int levels, int presmooth,
     int postsmooth, double *p, const double *rhs);
 
+/* geometric multigrid of the library (nusif_oracle_mg.c): level count and
+ * dims (3 ints per level), and the solve; mode 0 = FP64, 1 = FP32 in FP64
+ * iterative refinement. Returns V-cycles; *relres = ||b-Ap||/||b||. */
+int or_mg_levels(const OrGrid *g, int cap, int *dims_out);
+int or_mg_solve(const OrGrid *g, int mode, int level_cap, int pre, int post, int coarse_sweeps,
+    int maxcycles, double rtol, double *p, const double *rhs, double *relres);
+
 /* whole-run driver mirroring reference src/main.c:53-88 */
 typedef struct {
   int imax, jmax, kmax;

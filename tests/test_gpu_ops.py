@@ -74,9 +74,11 @@ BCS = [(1, 1, 1, 1, 1, 1), (2, 3, 2, 1, 3, 4), (3, 3, 1, 1, 2, 2)]
 def _case(dims, bc, name="dcavity", **over):
     from nusif.params import cavity
     keys = ("bcLeft", "bcRight", "bcBottom", "bcTop", "bcFront", "bcBack")
-    return cavity(dims, xlength=1.1, ylength=0.8, zlength=1.3, name=name, re=300.0,
-                  gamma=0.85, gx=0.05, gy=-0.1, gz=0.02, tau=0.5, te=1e9, omg=1.7,
-                  eps=1e-6, itermax=25, **dict(zip(keys, bc)), **over)
+    base = dict(xlength=1.1, ylength=0.8, zlength=1.3, name=name, re=300.0, gamma=0.85,
+                gx=0.05, gy=-0.1, gz=0.02, tau=0.5, te=1e9, omg=1.7, eps=1e-6, itermax=25)
+    base.update(zip(keys, bc))
+    base.update(over)
+    return cavity(dims, **base)
 
 
 @pytest.mark.parametrize("dims", SIZES)
