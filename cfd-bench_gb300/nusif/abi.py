@@ -94,6 +94,9 @@ SIGNATURES = [
     ("nusifParameterSet", C.c_int, [C.POINTER(Parameter), C.c_char_p, C.c_char_p]),
     ("nusifFreeDiscretization", None, [C.POINTER(Discretization)]),
     ("nusifFreeSolver", None, [C.POINTER(Solver)]),
+    ("nusifSolveRBStatic", C.c_int, [c_double_p, c_double_p, C.c_int, C.c_int, C.c_int,
+                                     C.c_double, C.c_double, C.c_double, C.c_double,
+                                     C.c_double, C.c_int, c_double_p, C.POINTER(C.c_int)]),
     ("nusifLaunchCount", C.c_ulonglong, []),
     ("nusifVersion", C.c_char_p, []),
 ]

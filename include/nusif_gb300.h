@@ -166,6 +166,19 @@ NUSIF_API int nusifParameterSet(Parameter *param, const char *key, const char *v
 /* release device memory of a discretization / solver (the reference never frees) */
 NUSIF_API void nusifFreeDiscretization(Discretization *d);
 NUSIF_API void nusifFreeSolver(Solver *s);
+/* Red-black SOR solve that allocates no memory. No counterpart in the
+ * reference. Same result as solve() with the rb solver on the same p, rhs
+ * (device arrays in the padded layout) and parameters, for callers that cannot
+ * call cudaMalloc (a CUDA graph under capture, hosts that forbid device
+ * allocation after start-up). Its scratch is a fixed 256.5 KiB __device__
+ * array of the library: grids needing more than 32768 per-block partial sums
+ * (larger than about 512^3 cells) are rejected with NUSIF_ERR_ARG. The first call on a device
+ * looks up that array's address and should come before any stream capture.
+ * Calls share the array: calls that overlap on the GPU race. Returns a
+ * NUSIF_* code; *res_out and *it_out get solve()'s residual and iterations. */
+NUSIF_API int nusifSolveRBStatic(double *p, const double *rhs, int imax, int jmax, int kmax,
+    double dx, double dy, double dz, double omega, double eps, int itermax, double *res_out,
+    int *it_out);
 /* kernels this library launched since it was loaded (observability) */
 NUSIF_API unsigned long long nusifLaunchCount(void);
 /* library version string */
