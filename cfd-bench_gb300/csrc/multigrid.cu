@@ -1,36 +1,744 @@
-// Geometric multigrid V-cycle solvers (kinds mg and mg-mixed).
+// Geometric multigrid pressure solvers (solver kinds "mg" and "mg-mixed").
+//
+// The reference's multigrid (src/solver-mg.c:299-402) never applies its
+// coarse-grid correction and, sequentially, never coarsens; these solvers are
+// the corrected algorithm (its CPU restatement: oracle/nusif_oracle_mg.c):
+//  - levels: an axis is halved while its size is even and >= 16;
+//  - operator: 7-point Laplacian, homogeneous Neumann walls applied without
+//    ghost cells (a neighbour outside the domain is the cell itself);
+//  - smoother: red-black Gauss-Seidel, odd cells first, x -= r / diag;
+//  - restriction: average of the children of the residual; prolongation:
+//    trilinear (3/4, 1/4 per coarsened axis), added to x;
+//  - V(pre, post) cycles; coarsest level: fixed sweeps from zero, in shared
+//    memory by one block;
+//  - right-hand side made mean-free; stop at ||b - Ap|| <= rtol ||b||.
+//  mg:       all FP64, p itself is the fine-level unknown; the residual norm
+//            is folded in the fine restriction after pre-smoothing.
+//  mg-mixed: FP64 residual of p (norm, mean shift) -> FP32 V-cycle for the
+//            correction from zero -> p += e in FP64, fused into the last
+//            fine post-smoothing pass (iterative refinement).
+// Every kernel returns at once when the device-side done flag is up, so the
+// host queues whole cycles in chunks and reads the state once per chunk.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include "nusif_internal.h"
+#include "reduce.cuh"
 #include "solver_internal.h"
 
 namespace nusif {
 
-struct MgHierarchy {
-  int levels = 0;
+constexpr int kMaxLevels = 16;
+
+struct MgState {
+  double shift;  // mean of the right-hand side
+  double nb2;    // ||rhs - shift||^2
+  double res2;   // last ||b - Ap||^2
+  double tol2;   // rtol^2 * nb2
+  double rtol2;
+  int cycles;    // V-cycles counted by the stop test
+  int maxcycles;
+  int done;
+  int pad;
 };
+
+struct MgLevelDesc {
+  int n[3];
+  int r[3];  // coarsening ratio from the finer level
+  double ih2[3];
+};
+
+// A level's array view: interior cell (i,j,k), 0-based, lives at
+// off + i + j*sy + k*sz (padded reference layout for p/rhs, compact otherwise).
+template <typename T>
+struct View {
+  T *x;
+  const T *b;
+  int nx, ny, nz;
+  int sy, sz, off;
+  T ex, ey, ez, diag, inv_diag;
+};
+
+struct MgHierarchy {
+  int nl = 0;
+  int mode = 0;  // 0 mg, 1 mg-mixed
+  MgLevelDesc lv[kMaxLevels];
+  double *x64[kMaxLevels] = {};
+  double *b64[kMaxLevels] = {};
+  float *x32[kMaxLevels] = {};
+  float *b32[kMaxLevels] = {};
+  MgState *d_state = nullptr;
+  MgState *h_state = nullptr;
+  ReduceScratch red;
+  int pre = 2, post = 2, coarse_sweeps = 64, maxcycles = 100;
+  double rtol = 1e-6;
+  int last_cycles = 0;
+  double *h_ptrs[2 * kMaxLevels] = {};  // exposed through Solver::r / Solver::e
+};
+
+namespace {
+
+constexpr int kBX = 32, kBY = 8, kNT = kBX * kBY;
+
+__device__ __forceinline__ bool mg_done(const MgState *st)
+{
+  return *reinterpret_cast<const volatile int *>(&st->done) != 0;
+}
+
+template <typename T>
+__device__ __forceinline__ T lap_at(const View<T> &v, const T *x, int i, int j, int k, int64_t c,
+    T xc)
+{
+  const T sx = (i > 0 ? x[c - 1] : xc) + (i < v.nx - 1 ? x[c + 1] : xc);
+  const T sy = (j > 0 ? x[c - v.sy] : xc) + (j < v.ny - 1 ? x[c + v.sy] : xc);
+  const T sz = (k > 0 ? x[c - v.sz] : xc) + (k < v.nz - 1 ? x[c + v.sz] : xc);
+  return sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
+}
+
+// One colour of a red-black Gauss-Seidel sweep. ZERO: the sweep starts from
+// x = 0 (the centre is not read; in the odd pass neither are neighbours).
+// FOLD: after the update, p += x for both cells of the pair and the Neumann
+// ghosts of p are refreshed (mixed precision, last fine pass).
+template <typename T, bool ZERO, bool FOLD>
+__global__ void __launch_bounds__(kNT) k_mg_smooth(View<T> v, int colour, const double *shift,
+    int kb, const MgState *st, double *p, int p_sj, int p_sk)
+{
+  if (mg_done(st)) return;
+  const int t = blockIdx.x * kBX + threadIdx.x;
+  const int j = blockIdx.y * kBY + threadIdx.y;
+  const int k0 = blockIdx.z * kb;
+  if (j >= v.ny) return;
+  const T sh = shift ? (T)(*shift) : (T)0;
+  const int k1 = min(k0 + kb, v.nz);
+  for (int k = k0; k < k1; k++) {
+    const int i = 2 * t + (((j + k + 1) & 1) == colour ? 0 : 1);
+    const int64_t row = v.off + (int64_t)k * v.sz + (int64_t)j * v.sy;
+    if (i < v.nx) {
+      const int64_t c = row + i;
+      T r;
+      if (ZERO && colour == 1) {
+        r = v.b[c] - sh;
+        v.x[c] = -r * v.inv_diag;
+      } else {
+        const T xc = ZERO ? (T)0 : v.x[c];
+        r = (v.b[c] - sh) - lap_at(v, v.x, i, j, k, c, xc);
+        v.x[c] = xc - r * v.inv_diag;
+      }
+    }
+    if (FOLD) {
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        const int ii = 2 * t + e;
+        if (ii >= v.nx) continue;
+        const double val = (double)v.x[row + ii];
+        const int64_t pc = (int64_t)(k + 1) * p_sk + (int64_t)(j + 1) * p_sj + (ii + 1);
+        const double np = p[pc] + val;
+        p[pc] = np;
+        if (ii == 0) p[pc - 1] = np;
+        if (ii == v.nx - 1) p[pc + 1] = np;
+        if (j == 0) p[pc - p_sj] = np;
+        if (j == v.ny - 1) p[pc + p_sj] = np;
+        if (k == 0) p[pc - p_sk] = np;
+        if (k == v.nz - 1) p[pc + p_sk] = np;
+      }
+    }
+  }
+}
+
+// Residual of the fine level averaged into the coarse right-hand side. One
+// thread per coarse cell. ACCUM: also sum r^2 (FP64) and let the last block
+// fold the partials and take the stop decision.
+template <typename T, bool ACCUM>
+__global__ void __launch_bounds__(kNT) k_mg_restrict(View<T> f, T *bc, int cnx, int cny, int cnz,
+    int rx, int ry, int rz, T inv_count, const double *shift, MgState *st,
+    double *partials, unsigned *ticket)
+{
+  if (mg_done(st)) return;
+  const int64_t ncoarse = (int64_t)cnx * cny * cnz;
+  const T sh = shift ? (T)(*shift) : (T)0;
+  double acc = 0.0;
+  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < ncoarse;
+       q += (int64_t)gridDim.x * kNT) {
+    const int I = (int)(q % cnx);
+    const int64_t rest = q / cnx;
+    const int J = (int)(rest % cny);
+    const int K = (int)(rest / cny);
+    T sum = 0;
+    for (int dk = 0; dk < rz; dk++)
+      for (int dj = 0; dj < ry; dj++)
+        for (int di = 0; di < rx; di++) {
+          const int i = I * rx + di, j = J * ry + dj, k = K * rz + dk;
+          const int64_t c = f.off + (int64_t)k * f.sz + (int64_t)j * f.sy + i;
+          const T r = (f.b[c] - sh) - lap_at(f, f.x, i, j, k, c, f.x[c]);
+          sum += r;
+          if (ACCUM) acc += (double)r * (double)r;
+        }
+    if (bc) bc[q] = sum * inv_count;
+  }
+  if (!ACCUM) return;
+  __shared__ double sm[kNT / 32];
+  acc = block_reduce_sum<kNT>(acc, sm);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = acc;
+    last = ticket_is_last(ticket);
+  }
+  __syncthreads();
+  if (!last) return;
+  const double total = fold_partials<kNT>(partials, gridDim.x, sm);
+  if (threadIdx.x == 0) {
+    st->res2 = total;
+    const int c = st->cycles + 1;
+    st->cycles = c;
+    st->done = (total <= st->tol2) || (c >= st->maxcycles);
+    *ticket = 0;
+  }
+}
+
+// FP64 residual of p (padded layout) into the FP32 fine right-hand side, with
+// its FP64 norm folded by the last block (mixed precision stop test).
+__global__ void __launch_bounds__(kNT) k_mx_residual(View<double> f, float *r32, MgState *st,
+    double *partials, unsigned *ticket)
+{
+  if (mg_done(st)) return;
+  const int64_t n = (int64_t)f.nx * f.ny * f.nz;
+  const double sh = st->shift;
+  double acc = 0.0;
+  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * kNT) {
+    const int i = (int)(q % f.nx);
+    const int64_t rest = q / f.nx;
+    const int j = (int)(rest % f.ny);
+    const int k = (int)(rest / f.ny);
+    const int64_t c = f.off + (int64_t)k * f.sz + (int64_t)j * f.sy + i;
+    const double r = (f.b[c] - sh) - lap_at(f, f.x, i, j, k, c, f.x[c]);
+    r32[q] = (float)r;
+    acc += r * r;
+  }
+  __shared__ double sm[kNT / 32];
+  acc = block_reduce_sum<kNT>(acc, sm);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = acc;
+    last = ticket_is_last(ticket);
+  }
+  __syncthreads();
+  if (!last) return;
+  const double total = fold_partials<kNT>(partials, gridDim.x, sm);
+  if (threadIdx.x == 0) {
+    st->res2 = total;
+    const int c = st->cycles;  // V-cycles completed before this residual
+    st->done = (total <= st->tol2) || (c >= st->maxcycles);
+    st->cycles = c + (st->done ? 0 : 1);
+    *ticket = 0;
+  }
+}
+
+// x_f += trilinear interpolation of x_c; one thread per fine cell
+template <typename T>
+__global__ void __launch_bounds__(kNT) k_mg_prolong(View<T> f, const T *xc, int cnx, int cny,
+    int cnz, int rx, int ry, int rz, const MgState *st)
+{
+  if (mg_done(st)) return;
+  const int64_t n = (int64_t)f.nx * f.ny * f.nz;
+  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * kNT) {
+    const int fi[3] = { (int)(q % f.nx), (int)((q / f.nx) % f.ny), (int)(q / ((int64_t)f.nx * f.ny)) };
+    const int cn[3] = { cnx, cny, cnz };
+    const int rr[3] = { rx, ry, rz };
+    int P[3], Q[3];
+    T w[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      if (rr[a] == 2) {
+        P[a] = fi[a] >> 1;
+        const int nb = (fi[a] & 1) ? P[a] + 1 : P[a] - 1;
+        Q[a] = (nb < 0 || nb >= cn[a]) ? P[a] : nb;
+        w[a] = (T)0.25;
+      } else {
+        P[a] = fi[a];
+        Q[a] = fi[a];
+        w[a] = (T)0;
+      }
+    }
+    const int64_t sy = cnx, sz = (int64_t)cnx * cny;
+    T v[2][2];
+#pragma unroll
+    for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+      for (int dy = 0; dy < 2; dy++) {
+        const int64_t base = (int64_t)(dz ? Q[2] : P[2]) * sz + (int64_t)(dy ? Q[1] : P[1]) * sy;
+        const T a0 = xc[base + P[0]], a1 = xc[base + Q[0]];
+        v[dz][dy] = a0 + w[0] * (a1 - a0);
+      }
+    const T y0 = v[0][0] + w[1] * (v[0][1] - v[0][0]);
+    const T y1 = v[1][0] + w[1] * (v[1][1] - v[1][0]);
+    const int64_t c = f.off + (int64_t)fi[2] * f.sz + (int64_t)fi[1] * f.sy + fi[0];
+    f.x[c] += y0 + w[2] * (y1 - y0);
+  }
+}
+
+// Coarsest level: `sweeps` red-black Gauss-Seidel sweeps from zero by one
+// block, the level held in shared memory (compact layout).
+template <typename T>
+__global__ void __launch_bounds__(512) k_mg_coarse(View<T> v, int sweeps, const MgState *st)
+{
+  if (mg_done(st)) return;
+  extern __shared__ unsigned char smem_raw[];
+  T *xs = reinterpret_cast<T *>(smem_raw);
+  T *bs = xs + (int64_t)v.nx * v.ny * v.nz;
+  const int n = v.nx * v.ny * v.nz;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    xs[q] = 0;
+    bs[q] = v.b[q];
+  }
+  __syncthreads();
+  View<T> s = v;
+  s.x = xs;
+  s.sy = v.nx;
+  s.sz = v.nx * v.ny;
+  s.off = 0;
+  for (int it = 0; it < sweeps; it++) {
+    for (int colour = 1; colour >= 0; colour--) {
+      for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int i = q % v.nx, j = (q / v.nx) % v.ny, k = q / (v.nx * v.ny);
+        if (((i + j + k + 3) & 1) != colour) continue;
+        const T xc = xs[q];
+        const T r = bs[q] - lap_at(s, xs, i, j, k, q, xc);
+        xs[q] = xc - r * s.inv_diag;
+      }
+      __syncthreads();
+    }
+  }
+  for (int q = threadIdx.x; q < n; q += blockDim.x) v.x[q] = xs[q];
+}
+
+// mean of the right-hand side, then ||rhs - mean||^2; initialises the state
+__global__ void __launch_bounds__(kNT) k_mg_rhs_sum(View<double> f, MgState *st,
+    double *partials, unsigned *ticket)
+{
+  const int64_t n = (int64_t)f.nx * f.ny * f.nz;
+  double acc = 0.0;
+  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * kNT) {
+    const int i = (int)(q % f.nx);
+    const int64_t rest = q / f.nx;
+    const int64_t c = f.off + (rest / f.ny) * f.sz + (rest % f.ny) * f.sy + i;
+    acc += f.b[c];
+  }
+  __shared__ double sm[kNT / 32];
+  acc = block_reduce_sum<kNT>(acc, sm);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = acc;
+    last = ticket_is_last(ticket);
+  }
+  __syncthreads();
+  if (!last) return;
+  const double total = fold_partials<kNT>(partials, gridDim.x, sm);
+  if (threadIdx.x == 0) {
+    st->shift = total / (double)n;
+    *ticket = 0;
+  }
+}
+
+__global__ void __launch_bounds__(kNT) k_mg_rhs_norm(View<double> f, MgState *st,
+    double *partials, unsigned *ticket)
+{
+  const int64_t n = (int64_t)f.nx * f.ny * f.nz;
+  const double sh = st->shift;
+  double acc = 0.0;
+  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * kNT) {
+    const int i = (int)(q % f.nx);
+    const int64_t rest = q / f.nx;
+    const int64_t c = f.off + (rest / f.ny) * f.sz + (rest % f.ny) * f.sy + i;
+    const double b = f.b[c] - sh;
+    acc += b * b;
+  }
+  __shared__ double sm[kNT / 32];
+  acc = block_reduce_sum<kNT>(acc, sm);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = acc;
+    last = ticket_is_last(ticket);
+  }
+  __syncthreads();
+  if (!last) return;
+  const double total = fold_partials<kNT>(partials, gridDim.x, sm);
+  if (threadIdx.x == 0) {
+    st->nb2 = total;
+    st->tol2 = st->rtol2 * total;
+    st->res2 = 0.0;
+    st->cycles = 0;
+    st->done = (total == 0.0);
+    *ticket = 0;
+  }
+}
+
+// ---------------------------------------------------------------- host side
+
+int sm_count_mg()
+{
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+int build_levels(const Grid *gr, int cap, MgLevelDesc *lv)
+{
+  double h[3] = { gr->dx, gr->dy, gr->dz };
+  lv[0].n[0] = gr->imax;
+  lv[0].n[1] = gr->jmax;
+  lv[0].n[2] = gr->kmax;
+  for (int a = 0; a < 3; a++) {
+    lv[0].r[a] = 1;
+    lv[0].ih2[a] = 1.0 / (h[a] * h[a]);
+  }
+  int nl = 1;
+  while (nl < kMaxLevels && (cap <= 0 || nl < cap)) {
+    MgLevelDesc &f = lv[nl - 1], &c = lv[nl];
+    bool any = false;
+    for (int a = 0; a < 3; a++) {
+      if (f.n[a] % 2 == 0 && f.n[a] >= 16) {
+        c.n[a] = f.n[a] / 2;
+        c.r[a] = 2;
+        h[a] *= 2.0;
+        any = true;
+      } else {
+        c.n[a] = f.n[a];
+        c.r[a] = 1;
+      }
+      c.ih2[a] = 1.0 / (h[a] * h[a]);
+    }
+    if (!any) break;
+    nl++;
+  }
+  return nl;
+}
+
+template <typename T>
+View<T> compact_view(const MgLevelDesc &L, T *x, const T *b)
+{
+  View<T> v;
+  v.x = x;
+  v.b = b;
+  v.nx = L.n[0];
+  v.ny = L.n[1];
+  v.nz = L.n[2];
+  v.sy = L.n[0];
+  v.sz = L.n[0] * L.n[1];
+  v.off = 0;
+  const double d = 2.0 * (L.ih2[0] + L.ih2[1] + L.ih2[2]);
+  v.ex = (T)L.ih2[0];
+  v.ey = (T)L.ih2[1];
+  v.ez = (T)L.ih2[2];
+  v.diag = (T)d;
+  v.inv_diag = (T)(1.0 / d);
+  return v;
+}
+
+View<double> padded_view(const MgLevelDesc &L, double *x, const double *b)
+{
+  View<double> v = compact_view<double>(L, x, b);
+  v.sy = L.n[0] + 2;
+  v.sz = (L.n[0] + 2) * (L.n[1] + 2);
+  v.off = 1 + v.sy + v.sz;
+  return v;
+}
+
+int planes_per_block(int nx, int ny, int nz)
+{
+  const int gx = ((nx + 1) / 2 + kBX - 1) / kBX, gy = (ny + kBY - 1) / kBY;
+  int kb = 16;
+  while (kb > 1 && (int64_t)gx * gy * ((nz + kb - 1) / kb) < 4 * sm_count_mg()) kb >>= 1;
+  return kb;
+}
+
+template <typename T, bool ZERO, bool FOLD>
+bool smooth_pass(const View<T> &v, int colour, const double *shift, const MgState *st,
+    double *p = nullptr)
+{
+  const int kb = planes_per_block(v.nx, v.ny, v.nz);
+  dim3 grid(((v.nx + 1) / 2 + kBX - 1) / kBX, (v.ny + kBY - 1) / kBY, (v.nz + kb - 1) / kb);
+  const int p_sj = v.nx + 2, p_sk = (v.nx + 2) * (v.ny + 2);
+  k_mg_smooth<T, ZERO, FOLD><<<grid, dim3(kBX, kBY), 0, stream()>>>(v, colour, shift, kb, st, p,
+      p_sj, p_sk);
+  return launched("k_mg_smooth");
+}
+
+// `count` sweeps; the first from zero when zero_first; the last even pass
+// folds into p when p != nullptr
+template <typename T>
+bool sweeps(const View<T> &v, int count, bool zero_first, const double *shift,
+    const MgState *st, double *p = nullptr)
+{
+  for (int s = 0; s < count; s++) {
+    const bool z = zero_first && s == 0;
+    const bool fold = p != nullptr && s == count - 1;
+    bool ok = z ? smooth_pass<T, true, false>(v, 1, shift, st)
+                : smooth_pass<T, false, false>(v, 1, shift, st);
+    if (!ok) return false;
+    if (fold)
+      ok = z ? smooth_pass<T, true, true>(v, 0, shift, st, p)
+             : smooth_pass<T, false, true>(v, 0, shift, st, p);
+    else
+      ok = z ? smooth_pass<T, true, false>(v, 0, shift, st)
+             : smooth_pass<T, false, false>(v, 0, shift, st);
+    if (!ok) return false;
+  }
+  return true;
+}
+
+int flat_blocks(int64_t n)
+{
+  int64_t b = (n + kNT - 1) / kNT;
+  const int64_t cap = 8 * (int64_t)sm_count_mg();
+  return (int)(b < cap ? (b > 0 ? b : 1) : cap);
+}
+
+template <typename T, bool ACCUM>
+bool restrict_to(const View<T> &f, T *bc, const MgLevelDesc &C, const double *shift, MgState *st,
+    ReduceScratch &red)
+{
+  const int64_t nc = (int64_t)C.n[0] * C.n[1] * C.n[2];
+  const int blocks = flat_blocks(nc);
+  if (ACCUM && red.capacity < blocks) {
+    fail(NUSIF_ERR_STATE, "multigrid reduction scratch too small");
+    return false;
+  }
+  const T inv = (T)(1.0 / (C.r[0] * C.r[1] * C.r[2]));
+  k_mg_restrict<T, ACCUM><<<blocks, kNT, 0, stream()>>>(f, bc, C.n[0], C.n[1], C.n[2], C.r[0],
+      C.r[1], C.r[2], inv, shift, st, red.partials, red.ticket);
+  return launched("k_mg_restrict");
+}
+
+template <typename T>
+bool prolong_to(const View<T> &f, const T *xc, const MgLevelDesc &C, const MgState *st)
+{
+  const int64_t nf = (int64_t)f.nx * f.ny * f.nz;
+  k_mg_prolong<T><<<flat_blocks(nf), kNT, 0, stream()>>>(f, xc, C.n[0], C.n[1], C.n[2], C.r[0],
+      C.r[1], C.r[2], st);
+  return launched("k_mg_prolong");
+}
+
+template <typename T>
+bool coarse_solve(const View<T> &v, int nsweeps, const MgState *st)
+{
+  const size_t n = (size_t)v.nx * v.ny * v.nz;
+  const size_t bytes = 2 * n * sizeof(T);
+  if (bytes <= 48 * 1024) {
+    k_mg_coarse<T><<<1, 512, bytes, stream()>>>(v, nsweeps, st);
+    return launched("k_mg_coarse");
+  }
+  // larger coarsest grids: sweeps in global memory
+  if (nsweeps == 0) return cuda_ok(cudaMemsetAsync(v.x, 0, n * sizeof(T), stream()), "zero x");
+  return sweeps<T>(v, nsweeps, true, nullptr, st);
+}
+
+// V-cycle from level l (x_l starts at zero) on the arrays xs/bs of type T
+template <typename T>
+bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, double *fold_p)
+{
+  const MgLevelDesc &L = H->lv[l];
+  View<T> v = compact_view<T>(L, xs[l], bs[l]);
+  const size_t n = (size_t)L.n[0] * L.n[1] * L.n[2];
+  MgState *st = H->d_state;
+  if (l == H->nl - 1) {
+    if (!coarse_solve<T>(v, H->coarse_sweeps, st)) return false;
+  } else {
+    if (H->pre > 0) {
+      if (!sweeps<T>(v, H->pre, true, nullptr, st)) return false;
+    } else if (!cuda_ok(cudaMemsetAsync(xs[l], 0, n * sizeof(T), stream()), "zero x")) {
+      return false;
+    }
+    if (!restrict_to<T, false>(v, bs[l + 1], H->lv[l + 1], nullptr, st, H->red)) return false;
+    if (!vcycle<T>(H, l + 1, xs, bs, nullptr)) return false;
+    if (!prolong_to<T>(v, xs[l + 1], H->lv[l + 1], st)) return false;
+    if (!sweeps<T>(v, H->post, false, nullptr, st, fold_p)) return false;
+    return true;
+  }
+  return true;
+}
+
+// p += e (FP64) and Neumann ghosts, for mixed precision without post-smoothing
+__global__ void k_mx_fold(View<float> e, double *p, int p_sj, int p_sk, const MgState *st)
+{
+  if (mg_done(st)) return;
+  const int64_t n = (int64_t)e.nx * e.ny * e.nz;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % e.nx), j = (int)((q / e.nx) % e.ny), k = (int)(q / ((int64_t)e.nx * e.ny));
+    const int64_t pc = (int64_t)(k + 1) * p_sk + (int64_t)(j + 1) * p_sj + (i + 1);
+    const double np = p[pc] + (double)e.x[q];
+    p[pc] = np;
+    if (i == 0) p[pc - 1] = np;
+    if (i == e.nx - 1) p[pc + 1] = np;
+    if (j == 0) p[pc - p_sj] = np;
+    if (j == e.ny - 1) p[pc + p_sj] = np;
+    if (k == 0) p[pc - p_sk] = np;
+    if (k == e.nz - 1) p[pc + p_sk] = np;
+  }
+}
+
+bool cycle_fp64(MgHierarchy *H, double *p, const double *rhs)
+{
+  MgState *st = H->d_state;
+  const double *shift = &st->shift;
+  View<double> v0 = padded_view(H->lv[0], p, rhs);
+  if (H->nl == 1) {
+    if (!sweeps<double>(v0, H->coarse_sweeps, false, shift, st)) return false;
+    // residual norm only
+    return restrict_to<double, true>(v0, nullptr, H->lv[0], shift, st, H->red);
+  }
+  if (!sweeps<double>(v0, H->pre, false, shift, st)) return false;
+  if (!restrict_to<double, true>(v0, H->b64[1], H->lv[1], shift, st, H->red)) return false;
+  if (!vcycle<double>(H, 1, H->x64, H->b64, nullptr)) return false;
+  if (!prolong_to<double>(v0, H->x64[1], H->lv[1], st)) return false;
+  return sweeps<double>(v0, H->post, false, shift, st);
+}
+
+bool cycle_mixed(MgHierarchy *H, double *p, const double *rhs)
+{
+  MgState *st = H->d_state;
+  View<double> v0 = padded_view(H->lv[0], p, rhs);
+  const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
+  k_mx_residual<<<flat_blocks(n0), kNT, 0, stream()>>>(v0, H->b32[0], st, H->red.partials,
+      H->red.ticket);
+  if (!launched("k_mx_residual")) return false;
+  const bool fold_in_smoother = H->post > 0 && H->nl > 1;
+  if (!vcycle<float>(H, 0, H->x32, H->b32, fold_in_smoother ? p : nullptr)) return false;
+  if (!fold_in_smoother) {
+    View<float> e = compact_view<float>(H->lv[0], H->x32[0], H->b32[0]);
+    k_mx_fold<<<flat_blocks(n0), kNT, 0, stream()>>>(e, p, v0.sy, v0.sz, st);
+    if (!launched("k_mx_fold")) return false;
+  }
+  return true;
+}
+
+}  // namespace
 
 bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
 {
-  (void)s;
-  (void)d;
-  (void)ss;
-  fail(NUSIF_ERR_ARG, "solver kinds mg and mg-mixed are not available in this build");
-  return false;
+  MgHierarchy *H = new MgHierarchy();
+  ss->mg = H;
+  const Extras &x = ss->ext;
+  H->mode = ss->kind == SOLVER_MG_MIXED ? 1 : 0;
+  H->pre = x.mg_pre;
+  H->post = x.mg_post;
+  H->coarse_sweeps = x.mg_coarse_sweeps;
+  H->maxcycles = x.mg_maxcycles;
+  H->rtol = x.rtol;
+  if (H->pre < 0 || H->post < 0 || H->coarse_sweeps < 0 || H->maxcycles < 1 || !(H->rtol >= 0)) {
+    fail(NUSIF_ERR_ARG, "multigrid: invalid mg_pre/mg_post/mg_coarse/mg_cycles/rtol");
+    return false;
+  }
+  H->nl = build_levels(&d->grid, x.mg_levels, H->lv);
+  for (int l = 0; l < H->nl; l++) {
+    const size_t n = (size_t)H->lv[l].n[0] * H->lv[l].n[1] * H->lv[l].n[2];
+    if (H->mode == 0 && l > 0) {
+      if (!cuda_ok(cudaMalloc(&H->x64[l], n * sizeof(double)), "cudaMalloc(mg x)")) return false;
+      if (!cuda_ok(cudaMalloc(&H->b64[l], n * sizeof(double)), "cudaMalloc(mg b)")) return false;
+      cudaMemset(H->x64[l], 0, n * sizeof(double));
+    }
+    if (H->mode == 1) {
+      if (!cuda_ok(cudaMalloc(&H->x32[l], n * sizeof(float)), "cudaMalloc(mg x32)")) return false;
+      if (!cuda_ok(cudaMalloc(&H->b32[l], n * sizeof(float)), "cudaMalloc(mg b32)")) return false;
+      cudaMemset(H->x32[l], 0, n * sizeof(float));
+    }
+  }
+  const int64_t n0 = (int64_t)d->grid.imax * d->grid.jmax * d->grid.kmax;
+  if (!reduce_scratch_alloc(H->red, flat_blocks(n0) + 16)) return false;
+  if (!cuda_ok(cudaMalloc(&H->d_state, sizeof(MgState)), "cudaMalloc(mg state)")) return false;
+  if (!cuda_ok(cudaMallocHost(&H->h_state, sizeof(MgState)), "cudaMallocHost(mg state)"))
+    return false;
+  memset(H->h_state, 0, sizeof(MgState));
+  // expose the level arrays like the reference's r[] / e[] (solver-mg.c:375-388)
+  for (int l = 0; l < H->nl; l++) {
+    H->h_ptrs[l] = H->mode == 0 ? H->b64[l] : reinterpret_cast<double *>(H->b32[l]);
+    H->h_ptrs[kMaxLevels + l] = H->mode == 0 ? H->x64[l] : reinterpret_cast<double *>(H->x32[l]);
+  }
+  s->r = H->h_ptrs;
+  s->e = H->h_ptrs + kMaxLevels;
+  s->levels = H->nl;
+  s->presmooth = H->pre;
+  s->postsmooth = H->post;
+  return cuda_ok(cudaDeviceSynchronize(), "mg setup");
 }
 
 double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
 {
+  MgHierarchy *H = ss->mg;
+  if (!H) {
+    fail(NUSIF_ERR_STATE, "mg solve without a hierarchy");
+    return NAN;
+  }
   (void)s;
-  (void)ss;
-  (void)p;
-  (void)rhs;
-  fail(NUSIF_ERR_STATE, "mg solve without a hierarchy");
-  return 0.0;
+  MgState *h = H->h_state;
+  memset(h, 0, sizeof(*h));
+  h->rtol2 = H->rtol * H->rtol;
+  h->maxcycles = H->maxcycles;
+  if (!cuda_ok(cudaMemcpyAsync(H->d_state, h, sizeof(MgState), cudaMemcpyHostToDevice, stream()),
+          "mg state upload"))
+    return NAN;
+  View<double> v0 = padded_view(H->lv[0], p, rhs);
+  const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
+  const int blocks = flat_blocks(n0);
+  k_mg_rhs_sum<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
+  if (!launched("k_mg_rhs_sum")) return NAN;
+  k_mg_rhs_norm<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
+  if (!launched("k_mg_rhs_norm")) return NAN;
+
+  int chunk = H->last_cycles > 0 ? H->last_cycles : 4;
+  for (;;) {
+    for (int q = 0; q < chunk; q++) {
+      const bool ok = H->mode == 0 ? cycle_fp64(H, p, rhs) : cycle_mixed(H, p, rhs);
+      if (!ok) return NAN;
+    }
+    if (!cuda_ok(cudaMemcpyAsync(h, H->d_state, sizeof(MgState), cudaMemcpyDeviceToHost,
+                     stream()),
+            "mg state download"))
+      return NAN;
+    if (!cuda_ok(cudaStreamSynchronize(stream()), "mg sync")) return NAN;
+    if (h->done) break;
+    chunk = 2;
+  }
+  if (!launch_pressure_ghosts(make_dims(v0.nx, v0.ny, v0.nz), p)) return NAN;
+  H->last_cycles = h->cycles;
+  ss->last_iterations = h->cycles;
+  const double rel = h->nb2 > 0.0 ? sqrt(h->res2 / h->nb2) : 0.0;
+  const char *v = getenv("NUSIF_VERBOSE");
+  if (v && v[0] && v[0] != '0')
+    printf("Multigrid took %d V-cycles to reach relative residual %e\n", h->cycles, rel);
+  return rel;
 }
 
 void mg_free(Solver *s, SolverState *ss)
 {
-  (void)s;
-  delete ss->mg;
+  MgHierarchy *H = ss->mg;
+  if (!H) return;
+  for (int l = 0; l < kMaxLevels; l++) {
+    if (H->x64[l]) cudaFree(H->x64[l]);
+    if (H->b64[l]) cudaFree(H->b64[l]);
+    if (H->x32[l]) cudaFree(H->x32[l]);
+    if (H->b32[l]) cudaFree(H->b32[l]);
+  }
+  if (H->d_state) cudaFree(H->d_state);
+  if (H->h_state) cudaFreeHost(H->h_state);
+  reduce_scratch_free(H->red);
+  delete H;
   ss->mg = nullptr;
+  if (s) {
+    s->r = nullptr;
+    s->e = nullptr;
+  }
 }
 
 }  // namespace nusif

@@ -66,7 +66,9 @@ class OrCase(C.Structure):
                 ("lid", C.c_double), ("inflow", C.c_double),
                 ("eps", C.c_double), ("omega", C.c_double), ("itermax", C.c_int),
                 ("solver", C.c_int), ("levels", C.c_int), ("presmooth", C.c_int),
-                ("postsmooth", C.c_int)]
+                ("postsmooth", C.c_int), ("rtol", C.c_double), ("mg_levels", C.c_int),
+                ("mg_pre", C.c_int), ("mg_post", C.c_int), ("mg_coarse", C.c_int),
+                ("mg_cycles", C.c_int)]
 
 
 class OrState(C.Structure):
@@ -137,8 +139,11 @@ def case_from_values(v: dict, solver: str = "rb") -> OrCase:
     c.lid = v.get("lid", 1.0)
     c.inflow = v.get("inflow", 2.0)
     c.eps, c.omega, c.itermax = v["eps"], v["omg"], v["itermax"]
-    c.solver = {"rb": 0, "mg-ref": 1}[solver]
+    c.solver = {"rb": 0, "mg-ref": 1, "mg": 2, "mg-mixed": 3}[solver]
     c.levels, c.presmooth, c.postsmooth = v["levels"], v["presmooth"], v["postsmooth"]
+    c.rtol = v.get("rtol", 1e-6)
+    c.mg_levels, c.mg_pre, c.mg_post = v.get("mg_levels", 0), v.get("mg_pre", 2), v.get("mg_post", 2)
+    c.mg_coarse, c.mg_cycles = v.get("mg_coarse", 64), v.get("mg_cycles", 100)
     return c
 
 

@@ -83,8 +83,10 @@ typedef struct {
   double lid, inflow;
   double eps, omega;
   int itermax;
-  int solver; /* 0 = rb, 1 = mg-ref */
+  int solver; /* 0 = rb, 1 = mg-ref, 2 = mg, 3 = mg-mixed */
   int levels, presmooth, postsmooth;
+  double rtol;
+  int mg_levels, mg_pre, mg_post, mg_coarse, mg_cycles;
 } OrCase;
 
 typedef struct {

@@ -1,0 +1,123 @@
+"""GPU multigrid solvers ("mg": FP64 V-cycles, "mg-mixed": FP32 V-cycles in
+FP64 iterative refinement) against their CPU restatement
+(oracle/nusif_oracle_mg.c) and against an independent numpy residual.
+
+Tolerances: FP64 V-cycles must use the same number of cycles as the oracle
+and give the pressure to 1e-10 of its magnitude (FMA and reduction order
+only). FP32 arithmetic on the GPU rounds differently from the CPU's FP32, so
+mixed precision is held to the stop criterion itself: the true residual of
+the returned pressure is below rtol, the cycle count is within one of the
+oracle's, and the pressure agrees with the FP64 solution to 1e-6 of its
+magnitude after the Neumann null space (the mean) is removed.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+from test_oracle_mg import neumann_residual
+
+pytestmark = pytest.mark.gpu
+
+DIMS = [(16, 16, 16), (32, 32, 32), (64, 32, 16), (48, 16, 32), (33, 17, 9), (8, 8, 8)]
+
+
+def _sim(dims, solver, rtol, **over):
+    from nusif import Simulation
+    from nusif.params import cavity
+    vals = cavity(dims, xlength=1.0, ylength=0.8, zlength=1.2, te=1e9, solver=solver,
+                  rtol=rtol, **over)
+    return Simulation(vals)
+
+
+def _interior_demeaned(p):
+    a = p[1:-1, 1:-1, 1:-1]
+    return a - a.mean()
+
+
+@pytest.mark.parametrize("dims", DIMS)
+def test_mg_fp64_matches_oracle(nusif_lib, oracle_mod, dims):
+    o = oracle_mod
+    rng = np.random.default_rng(17)
+    rtol = 1e-9
+    with _sim(dims, "mg", rtol, mg_cycles=60) as sim:
+        g = sim.d.grid
+        og = o.grid(*dims, g.xlength, g.ylength, g.zlength)
+        p0 = rng.standard_normal(sim.padded_shape)
+        rhs = rng.standard_normal(sim.padded_shape)
+        sim.set_field("p", p0)
+        sim.set_field("rhs", rhs)
+        rel = sim.solve()
+        cyc = sim.iterations
+        pc = p0.copy()
+        cyc_c, rel_c = o.op_mg_solve(og, "mg", pc, rhs, rtol=rtol, maxcycles=60)
+        assert cyc == cyc_c
+        assert rel == pytest.approx(rel_c, rel=1e-6)
+        p = sim.field("p")
+        assert rel_err(p[1:-1, 1:-1, 1:-1], pc[1:-1, 1:-1, 1:-1]) < 1e-10
+        assert neumann_residual(p, rhs, (g.dx, g.dy, g.dz)) == pytest.approx(rel, rel=1e-3)
+        np.testing.assert_array_equal(sim.field("rhs"), rhs)
+        np.testing.assert_array_equal(p[0, 1:-1, 1:-1], p[1, 1:-1, 1:-1])
+
+
+@pytest.mark.parametrize("dims", DIMS)
+def test_mg_mixed_matches_oracle(nusif_lib, oracle_mod, dims):
+    o = oracle_mod
+    rng = np.random.default_rng(23)
+    rtol = 1e-8
+    with _sim(dims, "mg-mixed", rtol, mg_cycles=60) as sim:
+        g = sim.d.grid
+        og = o.grid(*dims, g.xlength, g.ylength, g.zlength)
+        p0 = rng.standard_normal(sim.padded_shape)
+        rhs = rng.standard_normal(sim.padded_shape)
+        sim.set_field("p", p0)
+        sim.set_field("rhs", rhs)
+        rel = sim.solve()
+        cyc = sim.iterations
+        p = sim.field("p")
+        true_rel = neumann_residual(p, rhs, (g.dx, g.dy, g.dz))
+        pc = p0.copy()
+        cyc_c, rel_c = o.op_mg_solve(og, "mg-mixed", pc, rhs, rtol=rtol, maxcycles=60)
+        p64 = p0.copy()
+        o.op_mg_solve(og, "mg", p64, rhs, rtol=rtol, maxcycles=60)
+        if cyc_c < 60:
+            assert rel <= rtol
+            assert true_rel <= rtol * 1.001
+            assert abs(cyc - cyc_c) <= 1
+            a, b = _interior_demeaned(p), _interior_demeaned(p64)
+            assert np.max(np.abs(a - b)) <= 1e-6 * np.max(np.abs(b))
+        else:  # not converging in the cap (no coarsening possible): same cap reached
+            assert cyc == cyc_c
+        assert true_rel == pytest.approx(rel, rel=1e-3)
+
+
+@pytest.mark.parametrize("solver", ["mg", "mg-mixed"])
+def test_mg_zero_rhs_returns_at_once(nusif_lib, solver):
+    with _sim((16, 16, 16), solver, 1e-6) as sim:
+        p0 = np.random.default_rng(1).standard_normal(sim.padded_shape)
+        sim.set_field("p", p0)
+        sim.set_field("rhs", np.full(sim.padded_shape, 3.25))  # constant: mean-free part is 0
+        assert sim.solve() == 0.0
+        assert sim.iterations == 0
+        np.testing.assert_array_equal(sim.field("p")[1:-1, 1:-1, 1:-1], p0[1:-1, 1:-1, 1:-1])
+
+
+@pytest.mark.parametrize("solver", ["mg", "mg-mixed"])
+def test_mg_time_loop_matches_oracle(nusif_lib, oracle_mod, solver):
+    """A 32^3 cavity for 10 steps: the V-cycle solvers inside the time loop."""
+    from nusif import Simulation
+    from nusif.params import cavity
+    vals = cavity(32, te=1e9, solver=solver, rtol=1e-8)
+    run = oracle_mod.OracleRun(vals, solver)
+    tol = 1e-9 if solver == "mg" else 1e-5
+    with Simulation(vals) as sim:
+        for s in range(10):
+            a = sim.step()
+            it, res, dt, t = run.step()
+            assert a.dt == pytest.approx(dt, rel=1e-6 if solver == "mg-mixed" else 1e-10)
+            if solver == "mg":
+                assert a.it == it
+            assert a.res <= 1e-8
+            for f in "uvw":
+                assert rel_err(sim.field(f), run.field(f)) < tol, (s, f)
