@@ -53,6 +53,8 @@ def parse_args():
     ap.add_argument("--n", type=int, default=256, help="cells per axis of the cavity")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--itermax", type=int, default=None,
+                    help="cap of the red-black iterations per step (short profiling runs)")
     return ap.parse_args()
 
 
@@ -126,17 +128,17 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def bench_case(n: int, solver: str) -> dict:
+def bench_case(n: int, solver: str, itermax: int | None = None) -> dict:
     from nusif.params import config2
     vals = config2(solver=solver)
     vals.update(imax=n, jmax=n, kmax=n)
+    if itermax is not None:
+        vals["itermax"] = itermax
     return vals
 
 
 def pick_solver(requested: str) -> str:
-    if requested != "auto":
-        return requested
-    return "mg-mixed" if os.environ.get("NUSIF_BENCH_HAS_MG", "1") == "1" else "rb"
+    return "mg-mixed" if requested == "auto" else requested
 
 
 # ---------------------------------------------------------------- GPU arm
@@ -156,15 +158,8 @@ def run_gpu(args, rank, world, local):
     lib.nusifSetStream(C.c_void_p(stream.cuda_stream))
 
     solver = pick_solver(args.solver)
-    vals = bench_case(args.n, solver)
-    try:
-        sim = nusif.Simulation(vals)
-    except nusif.NusifError:
-        if args.solver != "auto":
-            raise
-        solver = "rb"
-        vals = bench_case(args.n, solver)
-        sim = nusif.Simulation(vals)
+    vals = bench_case(args.n, solver, args.itermax)
+    sim = nusif.Simulation(vals)
     i, j, k = sim.dims
     ncell = i * j * k
     padded = (i + 2) * (j + 2) * (k + 2)
@@ -365,7 +360,7 @@ def run_reference(args, rank, world):
     if rank != 0:
         return None
     solver = pick_solver(args.solver)
-    vals = bench_case(args.n, solver)
+    vals = bench_case(args.n, solver, args.itermax)
     it = float(vals["itermax"])
     samples = []
     for s in range(args.warmup + args.steps):
