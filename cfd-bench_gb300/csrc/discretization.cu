@@ -232,6 +232,129 @@ __global__ void __launch_bounds__(kBlock) k_fgh(FghArgs A, const double *__restr
   if (k == 1) h[c - sk] = w[c - sk];
 }
 
+// ---- F, G, H in flux form ----
+// The donor-cell scheme is conservative: the reference's convective
+// difference du2dx (discretization.c:491-497) is Tx(i) - Tx(i-1) with
+// Tx(i) = c1*cp*(u_i + u_i+1) + c2*|cp|*(u_i - u_i+1), cp the doubled transport
+// velocity on face i+1/2, and the same holds for every term except the
+// z-convection of G, whose "minus" half uses V(i,j,k+1) (discretization.c:
+// 543-550, kept). The viscous term joins the face flux (nu*(q_a - q_b) with
+// nu = (1/Re)/h^2), so a cell needs three face fluxes per component instead of
+// six convective halves plus three second differences: about 85 FP64
+// instructions per cell instead of about 140 (GB300's FP64 pipe bounds this
+// kernel). A block owns a 32 x 8 tile of (i, j) columns and marches in k:
+// x-face fluxes pass to the right neighbour by warp shuffle, y-face fluxes to
+// the next row through shared memory, z-face fluxes stay in registers.
+struct FaceCoef {
+  double c1, c2, nu;  // 0.25/h, gamma*0.25/h, (1/Re)/h^2
+};
+
+struct FluxArgs {
+  Dims g;
+  FaceCoef ax, ay, az;
+  double dt, gx, gy, gz;
+  int kb;  // k planes per block
+};
+
+// total (convective + viscous) flux of q across the face between q_a (minus
+// side) and q_b (plus side), transported by the doubled velocity cp
+__device__ __forceinline__ double face_flux(const FaceCoef &a, double cp, double qa, double qb)
+{
+  const double s = qa + qb, d = qa - qb;
+  return fma(fma(a.c2, fabs(cp), a.nu), d, a.c1 * cp * s);
+}
+
+struct XFace { double f, g, h; };
+struct ZFace { double f, h, gv, gc; };  // gv: viscous flux of G, gc: G's transport velocity
+
+__device__ __forceinline__ XFace x_face(const double *__restrict__ u, const double *__restrict__ v,
+    const double *__restrict__ w, int64_t c, int sj, int sk, const FaceCoef &a)
+{
+  const double uc = __ldg(u + c);
+  XFace r;
+  r.f = face_flux(a, uc + __ldg(u + c + 1), uc, __ldg(u + c + 1));
+  r.g = face_flux(a, uc + __ldg(u + c + sj), __ldg(v + c), __ldg(v + c + 1));
+  r.h = face_flux(a, uc + __ldg(u + c + sk), __ldg(w + c), __ldg(w + c + 1));
+  return r;
+}
+
+__device__ __forceinline__ XFace y_face(const double *__restrict__ u, const double *__restrict__ v,
+    const double *__restrict__ w, int64_t c, int sj, int sk, const FaceCoef &a)
+{
+  const double vc = __ldg(v + c);
+  XFace r;
+  r.f = face_flux(a, vc + __ldg(v + c + 1), __ldg(u + c), __ldg(u + c + sj));
+  r.g = face_flux(a, vc + __ldg(v + c + sj), vc, __ldg(v + c + sj));
+  r.h = face_flux(a, vc + __ldg(v + c + sk), __ldg(w + c), __ldg(w + c + sj));
+  return r;
+}
+
+__device__ __forceinline__ ZFace z_face(const double *__restrict__ u, const double *__restrict__ v,
+    const double *__restrict__ w, int64_t c, int sj, int sk, const FaceCoef &a)
+{
+  const double wc = __ldg(w + c);
+  ZFace r;
+  r.f = face_flux(a, wc + __ldg(w + c + 1), __ldg(u + c), __ldg(u + c + sk));
+  r.h = face_flux(a, wc + __ldg(w + c + sk), wc, __ldg(w + c + sk));
+  r.gv = a.nu * (__ldg(v + c) - __ldg(v + c + sk));
+  r.gc = wc + __ldg(w + c + sj);
+  return r;
+}
+
+constexpr int kFX = 32, kFY = 8;
+
+__global__ void __launch_bounds__(kFX *kFY) k_fgh_flux(FluxArgs A, const double *__restrict__ u,
+    const double *__restrict__ v, const double *__restrict__ w, double *__restrict__ f,
+    double *__restrict__ gg, double *__restrict__ h)
+{
+  __shared__ XFace ys[2][kFY][kFX];
+  const Dims &g = A.g;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i_raw = blockIdx.x * kFX + tx + 1;
+  const int j_raw = blockIdx.y * kFY + ty + 1;
+  const bool active = i_raw <= g.imax && j_raw <= g.jmax;
+  const int i = min(i_raw, g.imax), j = min(j_raw, g.jmax);  // loads stay in bounds
+  const int k0 = blockIdx.z * A.kb + 1;
+  const int k1 = min(k0 + A.kb - 1, g.kmax);
+  const int sj = g.sj, sk = g.sk;
+  const int64_t col = (int64_t)j * sj + i;
+  ZFace zm = z_face(u, v, w, (int64_t)(k0 - 1) * sk + col, sj, sk, A.az);
+  int buf = 0;
+  for (int k = k0; k <= k1; k++, buf ^= 1) {
+    const int64_t c = (int64_t)k * sk + col;
+    const XFace xp = x_face(u, v, w, c, sj, sk, A.ax);
+    XFace xm;
+    xm.f = __shfl_up_sync(0xffffffffu, xp.f, 1);
+    xm.g = __shfl_up_sync(0xffffffffu, xp.g, 1);
+    xm.h = __shfl_up_sync(0xffffffffu, xp.h, 1);
+    if (tx == 0) xm = x_face(u, v, w, c - 1, sj, sk, A.ax);
+    const XFace yp = y_face(u, v, w, c, sj, sk, A.ay);
+    ys[buf][ty][tx] = yp;
+    __syncthreads();
+    const XFace ym = ty > 0 ? ys[buf][ty - 1][tx] : y_face(u, v, w, c - sj, sj, sk, A.ay);
+    const ZFace zp = z_face(u, v, w, c, sj, sk, A.az);
+    if (active) {
+      const double uc = __ldg(u + c), vc = __ldg(v + c), wc = __ldg(w + c);
+      // F(imax), G(jmax), H(kmax) are wall faces carrying the velocity (discretization.c:609-651)
+      const double sf = (xp.f - xm.f) + (yp.f - ym.f) + (zp.f - zm.f);
+      f[c] = (i == g.imax) ? uc : fma(A.dt, A.gx - sf, uc);
+      const double vt = __ldg(v + c + sk);
+      const double s = vc + vt, d = vc - vt;
+      const double zconv =
+          fma(A.az.c2 * d, fabs(zp.gc) + fabs(zm.gc), A.az.c1 * s * (zp.gc - zm.gc));
+      const double sg = (xp.g - xm.g) + (yp.g - ym.g) + (zp.gv - zm.gv) + zconv;
+      gg[c] = (j == g.jmax) ? vc : fma(A.dt, A.gy - sg, vc);
+      const double sh = (xp.h - xm.h) + (yp.h - ym.h) + (zp.h - zm.h);
+      h[c] = (k == g.kmax) ? wc : fma(A.dt, A.gz - sh, wc);
+      // low wall faces F(0), G(0), H(0) carry the velocity (discretization.c:601-643)
+      if (i == 1) f[c - 1] = __ldg(u + c - 1);
+      if (j == 1) gg[c - sj] = __ldg(v + c - sj);
+      if (k == 1) h[c - sk] = __ldg(w + c - sk);
+    }
+    zm = zp;
+  }
+}
+
 // ---- RHS (discretization.c:334-362) ----
 __global__ void __launch_bounds__(kBlock) k_rhs(Dims g, double ix, double iy, double iz,
     double idt, const double *__restrict__ f, const double *__restrict__ gg,
@@ -372,25 +495,28 @@ bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, do
     double dt, double dx, double dy, double dz, const double *u, const double *v,
     const double *w, double *f, double *gg, double *h)
 {
-  FghArgs A;
+  FluxArgs A;
   A.g = g;
-  const double ix = 1.0 / dx, iy = 1.0 / dy, iz = 1.0 / dz;
-  A.c1x = ix * 0.25;
-  A.c1y = iy * 0.25;
-  A.c1z = iz * 0.25;
-  A.c2x = gamma * ix * 0.25;
-  A.c2y = gamma * iy * 0.25;
-  A.c2z = gamma * iz * 0.25;
-  A.ex = ix * ix;
-  A.ey = iy * iy;
-  A.ez = iz * iz;
-  A.iRe = 1.0 / re;
+  const double inv[3] = { 1.0 / dx, 1.0 / dy, 1.0 / dz };
+  const double iRe = 1.0 / re;
+  FaceCoef *fc[3] = { &A.ax, &A.ay, &A.az };
+  for (int a = 0; a < 3; a++) {
+    fc[a]->c1 = inv[a] * 0.25;
+    fc[a]->c2 = gamma * inv[a] * 0.25;
+    fc[a]->nu = iRe * (inv[a] * inv[a]);
+  }
   A.dt = dt;
   A.gx = gx;
   A.gy = gy;
   A.gz = gz;
-  k_fgh<<<cell_grid(g, kCellBlock), kCellBlock, 0, stream()>>>(A, u, v, w, f, gg, h);
-  return launched("k_fgh");
+  const int gx_blocks = (g.imax + kFX - 1) / kFX, gy_blocks = (g.jmax + kFY - 1) / kFY;
+  int kb = 32;
+  while (kb > 1 && (int64_t)gx_blocks * gy_blocks * ((g.kmax + kb - 1) / kb) < 8 * sm_count())
+    kb >>= 1;
+  A.kb = kb;
+  dim3 grid(gx_blocks, gy_blocks, (g.kmax + kb - 1) / kb);
+  k_fgh_flux<<<grid, dim3(kFX, kFY), 0, stream()>>>(A, u, v, w, f, gg, h);
+  return launched("k_fgh_flux");
 }
 
 bool launch_rhs(const Dims &g, double dt, double dx, double dy, double dz, const double *f,

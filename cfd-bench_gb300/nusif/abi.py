@@ -97,6 +97,9 @@ SIGNATURES = [
     ("nusifSolveRBStatic", C.c_int, [c_double_p, c_double_p, C.c_int, C.c_int, C.c_int,
                                      C.c_double, C.c_double, C.c_double, C.c_double,
                                      C.c_double, C.c_int, c_double_p, C.POINTER(C.c_int)]),
+    ("nusifCollectResult", C.c_int, [C.POINTER(Discretization), c_double_p, c_double_p,
+                                     c_double_p, c_double_p]),
+    ("nusifWriteVTK", C.c_int, [C.POINTER(Discretization), C.c_char_p, C.c_int]),
     ("nusifLaunchCount", C.c_ulonglong, []),
     ("nusifVersion", C.c_char_p, []),
 ]

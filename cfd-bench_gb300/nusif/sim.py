@@ -132,15 +132,44 @@ class Simulation:
         self.nt += 1
         return StepInfo(self.nt, self.t, dt, res, it)
 
-    def run(self, max_steps: int | None = None, callback=None) -> list[StepInfo]:
-        """``while (t <= te)`` (src/main.c:60), optionally capped at max_steps."""
+    def run(self, max_steps: int | None = None, callback=None,
+            residual_file: str | Path | None = None) -> list[StepInfo]:
+        """``while (t <= te)`` (src/main.c:60), optionally capped at max_steps.
+
+        ``residual_file``: write the reference's residual.dat, one "%f, %f" line
+        of (time at the start of the step, solve() result) per step
+        (src/main.c:74-76, src/progress.c:63-66)."""
         out = []
-        while self.t <= self.te and (max_steps is None or len(out) < max_steps):
-            info = self.step()
-            out.append(info)
-            if callback:
-                callback(self, info)
+        fh = open(residual_file, "w") if residual_file else None
+        try:
+            while self.t <= self.te and (max_steps is None or len(out) < max_steps):
+                t0 = self.t
+                info = self.step()
+                out.append(info)
+                if fh:
+                    fh.write("%f, %f\n" % (t0, info.res))
+                if callback:
+                    callback(self, info)
+        finally:
+            if fh:
+                fh.close()
         return out
+
+    # ---- output (reference src/main.c:97-143) ----
+    def collect(self) -> dict[str, np.ndarray]:
+        """Cell-centred u, v, w and interior p, shape (kmax, jmax, imax)
+        (commCollectResult, src/comm.c:327-477)."""
+        i, j, k = self.dims
+        out = {f: np.empty((k, j, i), dtype=np.float64) for f in "uvwp"}
+        self.lib.nusifCollectResult(C.byref(self.d), *(out[f].ctypes.data_as(abi.c_double_p)
+                                                       for f in "uvwp"))
+        abi.check(self.lib)
+        return out
+
+    def write_vtk(self, path: str | Path, binary: bool = False) -> None:
+        """The reference's <problem>.vtk (src/vtkWriter-seq.c)."""
+        self.lib.nusifWriteVTK(C.byref(self.d), str(path).encode(), int(binary))
+        abi.check(self.lib)
 
     def close(self) -> None:
         if self._closed:

@@ -172,13 +172,23 @@ NUSIF_API void nusifFreeSolver(Solver *s);
  * call cudaMalloc (a CUDA graph under capture, hosts that forbid device
  * allocation after start-up). Its scratch is a fixed 256.5 KiB __device__
  * array of the library: grids needing more than 32768 per-block partial sums
- * (larger than about 512^3 cells) are rejected with NUSIF_ERR_ARG. The first call on a device
- * looks up that array's address and should come before any stream capture.
+ * (larger than about 512^3 cells) are rejected with NUSIF_ERR_ARG. The first
+ * call on a device looks up that array's address and should come before any
+ * stream capture.
  * Calls share the array: calls that overlap on the GPU race. Returns a
  * NUSIF_* code; *res_out and *it_out get solve()'s residual and iterations. */
 NUSIF_API int nusifSolveRBStatic(double *p, const double *rhs, int imax, int jmax, int kmax,
     double dx, double dy, double dz, double omega, double eps, int itermax, double *res_out,
     int *it_out);
+/* Result collection, replaces commCollectResult (reference src/comm.c:327-477,
+ * sequential path): cell-centred u, v, w (face averages) and interior p as
+ * host arrays of imax*jmax*kmax doubles, i fastest. */
+NUSIF_API int nusifCollectResult(const Discretization *d, double *ug, double *vg, double *wg,
+    double *pg);
+/* The reference's VTK output (src/vtkWriter-seq.c:12-146, called from
+ * src/main.c:135-141): STRUCTURED_POINTS with "pressure" and "velocity";
+ * binary = 0 writes ASCII "%f" (the reference's default), 1 big-endian doubles. */
+NUSIF_API int nusifWriteVTK(const Discretization *d, const char *path, int binary);
 /* kernels this library launched since it was loaded (observability) */
 NUSIF_API unsigned long long nusifLaunchCount(void);
 /* library version string */

@@ -123,6 +123,24 @@ def config1_run() -> None:
     print(f"config1_rb: {len(its)} steps, {sum(its)} iterations")
 
 
+def program_outputs() -> None:
+    """The reference program (src/main.c) end to end on a 10^3 cavity: its
+    residual.dat and dcavity.vtk, as written by the reference's own writers."""
+    import shutil
+    import subprocess
+    exe = oracle.REF_DIR / "NusifSolver-rb"
+    vals = cavity(10, te=1.2, omg=1.7, eps=1e-3, itermax=100)
+    with tempfile.TemporaryDirectory() as d:
+        par = write_par(Path(d) / "cavity10.par", vals)
+        subprocess.run([str(exe), str(par)], cwd=d, check=True, stdout=subprocess.DEVNULL)
+        out = OUT / "program_cavity10"
+        out.mkdir(exist_ok=True)
+        shutil.copy(Path(d) / "residual.dat", out / "residual.dat")
+        shutil.copy(Path(d) / "dcavity.vtk", out / "dcavity.vtk")
+        (out / "case.par").write_text(par.read_text())
+    print("program_cavity10: residual.dat, dcavity.vtk")
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-config1", action="store_true")
@@ -147,6 +165,7 @@ def main() -> None:
                                 postsmooth=2), "mg-ref", 3, [3])
     run_case("cavity_tau0_rb", cavity(6, tau=-1.0, dt=0.01, te=1e9, eps=1e-3, itermax=50),
              "rb", 4, [4])
+    program_outputs()
     if not args.skip_config1:
         config1_run()
 
