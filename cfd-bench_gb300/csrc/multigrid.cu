@@ -23,6 +23,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <vector>
 
 #include "nusif_internal.h"
 #include "reduce.cuh"
@@ -31,18 +32,26 @@
 namespace nusif {
 
 constexpr int kMaxLevels = 16;
+constexpr int kMaxDirect = 1024;  // largest coarsest level solved exactly (dense inverse)
 
 struct MgState {
-  double shift;  // mean of the right-hand side
-  double nb2;    // ||rhs - shift||^2
-  double res2;   // last ||b - Ap||^2
-  double tol2;   // rtol^2 * nb2
+  double shift;      // mean of the right-hand side
+  double nb2;        // ||rhs - shift||^2
+  double res2;       // last FP64 ||b - Ap||^2
+  double tol2;       // rtol^2 * nb2
   double rtol2;
-  int cycles;    // V-cycles counted by the stop test
+  double tol_inner;  // mg-mixed: (rtol/2)^2 * nb2, target of the FP32 correction
+  double res2_inner; // mg-mixed: last ||r32 - A e||^2
+  int cycles;        // V-cycles done
+  int outer;         // mg-mixed: FP64 residual evaluations that found work to do
   int maxcycles;
-  int done;
+  int done;          // the solve is finished: every kernel returns at once
+  int inner_done;    // mg-mixed: this outer iteration's correction is good enough
   int pad;
 };
+
+// what the fold of a fine-level restriction decides
+enum { FOLD_NONE = 0, FOLD_OUTER = 1, FOLD_INNER = 2 };
 
 struct MgLevelDesc {
   int n[3];
@@ -72,9 +81,12 @@ struct MgHierarchy {
   MgState *d_state = nullptr;
   MgState *h_state = nullptr;
   ReduceScratch red;
-  int pre = 2, post = 2, coarse_sweeps = 64, maxcycles = 100;
+  int pre = 2, post = 2, coarse_sweeps = 0, maxcycles = 100;
+  double *minv64 = nullptr;  // exact coarsest solve (device), mg
+  float *minv32 = nullptr;   // the same in FP32, mg-mixed
   double rtol = 1e-6;
-  int last_cycles = 0;
+  int last_cycles = 0;  // queue size of the previous solve (cycles, or outer iterations)
+  int inner = 4;        // mg-mixed: most FP32 V-cycles per FP64 residual
   double *h_ptrs[2 * kMaxLevels] = {};  // exposed through Solver::r / Solver::e
 };
 
@@ -82,7 +94,16 @@ namespace {
 
 constexpr int kBX = 32, kBY = 8, kNT = kBX * kBY;
 
+// V-cycle kernels stop when the solve is done or (mg-mixed) when the current
+// correction already meets its target; inner_done stays 0 for FP64 mg
 __device__ __forceinline__ bool mg_done(const MgState *st)
+{
+  const volatile int *f = reinterpret_cast<const volatile int *>(&st->done);
+  const volatile int *g = reinterpret_cast<const volatile int *>(&st->inner_done);
+  return *f != 0 || *g != 0;
+}
+
+__device__ __forceinline__ bool solve_finished(const MgState *st)
 {
   return *reinterpret_cast<const volatile int *>(&st->done) != 0;
 }
@@ -148,13 +169,16 @@ __global__ void __launch_bounds__(kNT) k_mg_smooth(View<T> v, int colour, const 
 }
 
 // Residual of the fine level averaged into the coarse right-hand side. One
-// thread per coarse cell. ACCUM: also sum r^2 (FP64) and let the last block
-// fold the partials and take the stop decision.
-template <typename T, bool ACCUM>
+// thread per coarse cell. FOLD != FOLD_NONE: also sum r^2 (FP64) and let the
+// last block fold the partials and decide: FOLD_OUTER (FP64 mg) counts the
+// cycle and stops the solve at rtol; FOLD_INNER (mg-mixed) counts the FP32
+// V-cycle and ends this correction once it meets its target.
+template <typename T, int FOLD>
 __global__ void __launch_bounds__(kNT) k_mg_restrict(View<T> f, T *bc, int cnx, int cny, int cnz,
     int rx, int ry, int rz, T inv_count, const double *shift, MgState *st,
     double *partials, unsigned *ticket)
 {
+  constexpr bool ACCUM = FOLD != FOLD_NONE;
   if (mg_done(st)) return;
   const int64_t ncoarse = (int64_t)cnx * cny * cnz;
   const T sh = shift ? (T)(*shift) : (T)0;
@@ -189,20 +213,28 @@ __global__ void __launch_bounds__(kNT) k_mg_restrict(View<T> f, T *bc, int cnx, 
   if (!last) return;
   const double total = fold_partials<kNT>(partials, gridDim.x, sm);
   if (threadIdx.x == 0) {
-    st->res2 = total;
     const int c = st->cycles + 1;
     st->cycles = c;
-    st->done = (total <= st->tol2) || (c >= st->maxcycles);
+    if (FOLD == FOLD_OUTER) {
+      st->res2 = total;
+      st->done = (total <= st->tol2) || (c >= st->maxcycles);
+    } else {
+      st->res2_inner = total;
+      st->inner_done = total <= st->tol_inner;
+    }
     *ticket = 0;
   }
 }
 
 // FP64 residual of p (padded layout) into the FP32 fine right-hand side, with
-// its FP64 norm folded by the last block (mixed precision stop test).
+// its FP64 norm folded by the last block: the mixed-precision stop test. It
+// also opens the next correction (inner_done = 0). count_cycles: one FP32
+// V-cycle per outer iteration is counted here (single-level grids, where no
+// fine restriction counts them).
 __global__ void __launch_bounds__(kNT) k_mx_residual(View<double> f, float *r32, MgState *st,
-    double *partials, unsigned *ticket)
+    double *partials, unsigned *ticket, int count_cycles)
 {
-  if (mg_done(st)) return;
+  if (solve_finished(st)) return;
   const int64_t n = (int64_t)f.nx * f.ny * f.nz;
   const double sh = st->shift;
   double acc = 0.0;
@@ -229,9 +261,13 @@ __global__ void __launch_bounds__(kNT) k_mx_residual(View<double> f, float *r32,
   const double total = fold_partials<kNT>(partials, gridDim.x, sm);
   if (threadIdx.x == 0) {
     st->res2 = total;
-    const int c = st->cycles;  // V-cycles completed before this residual
-    st->done = (total <= st->tol2) || (c >= st->maxcycles);
-    st->cycles = c + (st->done ? 0 : 1);
+    const int m = st->outer;  // corrections applied before this residual
+    st->done = (total <= st->tol2) || (m >= st->maxcycles);
+    if (!st->done) {
+      st->outer = m + 1;
+      st->inner_done = 0;
+      if (count_cycles) st->cycles += 1;
+    }
     *ticket = 0;
   }
 }
@@ -315,6 +351,29 @@ __global__ void __launch_bounds__(512) k_mg_coarse(View<T> v, int sweeps, const 
   for (int q = threadIdx.x; q < n; q += blockDim.x) v.x[q] = xs[q];
 }
 
+// Coarsest level, exact: x = Minv * b with Minv the inverse of the coarsest
+// operator deflated by its null space (see coarse_inverse); one warp per row,
+// b staged in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(128) k_mg_direct(const T *__restrict__ minv,
+    const T *__restrict__ b, T *__restrict__ x, int n, const MgState *st)
+{
+  if (mg_done(st)) return;
+  extern __shared__ unsigned char smem_raw[];
+  T *bs = reinterpret_cast<T *>(smem_raw);
+  for (int q = threadIdx.x; q < n; q += blockDim.x) bs[q] = b[q];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int row = blockIdx.x * 4 + (threadIdx.x >> 5);
+  if (row >= n) return;
+  const T *m = minv + (int64_t)row * n;
+  T acc = 0;
+  for (int q = lane; q < n; q += 32) acc += m[q] * bs[q];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) x[row] = acc;
+}
+
 // mean of the right-hand side, then ||rhs - mean||^2; initialises the state
 __global__ void __launch_bounds__(kNT) k_mg_rhs_sum(View<double> f, MgState *st,
     double *partials, unsigned *ticket)
@@ -371,8 +430,12 @@ __global__ void __launch_bounds__(kNT) k_mg_rhs_norm(View<double> f, MgState *st
   if (threadIdx.x == 0) {
     st->nb2 = total;
     st->tol2 = st->rtol2 * total;
+    st->tol_inner = 0.25 * st->rtol2 * total;
     st->res2 = 0.0;
+    st->res2_inner = 0.0;
     st->cycles = 0;
+    st->outer = 0;
+    st->inner_done = 0;
     st->done = (total == 0.0);
     *ticket = 0;
   }
@@ -422,6 +485,63 @@ int build_levels(const Grid *gr, int cap, MgLevelDesc *lv)
     nl++;
   }
   return nl;
+}
+
+// Inverse of the coarsest operator with its null space deflated:
+// M = A - (s/n) 1 1^T, A the ghost-free Neumann Laplacian of level L, s its
+// largest diagonal magnitude. -M is symmetric positive definite; for a
+// mean-free b, x = M^-1 b solves A x = b with mean(x) = 0 (a b with a small
+// mean gives the solution for b minus its mean). Cholesky of -M, then the
+// n unit right-hand sides; row-major n x n result. Returns false if the
+// factorisation fails.
+bool coarse_inverse(const MgLevelDesc &L, std::vector<double> &minv)
+{
+  const int nx = L.n[0], ny = L.n[1], nz = L.n[2];
+  const int n = nx * ny * nz;
+  const double s = 2.0 * (L.ih2[0] + L.ih2[1] + L.ih2[2]);
+  std::vector<double> a((size_t)n * n, s / n);  // this is -M: -A + (s/n) 1 1^T
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        const int q = i + nx * (j + ny * k);
+        const int idx[3] = { i, j, k }, n3[3] = { nx, ny, nz }, st[3] = { 1, nx, nx * ny };
+        for (int ax = 0; ax < 3; ax++)
+          for (int sgn = -1; sgn <= 1; sgn += 2) {
+            const int c = idx[ax] + sgn;
+            if (c < 0 || c >= n3[ax]) continue;
+            a[(size_t)q * n + q] += L.ih2[ax];
+            a[(size_t)q * n + q + sgn * st[ax]] -= L.ih2[ax];
+          }
+      }
+  // Cholesky in place (lower triangle)
+  for (int c = 0; c < n; c++) {
+    double d = a[(size_t)c * n + c];
+    for (int q = 0; q < c; q++) d -= a[(size_t)c * n + q] * a[(size_t)c * n + q];
+    if (!(d > 0.0)) return false;
+    d = std::sqrt(d);
+    a[(size_t)c * n + c] = d;
+    for (int r = c + 1; r < n; r++) {
+      double v = a[(size_t)r * n + c];
+      for (int q = 0; q < c; q++) v -= a[(size_t)r * n + q] * a[(size_t)c * n + q];
+      a[(size_t)r * n + c] = v / d;
+    }
+  }
+  minv.assign((size_t)n * n, 0.0);
+  std::vector<double> y(n);
+  for (int col = 0; col < n; col++) {
+    for (int r = 0; r < n; r++) {  // L y = e_col
+      double v = (r == col) ? 1.0 : 0.0;
+      for (int q = 0; q < r; q++) v -= a[(size_t)r * n + q] * y[q];
+      y[r] = v / a[(size_t)r * n + r];
+    }
+    for (int r = n - 1; r >= 0; r--) {  // L^T z = y
+      double v = y[r];
+      for (int q = r + 1; q < n; q++) v -= a[(size_t)q * n + r] * y[q];
+      y[r] = v / a[(size_t)r * n + r];
+    }
+    for (int r = 0; r < n; r++) minv[(size_t)r * n + col] = -y[r];  // M^-1 = -(-M)^-1
+  }
+  return true;
 }
 
 template <typename T>
@@ -504,18 +624,18 @@ int flat_blocks(int64_t n)
   return (int)(b < cap ? (b > 0 ? b : 1) : cap);
 }
 
-template <typename T, bool ACCUM>
+template <typename T, int FOLD>
 bool restrict_to(const View<T> &f, T *bc, const MgLevelDesc &C, const double *shift, MgState *st,
     ReduceScratch &red)
 {
   const int64_t nc = (int64_t)C.n[0] * C.n[1] * C.n[2];
   const int blocks = flat_blocks(nc);
-  if (ACCUM && red.capacity < blocks) {
+  if (FOLD != FOLD_NONE && red.capacity < blocks) {
     fail(NUSIF_ERR_STATE, "multigrid reduction scratch too small");
     return false;
   }
   const T inv = (T)(1.0 / (C.r[0] * C.r[1] * C.r[2]));
-  k_mg_restrict<T, ACCUM><<<blocks, kNT, 0, stream()>>>(f, bc, C.n[0], C.n[1], C.n[2], C.r[0],
+  k_mg_restrict<T, FOLD><<<blocks, kNT, 0, stream()>>>(f, bc, C.n[0], C.n[1], C.n[2], C.r[0],
       C.r[1], C.r[2], inv, shift, st, red.partials, red.ticket);
   return launched("k_mg_restrict");
 }
@@ -530,9 +650,14 @@ bool prolong_to(const View<T> &f, const T *xc, const MgLevelDesc &C, const MgSta
 }
 
 template <typename T>
-bool coarse_solve(const View<T> &v, int nsweeps, const MgState *st)
+bool coarse_solve(const View<T> &v, int nsweeps, const MgState *st, const T *minv)
 {
   const size_t n = (size_t)v.nx * v.ny * v.nz;
+  if (minv) {
+    k_mg_direct<T><<<(int)((n + 3) / 4), 128, n * sizeof(T), stream()>>>(minv, v.b, v.x, (int)n,
+        st);
+    return launched("k_mg_direct");
+  }
   const size_t bytes = 2 * n * sizeof(T);
   if (bytes <= 48 * 1024) {
     k_mg_coarse<T><<<1, 512, bytes, stream()>>>(v, nsweeps, st);
@@ -543,35 +668,42 @@ bool coarse_solve(const View<T> &v, int nsweeps, const MgState *st)
   return sweeps<T>(v, nsweeps, true, nullptr, st);
 }
 
-// V-cycle from level l (x_l starts at zero) on the arrays xs/bs of type T
+// V-cycle from level l on the compact arrays xs/bs of type T. x_l starts at
+// zero when `zero` (always below the top level); `inner_test`: the fine
+// restriction folds the residual norm for the mixed-precision inner stop.
 template <typename T>
-bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, double *fold_p)
+bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero, bool inner_test)
 {
   const MgLevelDesc &L = H->lv[l];
   View<T> v = compact_view<T>(L, xs[l], bs[l]);
   const size_t n = (size_t)L.n[0] * L.n[1] * L.n[2];
   MgState *st = H->d_state;
   if (l == H->nl - 1) {
-    if (!coarse_solve<T>(v, H->coarse_sweeps, st)) return false;
-  } else {
-    if (H->pre > 0) {
-      if (!sweeps<T>(v, H->pre, true, nullptr, st)) return false;
-    } else if (!cuda_ok(cudaMemsetAsync(xs[l], 0, n * sizeof(T), stream()), "zero x")) {
-      return false;
-    }
-    if (!restrict_to<T, false>(v, bs[l + 1], H->lv[l + 1], nullptr, st, H->red)) return false;
-    if (!vcycle<T>(H, l + 1, xs, bs, nullptr)) return false;
-    if (!prolong_to<T>(v, xs[l + 1], H->lv[l + 1], st)) return false;
-    if (!sweeps<T>(v, H->post, false, nullptr, st, fold_p)) return false;
-    return true;
+    const T *minv = nullptr;
+    if constexpr (sizeof(T) == sizeof(double))
+      minv = reinterpret_cast<const T *>(H->minv64);
+    else
+      minv = reinterpret_cast<const T *>(H->minv32);
+    return coarse_solve<T>(v, H->coarse_sweeps, st, minv);
   }
-  return true;
+  if (H->pre > 0) {
+    if (!sweeps<T>(v, H->pre, zero, nullptr, st)) return false;
+  } else if (zero && !cuda_ok(cudaMemsetAsync(xs[l], 0, n * sizeof(T), stream()), "zero x")) {
+    return false;
+  }
+  const bool ok = inner_test
+                      ? restrict_to<T, FOLD_INNER>(v, bs[l + 1], H->lv[l + 1], nullptr, st, H->red)
+                      : restrict_to<T, FOLD_NONE>(v, bs[l + 1], H->lv[l + 1], nullptr, st, H->red);
+  if (!ok) return false;
+  if (!vcycle<T>(H, l + 1, xs, bs, true, false)) return false;
+  if (!prolong_to<T>(v, xs[l + 1], H->lv[l + 1], st)) return false;
+  return sweeps<T>(v, H->post, false, nullptr, st);
 }
 
-// p += e (FP64) and Neumann ghosts, for mixed precision without post-smoothing
+// p += e (FP64) and Neumann ghosts of p, after the inner V-cycles
 __global__ void k_mx_fold(View<float> e, double *p, int p_sj, int p_sk, const MgState *st)
 {
-  if (mg_done(st)) return;
+  if (solve_finished(st)) return;
   const int64_t n = (int64_t)e.nx * e.ny * e.nz;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x) {
@@ -596,31 +728,32 @@ bool cycle_fp64(MgHierarchy *H, double *p, const double *rhs)
   if (H->nl == 1) {
     if (!sweeps<double>(v0, H->coarse_sweeps, false, shift, st)) return false;
     // residual norm only
-    return restrict_to<double, true>(v0, nullptr, H->lv[0], shift, st, H->red);
+    return restrict_to<double, FOLD_OUTER>(v0, nullptr, H->lv[0], shift, st, H->red);
   }
   if (!sweeps<double>(v0, H->pre, false, shift, st)) return false;
-  if (!restrict_to<double, true>(v0, H->b64[1], H->lv[1], shift, st, H->red)) return false;
-  if (!vcycle<double>(H, 1, H->x64, H->b64, nullptr)) return false;
+  if (!restrict_to<double, FOLD_OUTER>(v0, H->b64[1], H->lv[1], shift, st, H->red)) return false;
+  if (!vcycle<double>(H, 1, H->x64, H->b64, true, false)) return false;
   if (!prolong_to<double>(v0, H->x64[1], H->lv[1], st)) return false;
   return sweeps<double>(v0, H->post, false, shift, st);
 }
 
+// one outer iteration of mixed-precision refinement: FP64 residual (and stop
+// test), up to `inner` FP32 V-cycles on A e = r (stopped on the device once
+// ||r - A e|| <= rtol/2 ||b||), p += e in FP64
 bool cycle_mixed(MgHierarchy *H, double *p, const double *rhs)
 {
   MgState *st = H->d_state;
   View<double> v0 = padded_view(H->lv[0], p, rhs);
   const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
   k_mx_residual<<<flat_blocks(n0), kNT, 0, stream()>>>(v0, H->b32[0], st, H->red.partials,
-      H->red.ticket);
+      H->red.ticket, H->nl == 1 ? 1 : 0);
   if (!launched("k_mx_residual")) return false;
-  const bool fold_in_smoother = H->post > 0 && H->nl > 1;
-  if (!vcycle<float>(H, 0, H->x32, H->b32, fold_in_smoother ? p : nullptr)) return false;
-  if (!fold_in_smoother) {
-    View<float> e = compact_view<float>(H->lv[0], H->x32[0], H->b32[0]);
-    k_mx_fold<<<flat_blocks(n0), kNT, 0, stream()>>>(e, p, v0.sy, v0.sz, st);
-    if (!launched("k_mx_fold")) return false;
-  }
-  return true;
+  const int inner = H->nl == 1 ? 1 : H->inner;
+  for (int q = 0; q < inner; q++)
+    if (!vcycle<float>(H, 0, H->x32, H->b32, q == 0, true)) return false;
+  View<float> e = compact_view<float>(H->lv[0], H->x32[0], H->b32[0]);
+  k_mx_fold<<<flat_blocks(n0), kNT, 0, stream()>>>(e, p, v0.sy, v0.sz, st);
+  return launched("k_mx_fold");
 }
 
 }  // namespace
@@ -635,6 +768,7 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
   H->post = x.mg_post;
   H->coarse_sweeps = x.mg_coarse_sweeps;
   H->maxcycles = x.mg_maxcycles;
+  H->inner = x.mg_inner < 1 ? 1 : x.mg_inner;
   H->rtol = x.rtol;
   if (H->pre < 0 || H->post < 0 || H->coarse_sweeps < 0 || H->maxcycles < 1 || !(H->rtol >= 0)) {
     fail(NUSIF_ERR_ARG, "multigrid: invalid mg_pre/mg_post/mg_coarse/mg_cycles/rtol");
@@ -652,6 +786,33 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
       if (!cuda_ok(cudaMalloc(&H->x32[l], n * sizeof(float)), "cudaMalloc(mg x32)")) return false;
       if (!cuda_ok(cudaMalloc(&H->b32[l], n * sizeof(float)), "cudaMalloc(mg b32)")) return false;
       cudaMemset(H->x32[l], 0, n * sizeof(float));
+    }
+  }
+  // coarsest level: exact solve when mg_coarse is 0 and the level is small
+  // (FP64 mg with a single level smooths p itself, so it keeps sweeps)
+  const MgLevelDesc &Lc = H->lv[H->nl - 1];
+  const int nc = Lc.n[0] * Lc.n[1] * Lc.n[2];
+  const bool single_fp64 = H->mode == 0 && H->nl == 1;
+  if (H->coarse_sweeps == 0 && (nc > kMaxDirect || single_fp64)) H->coarse_sweeps = 64;
+  if (H->coarse_sweeps == 0) {
+    std::vector<double> minv;
+    if (!coarse_inverse(Lc, minv)) {
+      fail(NUSIF_ERR_STATE, "multigrid: coarsest operator factorisation failed");
+      return false;
+    }
+    if (H->mode == 0) {
+      if (!cuda_ok(cudaMalloc(&H->minv64, minv.size() * sizeof(double)), "cudaMalloc(minv)") ||
+          !cuda_ok(cudaMemcpy(H->minv64, minv.data(), minv.size() * sizeof(double),
+                       cudaMemcpyHostToDevice),
+              "upload minv"))
+        return false;
+    } else {
+      std::vector<float> m32(minv.begin(), minv.end());
+      if (!cuda_ok(cudaMalloc(&H->minv32, m32.size() * sizeof(float)), "cudaMalloc(minv32)") ||
+          !cuda_ok(cudaMemcpy(H->minv32, m32.data(), m32.size() * sizeof(float),
+                       cudaMemcpyHostToDevice),
+              "upload minv32"))
+        return false;
     }
   }
   const int64_t n0 = (int64_t)d->grid.imax * d->grid.jmax * d->grid.kmax;
@@ -711,7 +872,8 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
     chunk = 2;
   }
   if (!launch_pressure_ghosts(make_dims(v0.nx, v0.ny, v0.nz), p)) return NAN;
-  H->last_cycles = h->cycles;
+  // queue as many units next time: V-cycles (mg) or residual evaluations (mg-mixed)
+  H->last_cycles = H->mode == 0 ? h->cycles : h->outer + 1;
   ss->last_iterations = h->cycles;
   const double rel = h->nb2 > 0.0 ? sqrt(h->res2 / h->nb2) : 0.0;
   const char *v = getenv("NUSIF_VERBOSE");
@@ -730,6 +892,8 @@ void mg_free(Solver *s, SolverState *ss)
     if (H->x32[l]) cudaFree(H->x32[l]);
     if (H->b32[l]) cudaFree(H->b32[l]);
   }
+  if (H->minv64) cudaFree(H->minv64);
+  if (H->minv32) cudaFree(H->minv32);
   if (H->d_state) cudaFree(H->d_state);
   if (H->h_state) cudaFreeHost(H->h_state);
   reduce_scratch_free(H->red);

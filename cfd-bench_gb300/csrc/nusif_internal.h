@@ -27,9 +27,10 @@ struct Extras {
   double lid = 1.0;         // dcavity lid speed (reference hard-codes 1)
   double inflow = 2.0;      // canal inflow speed (reference hard-codes 2.0)
   double rtol = 1e-6;       // relative residual target of the V-cycle solvers
-  int mg_levels = 0;        // 0: coarsen while every axis stays even and >= 8
+  int mg_levels = 0;        // 0: halve an axis while it is even and >= 16
   int mg_pre = 2, mg_post = 2;
-  int mg_coarse_sweeps = 64;
+  int mg_coarse_sweeps = 0;  // 0: exact coarsest solve (<= 1024 cells), else sweeps
+  int mg_inner = 4;          // mg-mixed: most FP32 V-cycles per FP64 residual
   int mg_maxcycles = 100;
 };
 Extras *extras_for(const Parameter *p, bool create);

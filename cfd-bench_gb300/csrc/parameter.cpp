@@ -97,6 +97,7 @@ int apply_extra(Parameter *param, const char *tok, const char *val)
   if (starts_with(tok, "mg_post")) { x->mg_post = atoi(v); hit = 1; }
   if (starts_with(tok, "mg_coarse")) { x->mg_coarse_sweeps = atoi(v); hit = 1; }
   if (starts_with(tok, "mg_cycles")) { x->mg_maxcycles = atoi(v); hit = 1; }
+  if (starts_with(tok, "mg_inner")) { x->mg_inner = atoi(v); hit = 1; }
   return hit;
 }
 

@@ -68,7 +68,7 @@ class OrCase(C.Structure):
                 ("solver", C.c_int), ("levels", C.c_int), ("presmooth", C.c_int),
                 ("postsmooth", C.c_int), ("rtol", C.c_double), ("mg_levels", C.c_int),
                 ("mg_pre", C.c_int), ("mg_post", C.c_int), ("mg_coarse", C.c_int),
-                ("mg_cycles", C.c_int)]
+                ("mg_cycles", C.c_int), ("mg_inner", C.c_int)]
 
 
 class OrState(C.Structure):
@@ -102,7 +102,7 @@ def load(fast: bool = False) -> C.CDLL:
                                     d_p, d_p]
     lib.or_mg_solve.restype = C.c_int
     lib.or_mg_solve.argtypes = [C.POINTER(OrGrid), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
-                                C.c_int, C.c_double, d_p, d_p, d_p]
+                                C.c_int, C.c_int, C.c_double, d_p, d_p, d_p]
     lib.or_mg_levels.restype = C.c_int
     lib.or_mg_levels.argtypes = [C.POINTER(OrGrid), C.c_int, C.POINTER(C.c_int)]
     lib.or_state_init.argtypes = [C.POINTER(OrState), C.POINTER(OrCase)]
@@ -143,7 +143,8 @@ def case_from_values(v: dict, solver: str = "rb") -> OrCase:
     c.levels, c.presmooth, c.postsmooth = v["levels"], v["presmooth"], v["postsmooth"]
     c.rtol = v.get("rtol", 1e-6)
     c.mg_levels, c.mg_pre, c.mg_post = v.get("mg_levels", 0), v.get("mg_pre", 2), v.get("mg_post", 2)
-    c.mg_coarse, c.mg_cycles = v.get("mg_coarse", 64), v.get("mg_cycles", 100)
+    c.mg_coarse, c.mg_cycles = v.get("mg_coarse", 0), v.get("mg_cycles", 100)
+    c.mg_inner = v.get("mg_inner", 4)
     return c
 
 
@@ -300,12 +301,14 @@ def op_solve_mg_ref(g: OrGrid, omega, levels, presmooth, postsmooth, p, rhs) -> 
                                   ptr(rhs))
 
 
-def op_mg_solve(g: OrGrid, mode: str, p, rhs, rtol=1e-6, pre=2, post=2, coarse_sweeps=64,
-                maxcycles=100, level_cap=0):
-    """The library's corrected V-cycle solvers ("mg": FP64, "mg-mixed": FP32 in FP64)."""
+def op_mg_solve(g: OrGrid, mode: str, p, rhs, rtol=1e-6, pre=2, post=2, coarse_sweeps=0,
+                maxcycles=100, level_cap=0, inner=4):
+    """The library's corrected V-cycle solvers ("mg": FP64, "mg-mixed": FP32 in FP64).
+    coarse_sweeps 0: exact coarsest solve; inner: FP32 V-cycles per FP64 residual."""
     rel = C.c_double()
     cyc = load().or_mg_solve(C.byref(g), {"mg": 0, "mg-mixed": 1}[mode], level_cap, pre, post,
-                             coarse_sweeps, maxcycles, rtol, ptr(p), ptr(rhs), C.byref(rel))
+                             coarse_sweeps, inner, maxcycles, rtol, ptr(p), ptr(rhs),
+                             C.byref(rel))
     return cyc, rel.value
 
 

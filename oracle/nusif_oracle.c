@@ -476,7 +476,7 @@ int or_state_step(OrState *s, double *res_out)
     res = or_solve_mg_ref(g, c->omega, c->levels, c->presmooth, c->postsmooth, s->p, s->rhs);
   else
     it = or_mg_solve(g, c->solver - 2, c->mg_levels, c->mg_pre, c->mg_post, c->mg_coarse,
-        c->mg_cycles, c->rtol, s->p, s->rhs, &res);
+        c->mg_inner, c->mg_cycles, c->rtol, s->p, s->rhs, &res);
   or_adapt_uv(g, s->dt, s->f, s->gf, s->h, s->p, s->u, s->v, s->w);
   s->t += s->dt;
   s->nt++;

@@ -69,7 +69,7 @@ double or_solve_mg_ref(const OrGrid *g, double omega, int levels, int presmooth,
  * iterative refinement. Returns V-cycles; *relres = ||b-Ap||/||b||. */
 int or_mg_levels(const OrGrid *g, int cap, int *dims_out);
 int or_mg_solve(const OrGrid *g, int mode, int level_cap, int pre, int post, int coarse_sweeps,
-    int maxcycles, double rtol, double *p, const double *rhs, double *relres);
+    int inner, int maxcycles, double rtol, double *p, const double *rhs, double *relres);
 
 /* whole-run driver mirroring reference src/main.c:53-88 */
 typedef struct {
@@ -86,7 +86,7 @@ typedef struct {
   int solver; /* 0 = rb, 1 = mg-ref, 2 = mg, 3 = mg-mixed */
   int levels, presmooth, postsmooth;
   double rtol;
-  int mg_levels, mg_pre, mg_post, mg_coarse, mg_cycles;
+  int mg_levels, mg_pre, mg_post, mg_coarse, mg_cycles, mg_inner;
 } OrCase;
 
 typedef struct {

@@ -144,17 +144,94 @@ static double mean_free_rhs(const OrGrid *g, const double *rhs, double *b, doubl
 }
 
 /*
+ * Inverse of the coarsest operator deflated by its null space:
+ * M = A - (s/n) 1 1^T with s = 2 sum 1/h^2; -M is SPD, factorised by Cholesky
+ * and inverted column by column (row-major result). For a mean-free b,
+ * x = M^-1 b solves A x = b with mean(x) = 0. Returns NULL on failure.
+ */
+static double *coarse_inverse(const MgLev *L)
+{
+  const int nx = L->n[0], ny = L->n[1], nz = L->n[2], n = nx * ny * nz;
+  const double s = 2.0 * (L->ih2[0] + L->ih2[1] + L->ih2[2]);
+  double *a = (double *)malloc(sizeof(double) * (size_t)n * n);
+  double *minv = (double *)malloc(sizeof(double) * (size_t)n * n);
+  double *y = (double *)malloc(sizeof(double) * (size_t)n);
+  for (size_t q = 0; q < (size_t)n * n; q++) a[q] = s / n;
+  for (int k = 0; k < nz; k++)
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        const int q = i + nx * (j + ny * k);
+        const int idx[3] = { i, j, k }, n3[3] = { nx, ny, nz }, st[3] = { 1, nx, nx * ny };
+        for (int ax = 0; ax < 3; ax++)
+          for (int sg = -1; sg <= 1; sg += 2) {
+            const int c = idx[ax] + sg;
+            if (c < 0 || c >= n3[ax]) continue;
+            a[(size_t)q * n + q] += L->ih2[ax];
+            a[(size_t)q * n + q + sg * st[ax]] -= L->ih2[ax];
+          }
+      }
+  for (int c = 0; c < n; c++) {
+    double d = a[(size_t)c * n + c];
+    for (int q = 0; q < c; q++) d -= a[(size_t)c * n + q] * a[(size_t)c * n + q];
+    if (!(d > 0.0)) {
+      free(a);
+      free(minv);
+      free(y);
+      return NULL;
+    }
+    d = sqrt(d);
+    a[(size_t)c * n + c] = d;
+    for (int r = c + 1; r < n; r++) {
+      double v = a[(size_t)r * n + c];
+      for (int q = 0; q < c; q++) v -= a[(size_t)r * n + q] * a[(size_t)c * n + q];
+      a[(size_t)r * n + c] = v / d;
+    }
+  }
+  for (int col = 0; col < n; col++) {
+    for (int r = 0; r < n; r++) {
+      double v = (r == col) ? 1.0 : 0.0;
+      for (int q = 0; q < r; q++) v -= a[(size_t)r * n + q] * y[q];
+      y[r] = v / a[(size_t)r * n + r];
+    }
+    for (int r = n - 1; r >= 0; r--) {
+      double v = y[r];
+      for (int q = r + 1; q < n; q++) v -= a[(size_t)q * n + r] * y[q];
+      y[r] = v / a[(size_t)r * n + r];
+    }
+    for (int r = 0; r < n; r++) minv[(size_t)r * n + col] = -y[r];
+  }
+  free(a);
+  free(y);
+  return minv;
+}
+
+#define MG_MAX_DIRECT 1024
+
+/*
  * Solve A p = rhs - mean(rhs) on the padded array p (warm start = its
- * interior). mode 0: "mg" (FP64), mode 1: "mg-mixed". Returns the number of
- * V-cycles; *relres = ||b - Ap|| / ||b|| of the returned p. The ghost layer of
- * p is refreshed (Neumann copy) on return.
+ * interior). mode 0: "mg" (FP64), mode 1: "mg-mixed". coarse_sweeps 0 selects
+ * the exact coarsest solve when that level has at most 1024 cells (else, and
+ * for a single-level FP64 solve, 64 sweeps). mode 1 runs up to `inner` FP32
+ * V-cycles per FP64 residual and ends them once ||r - A e||^2 <= (rtol/2)^2
+ * ||b||^2. Returns the number of V-cycles; *relres = ||b - Ap|| / ||b|| of the
+ * returned p. The ghost layer of p is refreshed (Neumann copy) on return.
  */
 int or_mg_solve(const OrGrid *g, int mode, int level_cap, int pre, int post, int coarse_sweeps,
-    int maxcycles, double rtol, double *p, const double *rhs, double *relres)
+    int inner, int maxcycles, double rtol, double *p, const double *rhs, double *relres)
 {
   MgLev lv[MG_MAX_LEVELS];
   int nl = mg_build(g, level_cap, lv);
   size_t n0 = (size_t)g->imax * g->jmax * g->kmax;
+  const MgLev *Lc = &lv[nl - 1];
+  const int nc = Lc->n[0] * Lc->n[1] * Lc->n[2];
+  if (coarse_sweeps == 0 && (nc > MG_MAX_DIRECT || (mode == 0 && nl == 1))) coarse_sweeps = 64;
+  double *minv = coarse_sweeps == 0 ? coarse_inverse(Lc) : NULL;
+  float *minv32 = NULL;
+  if (minv && mode == 1) {
+    minv32 = (float *)malloc(sizeof(float) * (size_t)nc * nc);
+    for (size_t q = 0; q < (size_t)nc * nc; q++) minv32[q] = (float)minv[q];
+  }
+  if (inner < 1) inner = 1;
   double *b0 = (double *)malloc(n0 * sizeof(double));
   double *x0 = (double *)malloc(n0 * sizeof(double));
   double nb2 = 0.0;
@@ -191,7 +268,7 @@ int or_mg_solve(const OrGrid *g, int mode, int level_cap, int pre, int post, int
       cycles = m;
       if (res2 <= tol2 || m >= maxcycles) break;
       if (nl > 1) {
-        mg_vcycle_d(lv, nl, 1, xs, bs, pre, post, coarse_sweeps);
+        mg_vcycle_d(lv, nl, 1, xs, bs, pre, post, coarse_sweeps, minv);
         mg_prolong_add_d(&lv[0], &lv[1], xs[0], xs[1]);
         for (int s = 0; s < post; s++) mg_sweep_d(&lv[0], xs[0], bs[0], 0);
       }
@@ -208,11 +285,25 @@ int or_mg_solve(const OrGrid *g, int mode, int level_cap, int pre, int post, int
       xs[l] = (float *)calloc(nn, sizeof(float));
       bs[l] = (float *)calloc(nn, sizeof(float));
     }
+    const double tol_inner = 0.25 * rtol * rtol * nb2;
     for (int m = 0;; m++) {
       res2 = mg_residual_to_f(&lv[0], x0, b0, bs[0]);
-      cycles = m;
       if (res2 <= tol2 || m >= maxcycles) break;
-      mg_vcycle_f(lv, nl, 0, xs, bs, pre, post, coarse_sweeps);
+      if (nl == 1) {
+        mg_coarsest_f(&lv[0], xs[0], bs[0], coarse_sweeps, minv32);
+        cycles++;
+      } else {
+        for (int q = 0; q < inner; q++) {
+          for (int s = 0; s < pre; s++) mg_sweep_f(&lv[0], xs[0], bs[0], q == 0 && s == 0);
+          if (pre == 0 && q == 0) memset(xs[0], 0, sizeof(float) * n0);
+          const double rin = mg_restrict_f(&lv[0], &lv[1], xs[0], bs[0], bs[1]);
+          cycles++;
+          if (rin <= tol_inner) break;
+          mg_vcycle_f(lv, nl, 1, xs, bs, pre, post, coarse_sweeps, minv32);
+          mg_prolong_add_f(&lv[0], &lv[1], xs[0], xs[1]);
+          for (int s = 0; s < post; s++) mg_sweep_f(&lv[0], xs[0], bs[0], 0);
+        }
+      }
       for (size_t q = 0; q < n0; q++) x0[q] += (double)xs[0][q];
     }
     for (int l = 0; l < nl; l++) {
@@ -229,6 +320,8 @@ int or_mg_solve(const OrGrid *g, int mode, int level_cap, int pre, int post, int
   or_pressure_ghosts(g, p);
   free(b0);
   free(x0);
+  free(minv);
+  free(minv32);
   if (relres) *relres = nb2 > 0.0 ? sqrt(res2 / nb2) : 0.0;
   return cycles;
 }
