@@ -52,7 +52,11 @@ def parse_args():
     ap.add_argument("--solver", default=os.environ.get("NUSIF_BENCH_SOLVER", "auto"))
     ap.add_argument("--n", type=int, default=256, help="cells per axis of the cavity")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="cavity", choices=["cavity", "channel"],
+                    help="cavity: the 256^3 benchmark; channel: mixed vs FP64 error study")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the FP64 multigrid comparison run")
     ap.add_argument("--itermax", type=int, default=None,
                     help="cap of the red-black iterations per step (short profiling runs)")
     return ap.parse_args()
@@ -143,12 +147,41 @@ def pick_solver(requested: str) -> str:
 
 # ---------------------------------------------------------------- GPU arm
 
+def timed_steps(sim, args, stream, local, world):
+    """W untimed steps, then K steps between CUDA events (max over ranks)."""
+    import torch
+    lib = sim.lib
+    for _ in range(args.warmup):
+        sim.step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = lib.nusifLaunchCount()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    infos = [sim.step() for _ in range(args.steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches = lib.nusifLaunchCount() - launches0
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return {"ms_per_step": ms / args.steps, "iters": [i.it for i in infos],
+            "res": [i.res for i in infos], "launches": int(launches), "clocks": clk}
+
+
 def run_gpu(args, rank, world, local):
-    import numpy as np
     import torch
 
     import nusif
-    from nusif import abi
 
     torch.cuda.set_device(local)
     if world > 1 and not torch.distributed.is_initialized():
@@ -163,124 +196,145 @@ def run_gpu(args, rank, world, local):
     i, j, k = sim.dims
     ncell = i * j * k
     padded = (i + 2) * (j + 2) * (k + 2)
+    head = timed_steps(sim, args, stream, local, world)
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-
-    for _ in range(args.warmup):
-        sim.step()
-    torch.cuda.synchronize()
-
-    clocks = ClockSampler(local)
-    clocks.start()
-    launches0 = lib.nusifLaunchCount()
-    barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    infos = [sim.step() for _ in range(args.steps)]
-    e1.record(stream)
-    torch.cuda.synchronize()
-    barrier()
-    launches = lib.nusifLaunchCount() - launches0
-    clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_per_step = ms / args.steps
-    iters = [inf.it for inf in infos]
-    ress = [inf.res for inf in infos]
-
-    # ---- dominant kernel, timed live: the pressure smoother / SOR sweep ----
-    roof = dominant_kernel_roofline(sim, solver, stream, ncell, padded)
+    # ---- dominant kernels, timed live with CUDA events on the library stream ----
+    roofs = kernel_rooflines(sim, solver, stream, ncell)
 
     # ---- e2e: same step through the C ABI with host buffers ----
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(sim, args, stream, padded)
+    sim.close()
+
+    # ---- the comparison the metric names: plain FP64 multigrid, same case ----
+    compare = None
+    if solver == "mg-mixed" and not args.no_compare:
+        sim64 = nusif.Simulation(bench_case(args.n, "mg", args.itermax))
+        ref64 = timed_steps(sim64, args, stream, local, world)
+        sim64.close()
+        compare = {"solver": "mg (FP64 V-cycles, same rtol 1e-6)",
+                   "ms_per_step": ref64["ms_per_step"],
+                   "v_cycles_per_step": ref64["iters"], "residual_per_step": ref64["res"],
+                   "speedup_of_value": ref64["ms_per_step"] / head["ms_per_step"]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(vals, solver, iters)
+        cpu = cpu_baseline(vals, solver, head["iters"])
 
-    sim.close()
     if rank != 0:
         return None
+    tol = ("relative residual 1e-6 (mean-free rhs)" if solver.startswith("mg")
+           else "eps 1e-6 (RMS), itermax %d" % vals["itermax"])
     out = {
         "metric": METRIC,
-        "value": ms_per_step / world,
+        "value": head["ms_per_step"] / world,
         "unit": UNIT,
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": ms_per_step,
+        "ms_per_step": head["ms_per_step"],
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64" if solver in ("rb", "mg", "mg-ref") else "f64+f32",
         "data": "synthetic: lid-driven cavity from rest, no dataset",
         "config": {"workload": f"lid-driven cavity {i}x{j}x{k}, Re 1000, tau 0.5, "
-                               f"solver {solver}",
-                   "cells": ncell, "solver": solver,
-                   "tolerance": "rtol 1e-6" if solver.startswith("mg") else "eps 1e-6 (RMS), itermax 10000",
+                               f"pressure solve {solver}",
+                   "cells": ncell, "solver": solver, "tolerance": tol,
+                   "learned_warm_start": False,
                    "l2": "no flush: 8 FP64 fields of %.0f MB each, far larger than L2" % (padded * 8 / 1e6),
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
-        "solver_iterations_per_step": iters,
-        "residual_per_step": ress,
-        "roofline": roof,
+        "solver_iterations_per_step": head["iters"],
+        "residual_per_step": head["res"],
+        "compare_fp64_mg": compare,
+        "roofline": roofs[0] if roofs else None,
+        "roofline_kernels": roofs,
         "e2e": e2e,
-        "gpu_launches": int(launches),
-        "clocks": clk,
+        "gpu_launches": head["launches"],
+        "clocks": head["clocks"],
         "cpu_baseline": cpu,
     }
     return out
 
 
-def dominant_kernel_roofline(sim, solver, stream, ncell, padded):
-    """Average launch duration of the pressure smoother, from CUDA events."""
+def _traffic(kernel: str, ncell: int):
+    """DRAM bytes per launch of a kernel from the committed ncu summary, scaled by cells."""
+    try:
+        entry = json.loads(TRAFFIC.read_text()).get(kernel)
+        return entry["bytes_per_cell_per_launch"] * ncell if entry else None
+    except Exception:
+        return None
+
+
+def _roof(name, kernel_key, ms, algo_bytes, ncell, peak, src, **extra):
+    achieved = algo_bytes / (ms * 1e-3) / 1e9
+    d = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+         "frac": achieved / peak, "traffic": _traffic(kernel_key, ncell), "kernel": name,
+         "launch_ms": ms, "algorithmic_bytes_per_launch": algo_bytes,
+         "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else src}
+    d.update(extra)
+    return d
+
+
+def kernel_rooflines(sim, solver, stream, ncell):
+    """Average launch duration (CUDA events) of the step's heaviest kernels and
+    their achieved bandwidth on algorithmic bytes. First entry: the dominant one."""
     import torch
     peak, src = hbm_peak()
-    s = sim.s
-    saved = (s.eps, s.itermax)
-    n_it = 40
+    lib = sim.lib
+    out = []
+    ev = lambda: torch.cuda.Event(enable_timing=True)
     if solver == "rb":
+        s = sim.s
+        saved = (s.eps, s.itermax)
+        n_it = 40
         s.eps, s.itermax = 0.0, n_it
-        # warm the chunk size, then time exactly n_it iterations (2 launches each)
-        sim.solve()
+        sim.solve()  # sets the chunk size
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0, e1 = ev(), ev()
         e0.record(stream)
         sim.solve()
         e1.record(stream)
         torch.cuda.synchronize()
         s.eps, s.itermax = saved
-        launches = 2 * n_it
-        per_launch_ms = e0.elapsed_time(e1) / launches
-        kernel = "k_sor_pass (one colour of a red-black SOR iteration, FP64)"
-        # algorithmic bytes: p read + p write + rhs read = 24 B per cell per iteration
-        bytes_per_launch = 12.0 * ncell
-    else:
-        return {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
-                "traffic": None, "kernel": "multigrid smoother", "peak_source": src}
-    achieved = bytes_per_launch / (per_launch_ms * 1e-3) / 1e9
-    traffic = None
-    try:
-        tr = json.loads(TRAFFIC.read_text())
-        entry = tr.get("k_sor_pass")
-        if entry:
-            traffic = entry["bytes_per_cell_per_launch"] * ncell
-    except Exception:
-        pass
-    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": traffic, "kernel": kernel,
-            "launch_ms": per_launch_ms, "algorithmic_bytes_per_launch": bytes_per_launch,
-            "peak_source": src,
-            "note": "FP64-pipe bound on GB300 (about 1.2 TFLOP/s FP64): see fp64 fields",
-            "fp64_instr_per_cell": 10,
-            "fp64_tflops_equiv": 20.0 * ncell / 2 / (per_launch_ms * 1e-3) / 1e12}
+        ms = e0.elapsed_time(e1) / (2 * n_it)
+        out.append(_roof("k_sor_pass: one colour of a red-black SOR iteration (FP64)",
+                         "k_sor_pass", ms, 12.0 * ncell, ncell, peak, src,
+                         note="FP64-pipe bound: 10 FP64 instructions per update",
+                         fp64_tflops=20.0 * ncell / 2 / (ms * 1e-3) / 1e12))
+    elif solver in ("mg", "mg-mixed"):
+        from nusif import abi
+        msr = C.c_double()
+        reps = 20
+        lib.nusifTimeKernel(C.byref(sim.s), sim.d.p, sim.d.rhs, 0, reps, C.byref(msr))
+        abi.check(lib)
+        if solver == "mg-mixed":
+            out.append(_roof("k_mg_smooth<float>: one colour pass of the fine FP32 smoother",
+                             "k_mg_smooth_f32", msr.value, 6.0 * ncell, ncell, peak, src))
+            lib.nusifTimeKernel(C.byref(sim.s), sim.d.p, sim.d.rhs, 1, reps, C.byref(msr))
+            abi.check(lib)
+            out.append(_roof("k_mx_residual: FP64 residual of p into FP32 (refinement)",
+                             "k_mx_residual", msr.value, 20.0 * ncell, ncell, peak, src,
+                             note="FP64-pipe bound"))
+        else:
+            out.append(_roof("k_mg_smooth<double>: one colour pass of the fine FP64 smoother",
+                             "k_mg_smooth_f64", msr.value, 12.0 * ncell, ncell, peak, src,
+                             note="FP64-pipe bound"))
+    # computeFG (flux form): reads u, v, w, writes f, g, h; idempotent for fixed u, v, w
+    sim.compute_fg()
+    torch.cuda.synchronize()
+    e0, e1 = ev(), ev()
+    reps = 5
+    e0.record(stream)
+    for _ in range(reps):
+        sim.compute_fg()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    out.append(_roof("k_fgh_flux: computeFG (FP64)", "k_fgh_flux",
+                     e0.elapsed_time(e1) / reps, 48.0 * ncell, ncell, peak, src,
+                     note="FP64-pipe bound: about 85 FP64 instructions per cell"))
+    return out
 
 
 def run_e2e(sim, args, stream, padded):
@@ -387,11 +441,80 @@ def run_reference(args, rank, world):
     }
 
 
+class DeviceArray:
+    """A device pointer seen by torch (plumbing for error norms on the GPU)."""
+
+    def __init__(self, ptr, shape):
+        self.__cuda_array_interface__ = {"shape": shape, "typestr": "<f8",
+                                         "data": (ctypes_addr(ptr), False), "version": 3}
+
+
+def ctypes_addr(p) -> int:
+    return C.cast(p, C.c_void_p).value
+
+
+def run_channel(args, local):
+    """Channel flow 4x1x1 at 512x128x128 (inflow 1 at x=0, outflow at x=4,
+    no-slip side walls, Re 100, fields from zero): mixed-precision multigrid
+    and FP64 multigrid, both to a 1e-8 relative residual, stepped side by side;
+    per-step relative L2 and Linf differences of u, v, w, p (p without its mean)."""
+    import torch
+
+    import nusif
+    from nusif.params import channel
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    lib = nusif.load_library()
+    lib.nusifSetStream(C.c_void_p(stream.cuda_stream))
+    steps = args.steps
+    sims = {s: nusif.Simulation(channel(solver=s, rtol=1e-8)) for s in ("mg-mixed", "mg")}
+    shape = sims["mg"].padded_shape
+
+    def view(sim, f):
+        return torch.as_tensor(DeviceArray(getattr(sim.d, f), shape), device="cuda")[1:-1, 1:-1, 1:-1]
+
+    err = {f: {"l2": [], "linf": []} for f in "uvwp"}
+    ms = {s: 0.0 for s in sims}
+    cycles = {s: [] for s in sims}
+    for _ in range(steps):
+        for s, sim in sims.items():
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            info = sim.step()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms[s] += e0.elapsed_time(e1)
+            cycles[s].append(info.it)
+        for f in "uvwp":
+            a, b = view(sims["mg-mixed"], f), view(sims["mg"], f)
+            if f == "p":
+                a, b = a - a.mean(), b - b.mean()
+            d = a - b
+            err[f]["l2"].append(float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(b).clamp_min(1e-300)))
+            err[f]["linf"].append(float(d.abs().max() / b.abs().max().clamp_min(1e-300)))
+    for sim in sims.values():
+        sim.close()
+    return {
+        "metric": "channel 512x128x128, 4x1x1, Re 100: mixed-precision vs FP64 multigrid field error",
+        "value": max(max(err[f]["l2"]) for f in "uvwp"), "unit": "max relative L2 difference",
+        "higher_is_better": False, "steps": steps, "n_gpus": 1,
+        "config": {"workload": "channel flow 512x128x128, inflow 1, outflow, no-slip walls, "
+                               "Re 100, fields from zero", "rtol": 1e-8},
+        "ms_per_step": {s: ms[s] / steps for s in ms},
+        "v_cycles_per_step_mean": {s: sum(c) / len(c) for s, c in cycles.items()},
+        "error_final": {f: {k: v[-1] for k, v in err[f].items()} for f in "uvwp"},
+        "error_max": {f: {k: max(v) for k, v in err[f].items()} for f in "uvwp"},
+        "error_every_50": {f: err[f]["l2"][::50] for f in "uvwp"},
+    }
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_info()
     if args.impl == "reference":
         out = run_reference(args, rank, world)
+    elif args.workload == "channel":
+        out = run_channel(args, local) if rank == 0 else None
     else:
         out = run_gpu(args, rank, world, local)
     if out is not None and rank == 0:

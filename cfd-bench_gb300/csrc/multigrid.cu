@@ -120,11 +120,11 @@ __device__ __forceinline__ T lap_at(const View<T> &v, const T *x, int i, int j, 
 
 // One colour of a red-black Gauss-Seidel sweep. ZERO: the sweep starts from
 // x = 0 (the centre is not read; in the odd pass neither are neighbours).
-// FOLD: after the update, p += x for both cells of the pair and the Neumann
-// ghosts of p are refreshed (mixed precision, last fine pass).
-template <typename T, bool ZERO, bool FOLD>
+// A thread owns the cell pair (2t, 2t+1) of a row and relaxes the one of the
+// pass's colour, walking kb planes.
+template <typename T, bool ZERO>
 __global__ void __launch_bounds__(kNT) k_mg_smooth(View<T> v, int colour, const double *shift,
-    int kb, const MgState *st, double *p, int p_sj, int p_sk)
+    int kb, const MgState *st)
 {
   if (mg_done(st)) return;
   const int t = blockIdx.x * kBX + threadIdx.x;
@@ -135,36 +135,66 @@ __global__ void __launch_bounds__(kNT) k_mg_smooth(View<T> v, int colour, const 
   const int k1 = min(k0 + kb, v.nz);
   for (int k = k0; k < k1; k++) {
     const int i = 2 * t + (((j + k + 1) & 1) == colour ? 0 : 1);
-    const int64_t row = v.off + (int64_t)k * v.sz + (int64_t)j * v.sy;
-    if (i < v.nx) {
-      const int64_t c = row + i;
-      T r;
-      if (ZERO && colour == 1) {
-        r = v.b[c] - sh;
-        v.x[c] = -r * v.inv_diag;
-      } else {
-        const T xc = ZERO ? (T)0 : v.x[c];
-        r = (v.b[c] - sh) - lap_at(v, v.x, i, j, k, c, xc);
-        v.x[c] = xc - r * v.inv_diag;
-      }
+    if (i >= v.nx) continue;
+    const int64_t c = v.off + (int64_t)k * v.sz + (int64_t)j * v.sy + i;
+    if (ZERO && colour == 1) {
+      v.x[c] = -(v.b[c] - sh) * v.inv_diag;
+    } else {
+      const T xc = ZERO ? (T)0 : v.x[c];
+      const T r = (v.b[c] - sh) - lap_at(v, v.x, i, j, k, c, xc);
+      v.x[c] = xc - r * v.inv_diag;
     }
-    if (FOLD) {
-#pragma unroll
-      for (int e = 0; e < 2; e++) {
-        const int ii = 2 * t + e;
-        if (ii >= v.nx) continue;
-        const double val = (double)v.x[row + ii];
-        const int64_t pc = (int64_t)(k + 1) * p_sk + (int64_t)(j + 1) * p_sj + (ii + 1);
-        const double np = p[pc] + val;
-        p[pc] = np;
-        if (ii == 0) p[pc - 1] = np;
-        if (ii == v.nx - 1) p[pc + 1] = np;
-        if (j == 0) p[pc - p_sj] = np;
-        if (j == v.ny - 1) p[pc + p_sj] = np;
-        if (k == 0) p[pc - p_sk] = np;
-        if (k == v.nz - 1) p[pc + p_sk] = np;
-      }
+  }
+}
+
+// The FP32 pass on levels with an even row length (every coarsened level and
+// even fine grids): the pair (2t, 2t+1) is read as one 8-byte vector in the
+// row and in the four neighbouring rows, the far x-neighbour comes from the
+// adjacent lane, so each warp reads whole 32-byte sectors. Same arithmetic
+// as k_mg_smooth<float>.
+template <bool ZERO>
+__global__ void __launch_bounds__(kNT) k_mg_smooth_f2(View<float> v, int colour, int kb,
+    const MgState *st)
+{
+  if (mg_done(st)) return;
+  const int t = blockIdx.x * kBX + threadIdx.x;
+  const int j = blockIdx.y * kBY + threadIdx.y;
+  const int k0 = blockIdx.z * kb;
+  if (j >= v.ny) return;  // whole warps: a warp is one row of 32 threads
+  const int k1 = min(k0 + kb, v.nz);
+  const int npair = v.nx >> 1;
+  const bool live = t < npair;
+  const int tt = live ? t : npair - 1;  // loads stay in the row
+  for (int k = k0; k < k1; k++) {
+    const int a = ((j + k + 1) & 1) == colour ? 0 : 1;  // which cell of the pair is updated
+    const int i = 2 * tt + a;
+    const int64_t row = (int64_t)k * v.sz + (int64_t)j * v.sy;
+    const float2 pc = *reinterpret_cast<const float2 *>(v.x + row + 2 * tt);
+    // neighbours across the pair boundary: lane-1's right cell, lane+1's left cell
+    float left = __shfl_up_sync(0xffffffffu, pc.y, 1);
+    float right = __shfl_down_sync(0xffffffffu, pc.x, 1);
+    if (threadIdx.x == 0 && tt > 0) left = v.x[row + 2 * tt - 1];
+    if (threadIdx.x == kBX - 1 && tt + 1 < npair) right = v.x[row + 2 * tt + 2];
+    const float xc = ZERO ? 0.0f : (a ? pc.y : pc.x);
+    float xw = a ? pc.x : left;    // x(i-1)
+    float xe = a ? right : pc.y;   // x(i+1)
+    if (i == 0) xw = xc;
+    if (i == v.nx - 1) xe = xc;
+    const int64_t c = row + i;
+    const int64_t pair = row + 2 * tt;
+    auto pick = [a](float2 q) { return a ? q.y : q.x; };
+    const float bc = pick(*reinterpret_cast<const float2 *>(v.b + pair));
+    if (ZERO && colour == 1) {
+      if (live) v.x[c] = -bc * v.inv_diag;
+      continue;
     }
+    const float ys = j > 0 ? pick(*reinterpret_cast<const float2 *>(v.x + pair - v.sy)) : xc;
+    const float yn = j < v.ny - 1 ? pick(*reinterpret_cast<const float2 *>(v.x + pair + v.sy)) : xc;
+    const float zb = k > 0 ? pick(*reinterpret_cast<const float2 *>(v.x + pair - v.sz)) : xc;
+    const float zt = k < v.nz - 1 ? pick(*reinterpret_cast<const float2 *>(v.x + pair + v.sz)) : xc;
+    const float lap = (xw + xe) * v.ex + (ys + yn) * v.ey + (zb + zt) * v.ez - v.diag * xc;
+    const float r = bc - lap;
+    if (live) v.x[c] = xc - r * v.inv_diag;
   }
 }
 
@@ -314,6 +344,58 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong(View<T> f, const T *xc, int 
     const int64_t c = f.off + (int64_t)fi[2] * f.sz + (int64_t)fi[1] * f.sy + fi[0];
     f.x[c] += y0 + w[2] * (y1 - y0);
   }
+}
+
+// x_f += trilinear interpolation of x_c when x was coarsened (rx == 2): one
+// thread per coarse x-position and fine (j, k) produces both x-children, so
+// the three coarse values of each (y, z) line are loaded once for two cells.
+// Same interpolation order as k_mg_prolong (x, then y, then z).
+template <typename T>
+__global__ void __launch_bounds__(kNT) k_mg_prolong_x2(View<T> f, const T *xc, int cnx, int cny,
+    int cnz, int ry, int rz, const MgState *st)
+{
+  if (mg_done(st)) return;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z * blockDim.z + threadIdx.z;
+  if (I >= cnx || j >= f.ny || k >= f.nz) return;
+  int Py, Qy, Pz, Qz;
+  T wy, wz;
+  if (ry == 2) {
+    Py = j >> 1;
+    const int nb = (j & 1) ? Py + 1 : Py - 1;
+    Qy = (nb < 0 || nb >= cny) ? Py : nb;
+    wy = (T)0.25;
+  } else {
+    Py = Qy = j;
+    wy = (T)0;
+  }
+  if (rz == 2) {
+    Pz = k >> 1;
+    const int nb = (k & 1) ? Pz + 1 : Pz - 1;
+    Qz = (nb < 0 || nb >= cnz) ? Pz : nb;
+    wz = (T)0.25;
+  } else {
+    Pz = Qz = k;
+    wz = (T)0;
+  }
+  const int Im = I > 0 ? I - 1 : I, Ip = I < cnx - 1 ? I + 1 : I;
+  const int64_t sy = cnx, sz = (int64_t)cnx * cny;
+  T lo[2][2], hi[2][2];
+#pragma unroll
+  for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+    for (int dy = 0; dy < 2; dy++) {
+      const int64_t base = (int64_t)(dz ? Qz : Pz) * sz + (int64_t)(dy ? Qy : Py) * sy;
+      const T a0 = xc[base + I];
+      lo[dz][dy] = a0 + (T)0.25 * (xc[base + Im] - a0);
+      hi[dz][dy] = a0 + (T)0.25 * (xc[base + Ip] - a0);
+    }
+  const T ly0 = lo[0][0] + wy * (lo[0][1] - lo[0][0]), ly1 = lo[1][0] + wy * (lo[1][1] - lo[1][0]);
+  const T hy0 = hi[0][0] + wy * (hi[0][1] - hi[0][0]), hy1 = hi[1][0] + wy * (hi[1][1] - hi[1][0]);
+  const int64_t c = f.off + (int64_t)k * f.sz + (int64_t)j * f.sy + 2 * I;
+  f.x[c] += ly0 + wz * (ly1 - ly0);
+  f.x[c + 1] += hy0 + wz * (hy1 - hy0);
 }
 
 // Coarsest level: `sweeps` red-black Gauss-Seidel sweeps from zero by one
@@ -582,36 +664,32 @@ int planes_per_block(int nx, int ny, int nz)
   return kb;
 }
 
-template <typename T, bool ZERO, bool FOLD>
-bool smooth_pass(const View<T> &v, int colour, const double *shift, const MgState *st,
-    double *p = nullptr)
+template <typename T, bool ZERO>
+bool smooth_pass(const View<T> &v, int colour, const double *shift, const MgState *st)
 {
   const int kb = planes_per_block(v.nx, v.ny, v.nz);
   dim3 grid(((v.nx + 1) / 2 + kBX - 1) / kBX, (v.ny + kBY - 1) / kBY, (v.nz + kb - 1) / kb);
-  const int p_sj = v.nx + 2, p_sk = (v.nx + 2) * (v.ny + 2);
-  k_mg_smooth<T, ZERO, FOLD><<<grid, dim3(kBX, kBY), 0, stream()>>>(v, colour, shift, kb, st, p,
-      p_sj, p_sk);
+  if constexpr (sizeof(T) == sizeof(float)) {
+    // paired loads need every row to start on an even cell (compact, even nx)
+    if (v.off == 0 && v.nx % 2 == 0 && shift == nullptr) {
+      k_mg_smooth_f2<ZERO><<<grid, dim3(kBX, kBY), 0, stream()>>>(v, colour, kb, st);
+      return launched("k_mg_smooth_f2");
+    }
+  }
+  k_mg_smooth<T, ZERO><<<grid, dim3(kBX, kBY), 0, stream()>>>(v, colour, shift, kb, st);
   return launched("k_mg_smooth");
 }
 
-// `count` sweeps; the first from zero when zero_first; the last even pass
-// folds into p when p != nullptr
+// `count` sweeps (odd colour, then even); the first from zero when zero_first
 template <typename T>
 bool sweeps(const View<T> &v, int count, bool zero_first, const double *shift,
-    const MgState *st, double *p = nullptr)
+    const MgState *st)
 {
   for (int s = 0; s < count; s++) {
     const bool z = zero_first && s == 0;
-    const bool fold = p != nullptr && s == count - 1;
-    bool ok = z ? smooth_pass<T, true, false>(v, 1, shift, st)
-                : smooth_pass<T, false, false>(v, 1, shift, st);
+    bool ok = z ? smooth_pass<T, true>(v, 1, shift, st) : smooth_pass<T, false>(v, 1, shift, st);
     if (!ok) return false;
-    if (fold)
-      ok = z ? smooth_pass<T, true, true>(v, 0, shift, st, p)
-             : smooth_pass<T, false, true>(v, 0, shift, st, p);
-    else
-      ok = z ? smooth_pass<T, true, false>(v, 0, shift, st)
-             : smooth_pass<T, false, false>(v, 0, shift, st);
+    ok = z ? smooth_pass<T, true>(v, 0, shift, st) : smooth_pass<T, false>(v, 0, shift, st);
     if (!ok) return false;
   }
   return true;
@@ -643,6 +721,13 @@ bool restrict_to(const View<T> &f, T *bc, const MgLevelDesc &C, const double *sh
 template <typename T>
 bool prolong_to(const View<T> &f, const T *xc, const MgLevelDesc &C, const MgState *st)
 {
+  if (C.r[0] == 2) {
+    const dim3 blk(32, 4, 2);
+    const dim3 grid((C.n[0] + 31) / 32, (f.ny + 3) / 4, (f.nz + 1) / 2);
+    k_mg_prolong_x2<T><<<grid, blk, 0, stream()>>>(f, xc, C.n[0], C.n[1], C.n[2], C.r[1], C.r[2],
+        st);
+    return launched("k_mg_prolong_x2");
+  }
   const int64_t nf = (int64_t)f.nx * f.ny * f.nz;
   k_mg_prolong<T><<<flat_blocks(nf), kNT, 0, stream()>>>(f, xc, C.n[0], C.n[1], C.n[2], C.r[0],
       C.r[1], C.r[2], st);
@@ -880,6 +965,67 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
   if (v && v[0] && v[0] != '0')
     printf("Multigrid took %d V-cycles to reach relative residual %e\n", h->cycles, rel);
   return rel;
+}
+
+// Average duration of `reps` launches of one fine-level kernel, between CUDA
+// events on the library stream: which = 0 the fine smoother pass (FP32 for
+// mg-mixed, FP64 for mg), 1 the FP64 residual of mg-mixed. It works on
+// scratch copies or on the solver's own FP32 arrays, never on p; a private
+// state that never stops keeps the kernels active.
+bool mg_time_kernel(SolverState *ss, const double *p, const double *rhs, int which, int reps,
+    double *ms_out)
+{
+  MgHierarchy *H = ss->mg;
+  if (!H || reps < 1) return false;
+  MgState host_st;
+  memset(&host_st, 0, sizeof(host_st));
+  host_st.maxcycles = 1 << 30;
+  host_st.tol2 = -1.0;
+  host_st.tol_inner = -1.0;
+  MgState *tst = nullptr;
+  double *pcopy = nullptr;
+  const size_t padded = (size_t)(H->lv[0].n[0] + 2) * (H->lv[0].n[1] + 2) * (H->lv[0].n[2] + 2);
+  bool ok = cuda_ok(cudaMalloc(&tst, sizeof(MgState)), "cudaMalloc(timing state)") &&
+            cuda_ok(cudaMemcpy(tst, &host_st, sizeof(MgState), cudaMemcpyHostToDevice),
+                "timing state upload") &&
+            cuda_ok(cudaMalloc(&pcopy, padded * sizeof(double)), "cudaMalloc(timing p)") &&
+            cuda_ok(cudaMemcpyAsync(pcopy, p, padded * sizeof(double), cudaMemcpyDeviceToDevice,
+                        stream()),
+                "timing p copy");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  View<double> v0 = padded_view(H->lv[0], pcopy, rhs);
+  const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
+  if (ok) {
+    // one untimed launch, then the timed ones
+    for (int q = 0; q <= reps && ok; q++) {
+      if (q == 1) cudaEventRecord(e0, stream());
+      if (which == 1 && H->mode == 1) {
+        k_mx_residual<<<flat_blocks(n0), kNT, 0, stream()>>>(v0, H->b32[0], tst, H->red.partials,
+            H->red.ticket, 0);
+        ok = launched("k_mx_residual");
+      } else if (H->mode == 1) {
+        View<float> v = compact_view<float>(H->lv[0], H->x32[0], H->b32[0]);
+        ok = smooth_pass<float, false>(v, q & 1, nullptr, tst);
+      } else {
+        ok = smooth_pass<double, false>(v0, q & 1, nullptr, tst);
+      }
+    }
+    cudaEventRecord(e1, stream());
+  }
+  float ms = 0.0f;
+  if (ok && cuda_ok(cudaEventSynchronize(e1), "timing sync")) {
+    cudaEventElapsedTime(&ms, e0, e1);
+    *ms_out = ms / reps;
+  } else {
+    ok = false;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (tst) cudaFree(tst);
+  if (pcopy) cudaFree(pcopy);
+  return ok;
 }
 
 void mg_free(Solver *s, SolverState *ss)

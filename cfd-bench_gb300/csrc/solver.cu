@@ -444,6 +444,21 @@ int nusifSolverIterations(const Solver *s)
   return ss ? ss->last_iterations : -1;
 }
 
+int nusifTimeKernel(Solver *s, const double *p, const double *rhs, int which, int reps,
+    double *ms_out)
+{
+  SolverState *ss = solver_state(s);
+  if (!ss || !ms_out || reps < 1) {
+    fail(NUSIF_ERR_ARG, "nusifTimeKernel: unknown solver or bad arguments");
+    return NUSIF_ERR_ARG;
+  }
+  if (ss->kind != SOLVER_MG && ss->kind != SOLVER_MG_MIXED) {
+    fail(NUSIF_ERR_ARG, "nusifTimeKernel: only the mg and mg-mixed solvers have timing hooks");
+    return NUSIF_ERR_ARG;
+  }
+  return mg_time_kernel(ss, p, rhs, which, reps, ms_out) ? NUSIF_OK : NUSIF_ERR_CUDA;
+}
+
 void nusifFreeSolver(Solver *s)
 {
   SolverState *ss = solver_state(s);

@@ -50,5 +50,7 @@ SolverState *solver_state(const Solver *s);
 bool mg_setup(Solver *s, Discretization *d, SolverState *ss);
 double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs);
 void mg_free(Solver *s, SolverState *ss);
+bool mg_time_kernel(SolverState *ss, const double *p, const double *rhs, int which, int reps,
+    double *ms_out);
 
 }  // namespace nusif

@@ -101,6 +101,8 @@ SIGNATURES = [
                                      c_double_p, c_double_p]),
     ("nusifWriteVTK", C.c_int, [C.POINTER(Discretization), C.c_char_p, C.c_int]),
     ("nusifLaunchCount", C.c_ulonglong, []),
+    ("nusifTimeKernel", C.c_int, [C.POINTER(Solver), c_double_p, c_double_p, C.c_int, C.c_int,
+                                  C.POINTER(C.c_double)]),
     ("nusifVersion", C.c_char_p, []),
 ]
 

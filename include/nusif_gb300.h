@@ -191,6 +191,12 @@ NUSIF_API int nusifCollectResult(const Discretization *d, double *ug, double *vg
 NUSIF_API int nusifWriteVTK(const Discretization *d, const char *path, int binary);
 /* kernels this library launched since it was loaded (observability) */
 NUSIF_API unsigned long long nusifLaunchCount(void);
+/* Measurement hook (mg and mg-mixed solvers): average duration in ms of `reps`
+ * launches of one fine-level kernel, timed with CUDA events on the library
+ * stream; which = 0 the fine smoother pass, 1 the FP64 residual of mg-mixed.
+ * Works on scratch copies: p and rhs are only read. */
+NUSIF_API int nusifTimeKernel(Solver *s, const double *p, const double *rhs, int which, int reps,
+    double *ms_out);
 /* library version string */
 NUSIF_API const char *nusifVersion(void);
 
