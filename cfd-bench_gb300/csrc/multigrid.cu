@@ -76,7 +76,8 @@ struct MgHierarchy {
   MgLevelDesc lv[kMaxLevels];
   double *x64[kMaxLevels] = {};
   double *b64[kMaxLevels] = {};
-  float *x32[kMaxLevels] = {};
+  float *x32[kMaxLevels] = {};   // current FP32 unknown of each level
+  float *x32b[kMaxLevels] = {};  // its ping-pong partner for the one-kernel sweep
   float *b32[kMaxLevels] = {};
   MgState *d_state = nullptr;
   MgState *h_state = nullptr;
@@ -343,6 +344,107 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong(View<T> f, const T *xc, int 
     const T y1 = v[1][0] + w[1] * (v[1][1] - v[1][0]);
     const int64_t c = f.off + (int64_t)fi[2] * f.sz + (int64_t)fi[1] * f.sy + fi[0];
     f.x[c] += y0 + w[2] * (y1 - y0);
+  }
+}
+
+// One whole red-black Gauss-Seidel sweep in one kernel, exact: reads x_old,
+// writes x_new (ping-pong), so no block ever reads a value another block
+// writes. A block owns a TX x TY tile of (i, j) columns and a chunk of planes;
+// per plane it stages x_old with a two-cell ring in shared memory, relaxes the
+// odd ("red") cells on the tile plus a one-cell ring (from old even values,
+// exactly what the first pass of a two-pass sweep computes there), then the
+// even cells of the previous plane on the tile (from the new odd values and
+// their own old value), and writes both colours of that plane. Planes walk
+// with a one-plane lag (odd at k, even at k-1); the odd planes just outside
+// the chunk are recomputed, so chunks are independent. One sweep reads x and
+// b once and writes x once. ZERO: x_old is zero (not read).
+constexpr int kSX = 64, kSY = 8;              // tile (cells)
+constexpr int kRX = kSX + 4, kRY = kSY + 4;   // staged x_old: tile + 2-cell ring
+constexpr int kQX = kSX + 2, kQY = kSY + 2;   // odd values: tile + 1-cell ring
+
+template <typename T, bool ZERO>
+__global__ void __launch_bounds__(256) k_rbgs_sweep(View<T> v, T *__restrict__ xnew, int kc,
+    const MgState *st)
+{
+  if (mg_done(st)) return;
+  __shared__ T xo[3][kRY][kRX];  // x_old planes (slot = plane mod 3), tile + 2-cell ring
+  __shared__ T xr[3][kQY][kQX];  // new odd values (slot = plane mod 3), tile + 1-cell ring
+  const T *__restrict__ xold = v.x;
+  const T *__restrict__ b = v.b;
+  const int nx = v.nx, ny = v.ny, nz = v.nz;
+  const int i0 = blockIdx.x * kSX, j0 = blockIdx.y * kSY;
+  const int k0 = blockIdx.z * kc, k1 = min(k0 + kc, nz);
+  const int tid = threadIdx.x;
+  // x_old of plane k into its slot; positions outside the domain are filled
+  // from the nearest cell but never used (the boundary tests below)
+  auto stage = [&](int k) {
+    if (k < 0 || k >= nz) return;
+    T(*dst)[kRX] = xo[k % 3];
+    for (int q = tid; q < kRX * kRY; q += 256) {
+      const int li = q % kRX, lj = q / kRX;
+      const int gi = min(max(i0 - 2 + li, 0), nx - 1), gj = min(max(j0 - 2 + lj, 0), ny - 1);
+      dst[lj][li] = ZERO ? (T)0 : xold[(int64_t)k * v.sz + (int64_t)gj * v.sy + gi];
+    }
+  };
+  stage(k0 - 2);
+  stage(k0 - 1);
+  for (int k = k0 - 1; k <= k1; k++) {
+    stage(k + 1);
+    __syncthreads();
+    // odd cells ((i+j+k) odd, 1-based) of plane k on the tile + 1-cell ring
+    if (k >= 0 && k < nz) {
+      T(*rq)[kQX] = xr[k % 3];
+      const T(*xk)[kRX] = xo[k % 3];
+      const T(*xkm)[kRX] = xo[(k + 2) % 3];
+      const T(*xkp)[kRX] = xo[(k + 1) % 3];
+      for (int q = tid; q < (kQX / 2) * kQY; q += 256) {
+        const int lj = q / (kQX / 2), pi = q % (kQX / 2);
+        const int gj = j0 - 1 + lj;
+        // first region column that holds an odd cell in this row
+        const int li = 2 * pi + (((i0 - 1 + gj + k + 3) & 1) ? 0 : 1);
+        const int gi = i0 - 1 + li;
+        if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
+        const int si = li + 1, sj = lj + 1;
+        const T xc = xk[sj][si];
+        const T sx = (gi > 0 ? xk[sj][si - 1] : xc) + (gi < nx - 1 ? xk[sj][si + 1] : xc);
+        const T sy = (gj > 0 ? xk[sj - 1][si] : xc) + (gj < ny - 1 ? xk[sj + 1][si] : xc);
+        const T sz = (k > 0 ? xkm[sj][si] : xc) + (k < nz - 1 ? xkp[sj][si] : xc);
+        const T lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
+        const T r = b[(int64_t)k * v.sz + (int64_t)gj * v.sy + gi] - lap;
+        rq[lj][li] = xc - r * v.inv_diag;
+      }
+    }
+    __syncthreads();
+    // even cells of plane k-1 on the tile, one cell pair per thread; both
+    // cells of the pair are written to x_new
+    const int ke = k - 1;
+    if (ke >= k0 && ke < k1) {
+      const T(*rm)[kQX] = xr[(ke + 2) % 3];  // plane ke-1
+      const T(*r0)[kQX] = xr[ke % 3];        // plane ke
+      const T(*rp)[kQX] = xr[(ke + 1) % 3];  // plane ke+1
+      const T(*xe)[kRX] = xo[ke % 3];
+      const int tj = tid / (kSX / 2), pi = tid % (kSX / 2);
+      const int gj = j0 + tj;
+      const int te = 2 * pi + ((i0 + gj + ke + 3) & 1);  // even cell of the pair
+      const int to = te ^ 1;                             // odd cell of the pair
+      const int lj = tj + 1;
+      if (gj < ny) {
+        const int gi = i0 + te;
+        if (gi < nx) {
+          const int li = te + 1;
+          const T xc = xe[lj + 1][li + 1];
+          const T sx = (gi > 0 ? r0[lj][li - 1] : xc) + (gi < nx - 1 ? r0[lj][li + 1] : xc);
+          const T sy = (gj > 0 ? r0[lj - 1][li] : xc) + (gj < ny - 1 ? r0[lj + 1][li] : xc);
+          const T sz = (ke > 0 ? rm[lj][li] : xc) + (ke < nz - 1 ? rp[lj][li] : xc);
+          const T lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
+          const int64_t c = (int64_t)ke * v.sz + (int64_t)gj * v.sy + gi;
+          xnew[c] = xc - (b[c] - lap) * v.inv_diag;
+        }
+        const int go = i0 + to;
+        if (go < nx) xnew[(int64_t)ke * v.sz + (int64_t)gj * v.sy + go] = r0[lj][to + 1];
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -756,6 +858,44 @@ bool coarse_solve(const View<T> &v, int nsweeps, const MgState *st, const T *min
 // V-cycle from level l on the compact arrays xs/bs of type T. x_l starts at
 // zero when `zero` (always below the top level); `inner_test`: the fine
 // restriction folds the residual norm for the mixed-precision inner stop.
+// `count` whole red-black sweeps of an FP32 level with the one-kernel sweep;
+// each swaps the level's current and ping-pong buffers (x32[l] stays current)
+bool fused_sweeps(MgHierarchy *H, int l, int count, bool zero_first, const MgState *st)
+{
+  const MgLevelDesc &L = H->lv[l];
+  const int gx = (L.n[0] + kSX - 1) / kSX, gy = (L.n[1] + kSY - 1) / kSY;
+  int kc = 32;
+  while (kc > 4 && (int64_t)gx * gy * ((L.n[2] + kc - 1) / kc) < 8 * sm_count_mg()) kc >>= 1;
+  const dim3 grid(gx, gy, (L.n[2] + kc - 1) / kc);
+  for (int s = 0; s < count; s++) {
+    const View<float> v = compact_view<float>(L, H->x32[l], H->b32[l]);
+    if (zero_first && s == 0)
+      k_rbgs_sweep<float, true><<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st);
+    else
+      k_rbgs_sweep<float, false><<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st);
+    if (!launched("k_rbgs_sweep")) return false;
+    float *t = H->x32[l];
+    H->x32[l] = H->x32b[l];
+    H->x32b[l] = t;
+  }
+  return true;
+}
+
+template <typename T>
+bool level_sweeps(MgHierarchy *H, int l, View<T> &v, int count, bool zero_first,
+    const MgState *st)
+{
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (!fused_sweeps(H, l, count, zero_first, st)) return false;
+    v.x = reinterpret_cast<T *>(H->x32[l]);
+    return true;
+  } else {
+    (void)H;
+    (void)l;
+    return sweeps<T>(v, count, zero_first, nullptr, st);
+  }
+}
+
 template <typename T>
 bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero, bool inner_test)
 {
@@ -772,7 +912,7 @@ bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero, bool inner_test)
     return coarse_solve<T>(v, H->coarse_sweeps, st, minv);
   }
   if (H->pre > 0) {
-    if (!sweeps<T>(v, H->pre, zero, nullptr, st)) return false;
+    if (!level_sweeps<T>(H, l, v, H->pre, zero, st)) return false;
   } else if (zero && !cuda_ok(cudaMemsetAsync(xs[l], 0, n * sizeof(T), stream()), "zero x")) {
     return false;
   }
@@ -782,7 +922,7 @@ bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero, bool inner_test)
   if (!ok) return false;
   if (!vcycle<T>(H, l + 1, xs, bs, true, false)) return false;
   if (!prolong_to<T>(v, xs[l + 1], H->lv[l + 1], st)) return false;
-  return sweeps<T>(v, H->post, false, nullptr, st);
+  return level_sweeps<T>(H, l, v, H->post, false, st);
 }
 
 // p += e (FP64) and Neumann ghosts of p, after the inner V-cycles
@@ -869,8 +1009,10 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
     }
     if (H->mode == 1) {
       if (!cuda_ok(cudaMalloc(&H->x32[l], n * sizeof(float)), "cudaMalloc(mg x32)")) return false;
+      if (!cuda_ok(cudaMalloc(&H->x32b[l], n * sizeof(float)), "cudaMalloc(mg x32b)")) return false;
       if (!cuda_ok(cudaMalloc(&H->b32[l], n * sizeof(float)), "cudaMalloc(mg b32)")) return false;
       cudaMemset(H->x32[l], 0, n * sizeof(float));
+      cudaMemset(H->x32b[l], 0, n * sizeof(float));
     }
   }
   // coarsest level: exact solve when mg_coarse is 0 and the level is small
@@ -968,8 +1110,9 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
 }
 
 // Average duration of `reps` launches of one fine-level kernel, between CUDA
-// events on the library stream: which = 0 the fine smoother pass (FP32 for
-// mg-mixed, FP64 for mg), 1 the FP64 residual of mg-mixed. It works on
+// events on the library stream: which = 0 the fine smoother (mg-mixed: one
+// whole FP32 sweep, one kernel; mg: one colour pass of the FP64 smoother),
+// 1 the FP64 residual of mg-mixed. It works on
 // scratch copies or on the solver's own FP32 arrays, never on p; a private
 // state that never stops keeps the kernels active.
 bool mg_time_kernel(SolverState *ss, const double *p, const double *rhs, int which, int reps,
@@ -1006,8 +1149,7 @@ bool mg_time_kernel(SolverState *ss, const double *p, const double *rhs, int whi
             H->red.ticket, 0);
         ok = launched("k_mx_residual");
       } else if (H->mode == 1) {
-        View<float> v = compact_view<float>(H->lv[0], H->x32[0], H->b32[0]);
-        ok = smooth_pass<float, false>(v, q & 1, nullptr, tst);
+        ok = fused_sweeps(H, 0, 1, false, tst);  // one whole sweep
       } else {
         ok = smooth_pass<double, false>(v0, q & 1, nullptr, tst);
       }
@@ -1036,6 +1178,7 @@ void mg_free(Solver *s, SolverState *ss)
     if (H->x64[l]) cudaFree(H->x64[l]);
     if (H->b64[l]) cudaFree(H->b64[l]);
     if (H->x32[l]) cudaFree(H->x32[l]);
+    if (H->x32b[l]) cudaFree(H->x32b[l]);
     if (H->b32[l]) cudaFree(H->b32[l]);
   }
   if (H->minv64) cudaFree(H->minv64);

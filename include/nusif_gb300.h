@@ -193,7 +193,9 @@ NUSIF_API int nusifWriteVTK(const Discretization *d, const char *path, int binar
 NUSIF_API unsigned long long nusifLaunchCount(void);
 /* Measurement hook (mg and mg-mixed solvers): average duration in ms of `reps`
  * launches of one fine-level kernel, timed with CUDA events on the library
- * stream; which = 0 the fine smoother pass, 1 the FP64 residual of mg-mixed.
+ * stream; which = 0 the fine smoother (mg-mixed: one whole FP32 red-black
+ * sweep; mg: one colour pass of the FP64 smoother), 1 the FP64 residual of
+ * mg-mixed.
  * Works on scratch copies: p and rhs are only read. */
 NUSIF_API int nusifTimeKernel(Solver *s, const double *p, const double *rhs, int which, int reps,
     double *ms_out);
