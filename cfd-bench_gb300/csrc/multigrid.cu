@@ -350,57 +350,103 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong(View<T> f, const T *xc, int 
 // One whole red-black Gauss-Seidel sweep in one kernel, exact: reads x_old,
 // writes x_new (ping-pong), so no block ever reads a value another block
 // writes. A block owns a TX x TY tile of (i, j) columns and a chunk of planes;
-// per plane it stages x_old with a two-cell ring in shared memory, relaxes the
-// odd ("red") cells on the tile plus a one-cell ring (from old even values,
-// exactly what the first pass of a two-pass sweep computes there), then the
-// even cells of the previous plane on the tile (from the new odd values and
-// their own old value), and writes both colours of that plane. Planes walk
-// with a one-plane lag (odd at k, even at k-1); the odd planes just outside
-// the chunk are recomputed, so chunks are independent. One sweep reads x and
-// b once and writes x once. ZERO: x_old is zero (not read).
+// per plane it relaxes the odd ("red") cells on the tile plus a one-cell ring
+// (from old even values: exactly what the first pass of a two-pass sweep
+// computes there), then the even cells of the previous plane on the tile
+// (from the new odd values and their own old value), and writes both colours
+// of that plane. Planes walk with a one-plane lag (odd at k, even at k-1); the
+// odd planes just outside the chunk are recomputed, so chunks are
+// independent. x_old (tile + two-cell ring) and b (tile + one-cell ring) are
+// staged in shared memory by asynchronous copies issued one plane ahead
+// (cp.async, completed by cp.async.wait_group), so global latency overlaps
+// the arithmetic of the plane before. One sweep reads x and b once and
+// writes x once. ZERO: x_old is zero (not read).
 constexpr int kSX = 64, kSY = 8;              // tile (cells)
 constexpr int kRX = kSX + 4, kRY = kSY + 4;   // staged x_old: tile + 2-cell ring
-constexpr int kQX = kSX + 2, kQY = kSY + 2;   // odd values: tile + 1-cell ring
+constexpr int kQX = kSX + 2, kQY = kSY + 2;   // odd values and b: tile + 1-cell ring
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T *smem, const T *gmem)
+{
+  if constexpr (sizeof(T) == 4)
+    cp_async4(smem, gmem);
+  else
+    cp_async8(smem, gmem);
+}
 
 template <typename T, bool ZERO>
 __global__ void __launch_bounds__(256) k_rbgs_sweep(View<T> v, T *__restrict__ xnew, int kc,
     const MgState *st)
 {
   if (mg_done(st)) return;
-  __shared__ T xo[3][kRY][kRX];  // x_old planes (slot = plane mod 3), tile + 2-cell ring
-  __shared__ T xr[3][kQY][kQX];  // new odd values (slot = plane mod 3), tile + 1-cell ring
+  __shared__ T xo[4][kRY][kRX];  // x_old planes, slot = plane & 3
+  __shared__ T bs[3][kQY][kQX];  // b planes, slot = plane % 3
+  __shared__ T xr[3][kQY][kQX];  // new odd values, slot = plane % 3
   const T *__restrict__ xold = v.x;
   const T *__restrict__ b = v.b;
   const int nx = v.nx, ny = v.ny, nz = v.nz;
   const int i0 = blockIdx.x * kSX, j0 = blockIdx.y * kSY;
   const int k0 = blockIdx.z * kc, k1 = min(k0 + kc, nz);
   const int tid = threadIdx.x;
-  // x_old of plane k into its slot; positions outside the domain are filled
-  // from the nearest cell but never used (the boundary tests below)
-  auto stage = [&](int k) {
-    if (k < 0 || k >= nz) return;
-    T(*dst)[kRX] = xo[k % 3];
+  // asynchronous copies of plane k: x_old (tile + 2 ring) and b (tile + 1
+  // ring); positions outside the domain copy the nearest cell and are never
+  // used (the boundary tests below); planes outside the domain are skipped
+  auto stage_x = [&](int k) {
+    if (ZERO || k < 0 || k >= nz) return;
+    T(*dst)[kRX] = xo[k & 3];
     for (int q = tid; q < kRX * kRY; q += 256) {
       const int li = q % kRX, lj = q / kRX;
       const int gi = min(max(i0 - 2 + li, 0), nx - 1), gj = min(max(j0 - 2 + lj, 0), ny - 1);
-      dst[lj][li] = ZERO ? (T)0 : xold[(int64_t)k * v.sz + (int64_t)gj * v.sy + gi];
+      cp_async_elem(&dst[lj][li], xold + (int64_t)k * v.sz + (int64_t)gj * v.sy + gi);
     }
   };
-  stage(k0 - 2);
-  stage(k0 - 1);
+  auto stage_b = [&](int k) {
+    if (k < 0 || k >= nz) return;
+    T(*dst)[kQX] = bs[k % 3];
+    for (int q = tid; q < kQX * kQY; q += 256) {
+      const int li = q % kQX, lj = q / kQX;
+      const int gi = min(max(i0 - 1 + li, 0), nx - 1), gj = min(max(j0 - 1 + lj, 0), ny - 1);
+      cp_async_elem(&dst[lj][li], b + (int64_t)k * v.sz + (int64_t)gj * v.sy + gi);
+    }
+  };
+  if (ZERO) {
+    for (int q = tid; q < 4 * kRX * kRY; q += 256) (&xo[0][0][0])[q] = (T)0;
+  }
+  stage_x(k0 - 2);
+  stage_x(k0 - 1);
+  stage_x(k0);
+  stage_b(k0 - 1);
+  cp_async_commit();
   for (int k = k0 - 1; k <= k1; k++) {
-    stage(k + 1);
+    stage_x(k + 2);  // prefetch: completes during this plane's arithmetic
+    stage_b(k + 1);
+    cp_async_commit();
+    cp_async_wait<1>();  // everything but the prefetch: x_old(k+1), b(k) are in
     __syncthreads();
     // odd cells ((i+j+k) odd, 1-based) of plane k on the tile + 1-cell ring
     if (k >= 0 && k < nz) {
       T(*rq)[kQX] = xr[k % 3];
-      const T(*xk)[kRX] = xo[k % 3];
-      const T(*xkm)[kRX] = xo[(k + 2) % 3];
-      const T(*xkp)[kRX] = xo[(k + 1) % 3];
+      const T(*xk)[kRX] = xo[k & 3];
+      const T(*xkm)[kRX] = xo[(k + 3) & 3];
+      const T(*xkp)[kRX] = xo[(k + 1) & 3];
+      const T(*bk)[kQX] = bs[k % 3];
       for (int q = tid; q < (kQX / 2) * kQY; q += 256) {
         const int lj = q / (kQX / 2), pi = q % (kQX / 2);
         const int gj = j0 - 1 + lj;
-        // first region column that holds an odd cell in this row
         const int li = 2 * pi + (((i0 - 1 + gj + k + 3) & 1) ? 0 : 1);
         const int gi = i0 - 1 + li;
         if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
@@ -410,7 +456,7 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<T> v, T *__restrict__ x
         const T sy = (gj > 0 ? xk[sj - 1][si] : xc) + (gj < ny - 1 ? xk[sj + 1][si] : xc);
         const T sz = (k > 0 ? xkm[sj][si] : xc) + (k < nz - 1 ? xkp[sj][si] : xc);
         const T lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
-        const T r = b[(int64_t)k * v.sz + (int64_t)gj * v.sy + gi] - lap;
+        const T r = bk[lj][li] - lap;
         rq[lj][li] = xc - r * v.inv_diag;
       }
     }
@@ -422,7 +468,8 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<T> v, T *__restrict__ x
       const T(*rm)[kQX] = xr[(ke + 2) % 3];  // plane ke-1
       const T(*r0)[kQX] = xr[ke % 3];        // plane ke
       const T(*rp)[kQX] = xr[(ke + 1) % 3];  // plane ke+1
-      const T(*xe)[kRX] = xo[ke % 3];
+      const T(*xe)[kRX] = xo[ke & 3];
+      const T(*be)[kQX] = bs[ke % 3];
       const int tj = tid / (kSX / 2), pi = tid % (kSX / 2);
       const int gj = j0 + tj;
       const int te = 2 * pi + ((i0 + gj + ke + 3) & 1);  // even cell of the pair
@@ -437,8 +484,7 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<T> v, T *__restrict__ x
           const T sy = (gj > 0 ? r0[lj - 1][li] : xc) + (gj < ny - 1 ? r0[lj + 1][li] : xc);
           const T sz = (ke > 0 ? rm[lj][li] : xc) + (ke < nz - 1 ? rp[lj][li] : xc);
           const T lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
-          const int64_t c = (int64_t)ke * v.sz + (int64_t)gj * v.sy + gi;
-          xnew[c] = xc - (b[c] - lap) * v.inv_diag;
+          xnew[(int64_t)ke * v.sz + (int64_t)gj * v.sy + gi] = xc - (be[lj][li] - lap) * v.inv_diag;
         }
         const int go = i0 + to;
         if (go < nx) xnew[(int64_t)ke * v.sz + (int64_t)gj * v.sy + go] = r0[lj][to + 1];
@@ -446,6 +492,7 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<T> v, T *__restrict__ x
     }
     __syncthreads();
   }
+  cp_async_wait<0>();
 }
 
 // x_f += trilinear interpolation of x_c when x was coarsened (rx == 2): one
