@@ -154,85 +154,7 @@ __global__ void k_inflow(Dims g, double inflow, double *__restrict__ u)
   u[(int64_t)k * g.sk + (int64_t)j * g.sj] = inflow;
 }
 
-// ---- F, G, H (discretization.c:455-652) ----
-struct FghArgs {
-  Dims g;
-  double c1x, c1y, c1z;  // 0.25 / h
-  double c2x, c2y, c2z;  // gamma * 0.25 / h
-  double ex, ey, ez;     // 1 / h^2
-  double iRe, dt, gx, gy, gz;
-};
-
-// donor-cell convective difference d(c q)/ds: cp, cm are the doubled
-// transport velocities on the + and - side, q/qp/qm the transported quantity
-__device__ __forceinline__ double donor(
-    double c1, double c2, double cp, double cm, double q, double qp, double qm)
-{
-  return c1 * (cp * (q + qp) - cm * (q + qm)) + c2 * (fabs(cp) * (q - qp) + fabs(cm) * (q - qm));
-}
-
-__device__ __forceinline__ double second(double e, double qp, double q, double qm)
-{
-  return e * (qp - 2.0 * q + qm);
-}
-
-__global__ void __launch_bounds__(kBlock) k_fgh(FghArgs A, const double *__restrict__ u,
-    const double *__restrict__ v, const double *__restrict__ w, double *__restrict__ f,
-    double *__restrict__ gg, double *__restrict__ h)
-{
-  const Dims &g = A.g;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
-  if (i > g.imax || j > g.jmax || k > g.kmax) return;
-  const int sj = g.sj, sk = g.sk;
-  const int64_t c = (int64_t)k * sk + (int64_t)j * sj + i;
-
-  // F on the +x face; the wall face F(imax) carries U itself
-  if (i == g.imax) {
-    f[c] = u[c];
-  } else {
-    const double uc = u[c], ue = u[c + 1], uw = u[c - 1];
-    const double un = u[c + sj], us = u[c - sj], ut = u[c + sk], ub = u[c - sk];
-    const double cx = donor(A.c1x, A.c2x, uc + ue, uc + uw, uc, ue, uw);
-    const double cy = donor(A.c1y, A.c2y, v[c] + v[c + 1], v[c - sj] + v[c + 1 - sj], uc, un, us);
-    const double cz = donor(A.c1z, A.c2z, w[c] + w[c + 1], w[c - sk] + w[c + 1 - sk], uc, ut, ub);
-    const double lap = second(A.ex, ue, uc, uw) + second(A.ey, un, uc, us) + second(A.ez, ut, uc, ub);
-    f[c] = uc + A.dt * (A.iRe * lap - cx - cy - cz + A.gx);
-  }
-  // G on the +y face
-  if (j == g.jmax) {
-    gg[c] = v[c];
-  } else {
-    const double vc = v[c], ve = v[c + 1], vw = v[c - 1];
-    const double vn = v[c + sj], vs = v[c - sj], vt = v[c + sk], vb = v[c - sk];
-    const double cx = donor(A.c1x, A.c2x, u[c] + u[c + sj], u[c - 1] + u[c - 1 + sj], vc, ve, vw);
-    const double cy = donor(A.c1y, A.c2y, vc + vn, vc + vs, vc, vn, vs);
-    // reference quirk kept for parity (discretization.c:543-550): the "minus"
-    // half uses V(i,j,k+1) where the textbook stencil has V(i,j,k-1)
-    const double cz = donor(A.c1z, A.c2z, w[c] + w[c + sj], w[c - sk] + w[c + sj - sk], vc, vt, vt);
-    const double lap = second(A.ex, ve, vc, vw) + second(A.ey, vn, vc, vs) + second(A.ez, vt, vc, vb);
-    gg[c] = vc + A.dt * (A.iRe * lap - cx - cy - cz + A.gy);
-  }
-  // H on the +z face
-  if (k == g.kmax) {
-    h[c] = w[c];
-  } else {
-    const double wc = w[c], we = w[c + 1], ww = w[c - 1];
-    const double wn = w[c + sj], ws = w[c - sj], wt = w[c + sk], wb = w[c - sk];
-    const double cx = donor(A.c1x, A.c2x, u[c] + u[c + sk], u[c - 1] + u[c - 1 + sk], wc, we, ww);
-    const double cy = donor(A.c1y, A.c2y, v[c] + v[c + sk], v[c - sj + sk] + v[c - sj], wc, wn, ws);
-    const double cz = donor(A.c1z, A.c2z, wc + wt, wc + wb, wc, wt, wb);
-    const double lap = second(A.ex, we, wc, ww) + second(A.ey, wn, wc, ws) + second(A.ez, wt, wc, wb);
-    h[c] = wc + A.dt * (A.iRe * lap - cx - cy - cz + A.gz);
-  }
-  // low wall faces F(0), G(0), H(0) carry the velocity (discretization.c:601-643)
-  if (i == 1) f[c - 1] = u[c - 1];
-  if (j == 1) gg[c - sj] = v[c - sj];
-  if (k == 1) h[c - sk] = w[c - sk];
-}
-
-// ---- F, G, H in flux form ----
+// ---- F, G, H (discretization.c:455-652) in flux form ----
 // The donor-cell scheme is conservative: the reference's convective
 // difference du2dx (discretization.c:491-497) is Tx(i) - Tx(i-1) with
 // Tx(i) = c1*cp*(u_i + u_i+1) + c2*|cp|*(u_i - u_i+1), cp the doubled transport
@@ -253,7 +175,8 @@ struct FluxArgs {
   Dims g;
   FaceCoef ax, ay, az;
   double dt, gx, gy, gz;
-  int kb;  // k planes per block
+  const StepScalars *sp;  // when set, dt comes from device memory (captured steps)
+  int kb;                 // k planes per block
 };
 
 // total (convective + viscous) flux of q across the face between q_a (minus
@@ -318,6 +241,7 @@ __global__ void __launch_bounds__(kFX *kFY) k_fgh_flux(FluxArgs A, const double 
   const int k1 = min(k0 + A.kb - 1, g.kmax);
   const int sj = g.sj, sk = g.sk;
   const int64_t col = (int64_t)j * sj + i;
+  const double dt = A.sp ? A.sp->dt : A.dt;
   ZFace zm = z_face(u, v, w, (int64_t)(k0 - 1) * sk + col, sj, sk, A.az);
   int buf = 0;
   for (int k = k0; k <= k1; k++, buf ^= 1) {
@@ -337,15 +261,15 @@ __global__ void __launch_bounds__(kFX *kFY) k_fgh_flux(FluxArgs A, const double 
       const double uc = __ldg(u + c), vc = __ldg(v + c), wc = __ldg(w + c);
       // F(imax), G(jmax), H(kmax) are wall faces carrying the velocity (discretization.c:609-651)
       const double sf = (xp.f - xm.f) + (yp.f - ym.f) + (zp.f - zm.f);
-      f[c] = (i == g.imax) ? uc : fma(A.dt, A.gx - sf, uc);
+      f[c] = (i == g.imax) ? uc : fma(dt, A.gx - sf, uc);
       const double vt = __ldg(v + c + sk);
       const double s = vc + vt, d = vc - vt;
       const double zconv =
           fma(A.az.c2 * d, fabs(zp.gc) + fabs(zm.gc), A.az.c1 * s * (zp.gc - zm.gc));
       const double sg = (xp.g - xm.g) + (yp.g - ym.g) + (zp.gv - zm.gv) + zconv;
-      gg[c] = (j == g.jmax) ? vc : fma(A.dt, A.gy - sg, vc);
+      gg[c] = (j == g.jmax) ? vc : fma(dt, A.gy - sg, vc);
       const double sh = (xp.h - xm.h) + (yp.h - ym.h) + (zp.h - zm.h);
-      h[c] = (k == g.kmax) ? wc : fma(A.dt, A.gz - sh, wc);
+      h[c] = (k == g.kmax) ? wc : fma(dt, A.gz - sh, wc);
       // low wall faces F(0), G(0), H(0) carry the velocity (discretization.c:601-643)
       if (i == 1) f[c - 1] = __ldg(u + c - 1);
       if (j == 1) gg[c - sj] = __ldg(v + c - sj);
@@ -357,27 +281,29 @@ __global__ void __launch_bounds__(kFX *kFY) k_fgh_flux(FluxArgs A, const double 
 
 // ---- RHS (discretization.c:334-362) ----
 __global__ void __launch_bounds__(kBlock) k_rhs(Dims g, double ix, double iy, double iz,
-    double idt, const double *__restrict__ f, const double *__restrict__ gg,
-    const double *__restrict__ h, double *__restrict__ rhs)
+    double idt_arg, const StepScalars *sp, const double *__restrict__ f,
+    const double *__restrict__ gg, const double *__restrict__ h, double *__restrict__ rhs)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
   if (i > g.imax || j > g.jmax || k > g.kmax) return;
+  const double idt = sp ? sp->idt : idt_arg;
   const int64_t c = (int64_t)k * g.sk + (int64_t)j * g.sj + i;
   rhs[c] = ((f[c] - f[c - 1]) * ix + (gg[c] - gg[c - g.sj]) * iy + (h[c] - h[c - g.sk]) * iz) * idt;
 }
 
 // ---- adaptUV (discretization.c:654-681) ----
-__global__ void __launch_bounds__(kBlock) k_adapt(Dims g, double fx, double fy, double fz,
-    const double *__restrict__ f, const double *__restrict__ gg, const double *__restrict__ h,
-    const double *__restrict__ p, double *__restrict__ u, double *__restrict__ v,
-    double *__restrict__ w)
+__global__ void __launch_bounds__(kBlock) k_adapt(Dims g, double fx_arg, double fy_arg,
+    double fz_arg, const StepScalars *sp, const double *__restrict__ f,
+    const double *__restrict__ gg, const double *__restrict__ h, const double *__restrict__ p,
+    double *__restrict__ u, double *__restrict__ v, double *__restrict__ w)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
   if (i > g.imax || j > g.jmax || k > g.kmax) return;
+  const double fx = sp ? sp->fx : fx_arg, fy = sp ? sp->fy : fy_arg, fz = sp ? sp->fz : fz_arg;
   const int64_t c = (int64_t)k * g.sk + (int64_t)j * g.sj + i;
   const double pc = p[c];
   u[c] = f[c] - (p[c + 1] - pc) * fx;
@@ -493,7 +419,7 @@ bool launch_special(const Dims &g, int problem, double lid, double inflow, doubl
 
 bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, double gz,
     double dt, double dx, double dy, double dz, const double *u, const double *v,
-    const double *w, double *f, double *gg, double *h)
+    const double *w, double *f, double *gg, double *h, const StepScalars *sp, int kb_fixed)
 {
   FluxArgs A;
   A.g = g;
@@ -509,10 +435,12 @@ bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, do
   A.gx = gx;
   A.gy = gy;
   A.gz = gz;
+  A.sp = sp;
   const int gx_blocks = (g.imax + kFX - 1) / kFX, gy_blocks = (g.jmax + kFY - 1) / kFY;
   int kb = 32;
   while (kb > 1 && (int64_t)gx_blocks * gy_blocks * ((g.kmax + kb - 1) / kb) < 8 * sm_count())
     kb >>= 1;
+  if (kb_fixed > 0) kb = kb_fixed;
   A.kb = kb;
   dim3 grid(gx_blocks, gy_blocks, (g.kmax + kb - 1) / kb);
   k_fgh_flux<<<grid, dim3(kFX, kFY), 0, stream()>>>(A, u, v, w, f, gg, h);
@@ -520,10 +448,10 @@ bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, do
 }
 
 bool launch_rhs(const Dims &g, double dt, double dx, double dy, double dz, const double *f,
-    const double *gg, const double *h, double *rhs)
+    const double *gg, const double *h, double *rhs, const StepScalars *sp)
 {
   k_rhs<<<cell_grid(g, kCellBlock), kCellBlock, 0, stream()>>>(
-      g, 1.0 / dx, 1.0 / dy, 1.0 / dz, 1.0 / dt, f, gg, h, rhs);
+      g, 1.0 / dx, 1.0 / dy, 1.0 / dz, sp ? 0.0 : 1.0 / dt, sp, f, gg, h, rhs);
   return launched("k_rhs");
 }
 
@@ -543,10 +471,10 @@ bool launch_subtract_mean(const Dims &g, double *p, const double *d_mean)
 
 bool launch_adapt_uv(const Dims &g, double dt, double dx, double dy, double dz,
     const double *f, const double *gg, const double *h, const double *p, double *u, double *v,
-    double *w)
+    double *w, const StepScalars *sp)
 {
   k_adapt<<<cell_grid(g, kCellBlock), kCellBlock, 0, stream()>>>(
-      g, dt / dx, dt / dy, dt / dz, f, gg, h, p, u, v, w);
+      g, dt / dx, dt / dy, dt / dz, sp, f, gg, h, p, u, v, w);
   return launched("k_adapt");
 }
 

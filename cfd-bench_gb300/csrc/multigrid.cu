@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong(View<T> f, const T *xc, int 
 
 // One whole red-black Gauss-Seidel sweep in one kernel, exact: reads x_old,
 // writes x_new (ping-pong), so no block ever reads a value another block
-// writes. A block owns a TX x TY tile of (i, j) columns and a chunk of planes;
+// writes. A block owns a 64 x 8 tile of (i, j) columns and a chunk of planes;
 // per plane it relaxes the odd ("red") cells on the tile plus a one-cell ring
 // (from old even values: exactly what the first pass of a two-pass sweep
 // computes there), then the even cells of the previous plane on the tile
@@ -361,133 +361,113 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong(View<T> f, const T *xc, int 
 // (cp.async, completed by cp.async.wait_group), so global latency overlaps
 // the arithmetic of the plane before. One sweep reads x and b once and
 // writes x once. ZERO: x_old is zero (not read).
-constexpr int kSX = 64, kSY = 8;              // tile (cells)
-constexpr int kRX = kSX + 4, kRY = kSY + 4;   // staged x_old: tile + 2-cell ring
-constexpr int kQX = kSX + 2, kQY = kSY + 2;   // odd values and b: tile + 1-cell ring
+constexpr int kSX = 64, kSY = 8;  // tile (cells)
+constexpr int kWX = kSX + 8;      // staged row: tile + 4 cells each side (16-byte chunks)
+constexpr int kRY = kSY + 4;      // staged x_old rows: tile + 2-row ring
+constexpr int kBYr = kSY + 2;     // staged b rows and odd values: tile + 1-row ring
+constexpr int kQX = kSX + 2;      // odd values: tile + 1-cell ring
 
-__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
-{
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-template <typename T>
-__device__ __forceinline__ void cp_async_elem(T *smem, const T *gmem)
-{
-  if constexpr (sizeof(T) == 4)
-    cp_async4(smem, gmem);
-  else
-    cp_async8(smem, gmem);
-}
-
-template <typename T, bool ZERO>
-__global__ void __launch_bounds__(256) k_rbgs_sweep(View<T> v, T *__restrict__ xnew, int kc,
-    const MgState *st)
+// FP32 levels with nx % 4 == 0 (rows start on 16-byte boundaries): every
+// staged row is 18 chunks of four cells starting 4 cells left of the tile,
+// one chunk per thread per array per plane. Chunks outside the domain copy
+// the nearest in-domain chunk and are never read (boundary tests below).
+template <bool ZERO>
+__global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__restrict__ xnew,
+    int kc, const MgState *st)
 {
   if (mg_done(st)) return;
-  __shared__ T xo[4][kRY][kRX];  // x_old planes, slot = plane & 3
-  __shared__ T bs[3][kQY][kQX];  // b planes, slot = plane % 3
-  __shared__ T xr[3][kQY][kQX];  // new odd values, slot = plane % 3
-  const T *__restrict__ xold = v.x;
-  const T *__restrict__ b = v.b;
+  __shared__ __align__(16) float xo[4][kRY][kWX];   // x_old planes, slot = plane & 3
+  __shared__ __align__(16) float bs[3][kBYr][kWX];  // b planes, slot = plane % 3
+  __shared__ float xr[3][kBYr][kQX];                // new odd values, slot = plane % 3
+  const float *__restrict__ xold = v.x;
+  const float *__restrict__ b = v.b;
   const int nx = v.nx, ny = v.ny, nz = v.nz;
   const int i0 = blockIdx.x * kSX, j0 = blockIdx.y * kSY;
   const int k0 = blockIdx.z * kc, k1 = min(k0 + kc, nz);
   const int tid = threadIdx.x;
-  // asynchronous copies of plane k: x_old (tile + 2 ring) and b (tile + 1
-  // ring); positions outside the domain copy the nearest cell and are never
-  // used (the boundary tests below); planes outside the domain are skipped
-  auto stage_x = [&](int k) {
-    if (ZERO || k < 0 || k >= nz) return;
-    T(*dst)[kRX] = xo[k & 3];
-    for (int q = tid; q < kRX * kRY; q += 256) {
-      const int li = q % kRX, lj = q / kRX;
-      const int gi = min(max(i0 - 2 + li, 0), nx - 1), gj = min(max(j0 - 2 + lj, 0), ny - 1);
-      cp_async_elem(&dst[lj][li], xold + (int64_t)k * v.sz + (int64_t)gj * v.sy + gi);
-    }
-  };
-  auto stage_b = [&](int k) {
-    if (k < 0 || k >= nz) return;
-    T(*dst)[kQX] = bs[k % 3];
-    for (int q = tid; q < kQX * kQY; q += 256) {
-      const int li = q % kQX, lj = q / kQX;
-      const int gi = min(max(i0 - 1 + li, 0), nx - 1), gj = min(max(j0 - 1 + lj, 0), ny - 1);
-      cp_async_elem(&dst[lj][li], b + (int64_t)k * v.sz + (int64_t)gj * v.sy + gi);
-    }
+  constexpr int kChunks = kWX / 4;  // 18 per row
+  // this thread's chunk: row cr, chunk cc, and its offset inside a plane
+  const int cr = tid / kChunks, cc = tid - cr * kChunks;
+  const int gic = min(max(i0 - 4 + 4 * cc, 0), nx - 4);
+  const bool x_lane = cr < kRY, b_lane = cr < kBYr;
+  const int gjx = min(max(j0 - 2 + cr, 0), ny - 1), gjb = min(max(j0 - 1 + cr, 0), ny - 1);
+  const int64_t xoff = (int64_t)gjx * v.sy + gic, boff = (int64_t)gjb * v.sy + gic;
+  auto stage = [&](int kx, int kb) {
+    if (!ZERO && x_lane && kx >= 0 && kx < nz)
+      cp_async16(&xo[kx & 3][cr][4 * cc], xold + (int64_t)kx * v.sz + xoff);
+    if (b_lane && kb >= 0 && kb < nz)
+      cp_async16(&bs[kb % 3][cr][4 * cc], b + (int64_t)kb * v.sz + boff);
   };
   if (ZERO) {
-    for (int q = tid; q < 4 * kRX * kRY; q += 256) (&xo[0][0][0])[q] = (T)0;
+    for (int q = tid; q < 4 * kRY * kWX; q += 256) (&xo[0][0][0])[q] = 0.0f;
   }
-  stage_x(k0 - 2);
-  stage_x(k0 - 1);
-  stage_x(k0);
-  stage_b(k0 - 1);
+  stage(k0 - 2, -1);
+  stage(k0 - 1, k0 - 1);
+  stage(k0, -1);
   cp_async_commit();
+  constexpr int kOdd = (kQX / 2) * kBYr;  // odd cells per plane on tile + ring (330)
   for (int k = k0 - 1; k <= k1; k++) {
-    stage_x(k + 2);  // prefetch: completes during this plane's arithmetic
-    stage_b(k + 1);
+    stage(k + 2, k + 1);  // prefetch: completes during this plane's arithmetic
     cp_async_commit();
-    cp_async_wait<1>();  // everything but the prefetch: x_old(k+1), b(k) are in
+    cp_async_wait<1>();   // all but the prefetch: x_old(k+1), b(k) are in
     __syncthreads();
-    // odd cells ((i+j+k) odd, 1-based) of plane k on the tile + 1-cell ring
     if (k >= 0 && k < nz) {
-      T(*rq)[kQX] = xr[k % 3];
-      const T(*xk)[kRX] = xo[k & 3];
-      const T(*xkm)[kRX] = xo[(k + 3) & 3];
-      const T(*xkp)[kRX] = xo[(k + 1) & 3];
-      const T(*bk)[kQX] = bs[k % 3];
-      for (int q = tid; q < (kQX / 2) * kQY; q += 256) {
-        const int lj = q / (kQX / 2), pi = q % (kQX / 2);
+      float(*rq)[kQX] = xr[k % 3];
+      const float(*xk)[kWX] = xo[k & 3];
+      const float(*xkm)[kWX] = xo[(k + 3) & 3];
+      const float(*xkp)[kWX] = xo[(k + 1) & 3];
+      const float(*bk)[kWX] = bs[k % 3];
+      for (int q = tid; q < kOdd; q += 256) {
+        const int lj = q / (kQX / 2), pi = q - lj * (kQX / 2);
         const int gj = j0 - 1 + lj;
-        const int li = 2 * pi + (((i0 - 1 + gj + k + 3) & 1) ? 0 : 1);
+        const int li = 2 * pi + ((i0 + gj + k) & 1 ? 0 : 1);  // odd cell column
         const int gi = i0 - 1 + li;
         if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
-        const int si = li + 1, sj = lj + 1;
-        const T xc = xk[sj][si];
-        const T sx = (gi > 0 ? xk[sj][si - 1] : xc) + (gi < nx - 1 ? xk[sj][si + 1] : xc);
-        const T sy = (gj > 0 ? xk[sj - 1][si] : xc) + (gj < ny - 1 ? xk[sj + 1][si] : xc);
-        const T sz = (k > 0 ? xkm[sj][si] : xc) + (k < nz - 1 ? xkp[sj][si] : xc);
-        const T lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
-        const T r = bk[lj][li] - lap;
-        rq[lj][li] = xc - r * v.inv_diag;
+        const int si = li + 3, sj = lj + 1;  // staged x_old column / row
+        const float xc = xk[sj][si];
+        const float sx = (gi > 0 ? xk[sj][si - 1] : xc) + (gi < nx - 1 ? xk[sj][si + 1] : xc);
+        const float sy = (gj > 0 ? xk[sj - 1][si] : xc) + (gj < ny - 1 ? xk[sj + 1][si] : xc);
+        const float sz = (k > 0 ? xkm[sj][si] : xc) + (k < nz - 1 ? xkp[sj][si] : xc);
+        const float lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
+        rq[lj][li] = xc - (bk[lj][li + 3] - lap) * v.inv_diag;
       }
     }
     __syncthreads();
-    // even cells of plane k-1 on the tile, one cell pair per thread; both
-    // cells of the pair are written to x_new
+    // even cells of plane k-1 on the tile: one cell pair per thread, both
+    // cells stored as one 8-byte vector
     const int ke = k - 1;
     if (ke >= k0 && ke < k1) {
-      const T(*rm)[kQX] = xr[(ke + 2) % 3];  // plane ke-1
-      const T(*r0)[kQX] = xr[ke % 3];        // plane ke
-      const T(*rp)[kQX] = xr[(ke + 1) % 3];  // plane ke+1
-      const T(*xe)[kRX] = xo[ke & 3];
-      const T(*be)[kQX] = bs[ke % 3];
-      const int tj = tid / (kSX / 2), pi = tid % (kSX / 2);
+      const float(*rm)[kQX] = xr[(ke + 2) % 3];
+      const float(*r0)[kQX] = xr[ke % 3];
+      const float(*rp)[kQX] = xr[(ke + 1) % 3];
+      const float(*xe)[kWX] = xo[ke & 3];
+      const float(*be)[kWX] = bs[ke % 3];
+      const int tj = tid >> 5, pi = tid & 31;
       const int gj = j0 + tj;
-      const int te = 2 * pi + ((i0 + gj + ke + 3) & 1);  // even cell of the pair
-      const int to = te ^ 1;                             // odd cell of the pair
-      const int lj = tj + 1;
-      if (gj < ny) {
-        const int gi = i0 + te;
-        if (gi < nx) {
-          const int li = te + 1;
-          const T xc = xe[lj + 1][li + 1];
-          const T sx = (gi > 0 ? r0[lj][li - 1] : xc) + (gi < nx - 1 ? r0[lj][li + 1] : xc);
-          const T sy = (gj > 0 ? r0[lj - 1][li] : xc) + (gj < ny - 1 ? r0[lj + 1][li] : xc);
-          const T sz = (ke > 0 ? rm[lj][li] : xc) + (ke < nz - 1 ? rp[lj][li] : xc);
-          const T lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
-          xnew[(int64_t)ke * v.sz + (int64_t)gj * v.sy + gi] = xc - (be[lj][li] - lap) * v.inv_diag;
-        }
-        const int go = i0 + to;
-        if (go < nx) xnew[(int64_t)ke * v.sz + (int64_t)gj * v.sy + go] = r0[lj][to + 1];
+      const int e = (i0 + gj + ke + 1) & 1;  // position of the even cell in the pair
+      const int te = 2 * pi + e;
+      const int gi = i0 + te;
+      if (gj < ny && i0 + 2 * pi < nx) {
+        const int li = te + 1, lj = tj + 1;
+        const float xc = xe[lj + 1][te + 4];
+        const float sx = (gi > 0 ? r0[lj][li - 1] : xc) + (gi < nx - 1 ? r0[lj][li + 1] : xc);
+        const float sy = (gj > 0 ? r0[lj - 1][li] : xc) + (gj < ny - 1 ? r0[lj + 1][li] : xc);
+        const float sz = (ke > 0 ? rm[lj][li] : xc) + (ke < nz - 1 ? rp[lj][li] : xc);
+        const float lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
+        const float even = xc - (be[lj][te + 4] - lap) * v.inv_diag;
+        const float odd = r0[lj][(te ^ 1) + 1];
+        const float2 pair = e ? make_float2(odd, even) : make_float2(even, odd);
+        *reinterpret_cast<float2 *>(xnew + (int64_t)ke * v.sz + (int64_t)gj * v.sy + i0 + 2 * pi) =
+            pair;
       }
     }
     __syncthreads();
@@ -910,6 +890,10 @@ bool coarse_solve(const View<T> &v, int nsweeps, const MgState *st, const T *min
 bool fused_sweeps(MgHierarchy *H, int l, int count, bool zero_first, const MgState *st)
 {
   const MgLevelDesc &L = H->lv[l];
+  if (L.n[0] % 4 != 0) {  // rows not 16-byte aligned: the two-pass in-place sweep
+    const View<float> v = compact_view<float>(L, H->x32[l], H->b32[l]);
+    return sweeps<float>(v, count, zero_first, nullptr, st);
+  }
   const int gx = (L.n[0] + kSX - 1) / kSX, gy = (L.n[1] + kSY - 1) / kSY;
   int kc = 32;
   while (kc > 4 && (int64_t)gx * gy * ((L.n[2] + kc - 1) / kc) < 8 * sm_count_mg()) kc >>= 1;
@@ -917,9 +901,9 @@ bool fused_sweeps(MgHierarchy *H, int l, int count, bool zero_first, const MgSta
   for (int s = 0; s < count; s++) {
     const View<float> v = compact_view<float>(L, H->x32[l], H->b32[l]);
     if (zero_first && s == 0)
-      k_rbgs_sweep<float, true><<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st);
+      k_rbgs_sweep<true><<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st);
     else
-      k_rbgs_sweep<float, false><<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st);
+      k_rbgs_sweep<false><<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st);
     if (!launched("k_rbgs_sweep")) return false;
     float *t = H->x32[l];
     H->x32[l] = H->x32b[l];

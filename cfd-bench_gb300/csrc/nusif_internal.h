@@ -64,6 +64,16 @@ struct ReduceScratch {
 bool reduce_scratch_alloc(ReduceScratch &r, int capacity);
 void reduce_scratch_free(ReduceScratch &r);
 
+// Scalars of one time step kept in device memory, so that a step can run
+// without a host round trip (graph-captured batched steps). Same expressions
+// as the host path: dt (computeTimestep), 1/dt (computeRHS), dt/h (adaptUV).
+struct StepScalars {
+  double dt, idt, fx, fy, fz;
+  double t;  // simulated time after the last completed step
+  int nt;    // completed steps
+  int pad;
+};
+
 // Device state of one Discretization (kept beside the reference struct).
 struct DiscState {
   Dims dims;
@@ -82,13 +92,14 @@ bool launch_bc(const Dims &g, const int bc[6], int problem, double lid, double i
     double *u, double *v, double *w);
 bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, double gz,
     double dt, double dx, double dy, double dz, const double *u, const double *v,
-    const double *w, double *f, double *gg, double *h);
+    const double *w, double *f, double *gg, double *h, const StepScalars *sp = nullptr,
+    int kb_fixed = 0);
 bool launch_rhs(const Dims &g, double dt, double dx, double dy, double dz, const double *f,
-    const double *gg, const double *h, double *rhs);
+    const double *gg, const double *h, double *rhs, const StepScalars *sp = nullptr);
 bool launch_interior_sum(const Dims &g, const double *p, ReduceScratch &red, double *d_out);
 bool launch_subtract_mean(const Dims &g, double *p, const double *d_sum, double ncell);
 bool launch_adapt_uv(const Dims &g, double dt, double dx, double dy, double dz,
     const double *f, const double *gg, const double *h, const double *p, double *u, double *v,
-    double *w);
+    double *w, const StepScalars *sp = nullptr);
 
 }  // namespace nusif
