@@ -1092,6 +1092,64 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
   return cuda_ok(cudaDeviceSynchronize(), "mg setup");
 }
 
+namespace {
+
+__global__ void k_mg_state_init(MgState *st, double rtol2, int maxcycles)
+{
+  MgState s;
+  memset(&s, 0, sizeof(s));
+  s.rtol2 = rtol2;
+  s.maxcycles = maxcycles;
+  *st = s;
+}
+
+// after a captured solve: count a step whose queue ran out before rtol
+__global__ void k_mg_count_unconverged(const MgState *st, int *counter, int *last_cycles)
+{
+  if (!st->done) *counter += 1;
+  *last_cycles = st->cycles;
+}
+
+}  // namespace
+
+// The solve as a fixed sequence of launches with no host synchronisation
+// (graph capture): state initialisation, right-hand-side statistics, `queue`
+// units (FP64 V-cycles for mg, outer refinement iterations for mg-mixed; the
+// device-side flags turn the surplus into empty launches), ghost refresh, and
+// a check that records steps whose queue was too short.
+bool mg_enqueue(SolverState *ss, double *p, const double *rhs, int queue, int *unconverged,
+    int *last_cycles)
+{
+  MgHierarchy *H = ss->mg;
+  if (!H) {
+    fail(NUSIF_ERR_STATE, "mg enqueue without a hierarchy");
+    return false;
+  }
+  k_mg_state_init<<<1, 1, 0, stream()>>>(H->d_state, H->rtol * H->rtol, H->maxcycles);
+  if (!launched("k_mg_state_init")) return false;
+  View<double> v0 = padded_view(H->lv[0], p, rhs);
+  const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
+  const int blocks = flat_blocks(n0);
+  k_mg_rhs_sum<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
+  if (!launched("k_mg_rhs_sum")) return false;
+  k_mg_rhs_norm<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
+  if (!launched("k_mg_rhs_norm")) return false;
+  for (int q = 0; q < queue; q++)
+    if (!(H->mode == 0 ? cycle_fp64(H, p, rhs) : cycle_mixed(H, p, rhs))) return false;
+  if (!launch_pressure_ghosts(make_dims(v0.nx, v0.ny, v0.nz), p)) return false;
+  k_mg_count_unconverged<<<1, 1, 0, stream()>>>(H->d_state, unconverged, last_cycles);
+  return launched("k_mg_count_unconverged");
+}
+
+// FP32 sweeps swap buffers on the host; a captured sequence must end with the
+// same buffer current as it started, so it needs an even number of sweeps per
+// level in every V-cycle (the default V(2,2) has)
+bool mg_capture_ok(const SolverState *ss)
+{
+  const MgHierarchy *H = ss->mg;
+  return H && (H->mode == 0 || (H->pre % 2 == 0 && H->post % 2 == 0));
+}
+
 double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
 {
   MgHierarchy *H = ss->mg;

@@ -97,9 +97,11 @@ bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, do
 bool launch_rhs(const Dims &g, double dt, double dx, double dy, double dz, const double *f,
     const double *gg, const double *h, double *rhs, const StepScalars *sp = nullptr);
 bool launch_interior_sum(const Dims &g, const double *p, ReduceScratch &red, double *d_out);
-bool launch_subtract_mean(const Dims &g, double *p, const double *d_sum, double ncell);
+bool launch_subtract_mean(const Dims &g, double *p, const double *d_mean);
 bool launch_adapt_uv(const Dims &g, double dt, double dx, double dy, double dz,
     const double *f, const double *gg, const double *h, const double *p, double *u, double *v,
     double *w, const StepScalars *sp = nullptr);
+bool launch_special(const Dims &g, int problem, double lid, double inflow, double *u);
+int problem_code(const char *name);
 
 }  // namespace nusif

@@ -52,5 +52,8 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs);
 void mg_free(Solver *s, SolverState *ss);
 bool mg_time_kernel(SolverState *ss, const double *p, const double *rhs, int which, int reps,
     double *ms_out);
+bool mg_enqueue(SolverState *ss, double *p, const double *rhs, int queue, int *unconverged,
+    int *last_cycles);
+bool mg_capture_ok(const SolverState *ss);
 
 }  // namespace nusif

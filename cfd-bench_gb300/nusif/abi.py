@@ -100,6 +100,15 @@ SIGNATURES = [
     ("nusifCollectResult", C.c_int, [C.POINTER(Discretization), c_double_p, c_double_p,
                                      c_double_p, c_double_p]),
     ("nusifWriteVTK", C.c_int, [C.POINTER(Discretization), C.c_char_p, C.c_int]),
+    ("nusifBatchCreate", C.c_void_p, [C.c_int, C.POINTER(C.c_char_p), C.c_int, C.c_int]),
+    ("nusifBatchStep", C.c_int, [C.c_void_p, C.c_int]),
+    ("nusifBatchSize", C.c_int, [C.c_void_p]),
+    ("nusifBatchInstance", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.POINTER(Discretization)),
+                                     C.POINTER(C.POINTER(Solver))]),
+    ("nusifBatchStats", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("nusifBatchFree", None, [C.c_void_p]),
     ("nusifLaunchCount", C.c_ulonglong, []),
     ("nusifTimeKernel", C.c_int, [C.POINTER(Solver), c_double_p, c_double_p, C.c_int, C.c_int,
                                   C.POINTER(C.c_double)]),

@@ -189,6 +189,24 @@ NUSIF_API int nusifCollectResult(const Discretization *d, double *ug, double *vg
  * src/main.c:135-141): STRUCTURED_POINTS with "pressure" and "velocity";
  * binary = 0 writes ASCII "%f" (the reference's default), 1 big-endian doubles. */
 NUSIF_API int nusifWriteVTK(const Discretization *d, const char *path, int binary);
+/* Batched instances (no reference counterpart: the reference runs one case per
+ * process). Each parameter file is one independent case (uneven grids welcome)
+ * with the mg or mg-mixed solver (even mg_pre / mg_post). One time step of
+ * every instance is captured as one CUDA graph (device-side dt, a queue of
+ * `queue` device-gated multigrid units per step); tune != 0 times the F/G/H
+ * tile depth per instance first. Returns NULL on error. */
+typedef struct NusifBatch NusifBatch;
+NUSIF_API NusifBatch *nusifBatchCreate(int n, const char *const *parfiles, int queue, int tune);
+/* advance every instance by `steps` time steps (one graph launch each) */
+NUSIF_API int nusifBatchStep(NusifBatch *b, int steps);
+NUSIF_API int nusifBatchSize(const NusifBatch *b);
+/* the instance's Discretization / Solver, for nusifDownloadField and friends */
+NUSIF_API int nusifBatchInstance(NusifBatch *b, int idx, Discretization **d, Solver **s);
+/* per instance: time, last dt, steps, V-cycles of the last step, steps that
+ * ended above rtol (queue too short), autotuned F/G/H planes per block */
+NUSIF_API int nusifBatchStats(NusifBatch *b, int idx, double *t, double *dt, int *nt, int *cycles,
+    int *unconverged, int *fg_planes);
+NUSIF_API void nusifBatchFree(NusifBatch *b);
 /* kernels this library launched since it was loaded (observability) */
 NUSIF_API unsigned long long nusifLaunchCount(void);
 /* Measurement hook (mg and mg-mixed solvers): average duration in ms of `reps`
