@@ -52,10 +52,14 @@ def parse_args():
     ap.add_argument("--solver", default=os.environ.get("NUSIF_BENCH_SOLVER", "auto"))
     ap.add_argument("--n", type=int, default=256, help="cells per axis of the cavity")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--guess", default="extrapolate", choices=["previous", "extrapolate"],
+                    help="initial pressure of each V-cycle solve: p(n-1), or 2 p(n-1) - p(n-2)")
     ap.add_argument("--batch-n", type=int, default=96, help="instances of the batch workload")
     ap.add_argument("--workload", default="cavity", choices=["cavity", "channel", "batch"],
                     help="cavity: the 256^3 benchmark; channel: mixed vs FP64 error study")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-roofline", action="store_true",
+                    help="skip the per-kernel timing launches (clean launch lists for ncu)")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the FP64 multigrid comparison run")
     ap.add_argument("--itermax", type=int, default=None,
@@ -133,12 +137,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def bench_case(n: int, solver: str, itermax: int | None = None) -> dict:
+def bench_case(n: int, solver: str, itermax: int | None = None,
+               guess: str = "previous") -> dict:
     from nusif.params import config2
     vals = config2(solver=solver)
     vals.update(imax=n, jmax=n, kmax=n)
     if itermax is not None:
         vals["itermax"] = itermax
+    if solver in ("mg", "mg-mixed"):
+        vals["mg_guess"] = guess
     return vals
 
 
@@ -203,7 +210,7 @@ def run_gpu(args, rank, world, local):
     lib.nusifSetStream(C.c_void_p(stream.cuda_stream))
 
     solver = pick_solver(args.solver)
-    vals = bench_case(args.n, solver, args.itermax)
+    vals = bench_case(args.n, solver, args.itermax, args.guess)
     sim = nusif.Simulation(vals)
     i, j, k = sim.dims
     ncell = i * j * k
@@ -211,7 +218,7 @@ def run_gpu(args, rank, world, local):
     head = timed_steps(sim, args, stream, local, world)
 
     # ---- dominant kernels, timed live with CUDA events on the library stream ----
-    roofs = kernel_rooflines(sim, solver, stream, ncell)
+    roofs = [] if args.no_roofline else kernel_rooflines(sim, solver, stream, ncell)
 
     # ---- e2e: same step through the C ABI with host buffers ----
     e2e = None
@@ -220,15 +227,19 @@ def run_gpu(args, rank, world, local):
     sim.close()
 
     # ---- the comparison the metric names: plain FP64 multigrid, same case ----
+    # (previous-p guess: plain FP64 multigrid; and with this run's guess)
     compare = None
     if solver == "mg-mixed" and not args.no_compare:
-        sim64 = nusif.Simulation(bench_case(args.n, "mg", args.itermax))
-        ref64 = timed_steps(sim64, args, stream, local, world)
-        sim64.close()
-        compare = {"solver": "mg (FP64 V-cycles, same rtol 1e-6)",
-                   "ms_per_step": ref64["ms_per_step"],
-                   "v_cycles_per_step": ref64["iters"], "residual_per_step": ref64["res"],
-                   "speedup_of_value": ref64["ms_per_step"] / head["ms_per_step"]}
+        compare = []
+        for g in dict.fromkeys(["previous", args.guess]):
+            sim64 = nusif.Simulation(bench_case(args.n, "mg", args.itermax, g))
+            ref64 = timed_steps(sim64, args, stream, local, world)
+            sim64.close()
+            compare.append({"solver": "mg (FP64 V-cycles, same rtol 1e-6)", "guess": g,
+                            "ms_per_step": ref64["ms_per_step"],
+                            "v_cycles_per_step": ref64["iters"],
+                            "residual_per_step": ref64["res"],
+                            "speedup_of_value": ref64["ms_per_step"] / head["ms_per_step"]})
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -255,6 +266,7 @@ def run_gpu(args, rank, world, local):
                                f"pressure solve {solver}",
                    "cells": ncell, "solver": solver, "tolerance": tol,
                    "learned_warm_start": False,
+                   "initial_guess": (args.guess if solver in ("mg", "mg-mixed") else "previous"),
                    "l2": "no flush: 8 FP64 fields of %.0f MB each, far larger than L2" % (padded * 8 / 1e6),
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "solver_iterations_per_step": head["iters"],
@@ -550,7 +562,7 @@ def run_batch(args, local):
     cases = batch_cases(args.batch_n)
     cells = [c["imax"] * c["jmax"] * c["kmax"] for c in cases]
     t0 = time.perf_counter()
-    batch = nusif.Batch(cases, queue=4, tune=True)
+    batch = nusif.Batch(cases, queue=0, tune=True)
     setup_s = time.perf_counter() - t0
     batch.step(args.warmup)
     launches0 = lib.nusifLaunchCount()
@@ -586,7 +598,7 @@ def run_batch(args, local):
         "config": {"workload": f"{len(cases)} lid-driven cavities, edges from "
                                "{32,48,64,96,128}^3, Re ~ U[100,5000] (seeded), "
                                "one CUDA graph launch per time step", "seed": BATCH_SEED,
-                   "cells_total": sum(cells), "queue": 4},
+                   "cells_total": sum(cells), "mg_loop": "graph while-loop to rtol"},
         "ms_per_step": wall * 1e3 / args.steps,
         "setup_s": setup_s,
         "gpu_launches_outside_graphs": int(lib.nusifLaunchCount() - launches0),

@@ -5,9 +5,11 @@
 //  - a device-resident time step: the CFL maxima feed a one-thread kernel
 //    that computes dt with the host's expressions (computeTimestep,
 //    discretization.c:431-453) into StepScalars, which F/G/H, RHS and adaptUV
-//    read; the multigrid solve is a fixed queue of device-gated units
-//    (mg_enqueue). One time step of one instance is then a launch sequence
-//    with no host synchronisation;
+//    read; the multigrid solve is a CUDA graph while-loop over device-gated
+//    units (mg_enqueue_loop) that runs exactly as many units as the
+//    host-driven solve, or optionally a fixed queue of units (mg_enqueue).
+//    One time step of one instance is then a launch sequence with no host
+//    synchronisation;
 //  - one CUDA graph per step kind (with / without normalizePressure, every
 //    100 steps as main.c:68-70): each instance's sequence is captured on its
 //    own stream as an independent branch, so one graph launch advances every
@@ -16,7 +18,8 @@
 //    kernel are timed on that grid (CUDA events) and the fastest is captured.
 // Results are those of stepping each instance alone with the mg / mg-mixed
 // solvers (same kernels, same arithmetic, dt computed with the same
-// expressions); steps whose queue ran out before rtol are counted.
+// expressions); steps whose solve ended above rtol (a fixed queue that ran
+// out, or the mg_cycles limit) are counted.
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -36,7 +39,7 @@ namespace {
 
 struct BatchDev {
   StepScalars sc;
-  int unconverged;  // steps whose multigrid queue ended above rtol
+  int unconverged;  // steps whose multigrid solve ended above rtol
   int last_cycles;  // V-cycles of the last step
 };
 
@@ -83,9 +86,10 @@ using namespace nusif;
 struct NusifBatch {
   std::vector<BatchInst *> inst;
   cudaStream_t main = nullptr;
+  cudaStream_t body = nullptr;  // captures the multigrid while-loop bodies
   cudaEvent_t fork = nullptr;
   cudaGraphExec_t exec[2] = { nullptr, nullptr };
-  int queue = 4;
+  int queue = 0;  // > 0: fixed number of multigrid units per step, else a while-loop
   int nt = 0;
 };
 
@@ -93,7 +97,7 @@ namespace {
 
 // one time step of one instance, reference order (src/main.c:61-79), on the
 // current library stream, without host synchronisation
-bool enqueue_step(BatchInst *b, bool normalize, int queue)
+bool enqueue_step(BatchInst *b, bool normalize, int queue, cudaStream_t body)
 {
   Discretization *d = &b->d;
   DiscState *st = disc_state(d);
@@ -117,8 +121,11 @@ bool enqueue_step(BatchInst *b, bool normalize, int queue)
     if (!launch_interior_sum(g, d->p, st->red, st->d_scalars + 3)) return false;
     if (!launch_subtract_mean(g, d->p, st->d_scalars + 4)) return false;
   }
-  if (!mg_enqueue(ss, d->p, d->rhs, queue, &b->dev->unconverged, &b->dev->last_cycles))
-    return false;
+  const bool solved = queue > 0 ? mg_enqueue(ss, d->p, d->rhs, queue, &b->dev->unconverged,
+                                      &b->dev->last_cycles)
+                                : mg_enqueue_loop(ss, d->p, d->rhs, body, &b->dev->unconverged,
+                                      &b->dev->last_cycles);
+  if (!solved) return false;
   if (!launch_adapt_uv(g, 0.0, d->grid.dx, d->grid.dy, d->grid.dz, d->f, d->g, d->h, d->p, d->u,
           d->v, d->w, sp))
     return false;
@@ -137,7 +144,7 @@ bool capture(NusifBatch *B, bool normalize, cudaGraphExec_t *out)
     if (!ok) break;
     ok = cuda_ok(cudaStreamWaitEvent(b->stream, B->fork, 0), "branch wait");
     nusifSetStream(b->stream);
-    ok = ok && enqueue_step(b, normalize, B->queue);
+    ok = ok && enqueue_step(b, normalize, B->queue, B->body);
     ok = ok && cuda_ok(cudaEventRecord(b->join, b->stream), "join record") &&
          cuda_ok(cudaStreamWaitEvent(B->main, b->join, 0), "join wait");
   }
@@ -199,6 +206,7 @@ void batch_free(NusifBatch *B)
     delete b;
   }
   if (B->fork) cudaEventDestroy(B->fork);
+  if (B->body) cudaStreamDestroy(B->body);
   if (B->main) cudaStreamDestroy(B->main);
   delete B;
 }
@@ -209,14 +217,15 @@ extern "C" {
 
 NusifBatch *nusifBatchCreate(int n, const char *const *parfiles, int queue, int tune)
 {
-  if (n < 1 || !parfiles || queue < 1) {
-    fail(NUSIF_ERR_ARG, "nusifBatchCreate: need at least one parameter file and queue >= 1");
+  if (n < 1 || !parfiles) {
+    fail(NUSIF_ERR_ARG, "nusifBatchCreate: need at least one parameter file");
     return nullptr;
   }
   NusifBatch *B = new NusifBatch();
   B->queue = queue;
   cudaStream_t saved = stream();
   bool ok = cuda_ok(cudaStreamCreateWithFlags(&B->main, cudaStreamNonBlocking), "stream") &&
+            cuda_ok(cudaStreamCreateWithFlags(&B->body, cudaStreamNonBlocking), "stream") &&
             cuda_ok(cudaEventCreateWithFlags(&B->fork, cudaEventDisableTiming), "event");
   for (int q = 0; q < n && ok; q++) {
     BatchInst *b = new BatchInst();

@@ -47,7 +47,7 @@ struct MgState {
   int maxcycles;
   int done;          // the solve is finished: every kernel returns at once
   int inner_done;    // mg-mixed: this outer iteration's correction is good enough
-  int pad;
+  int loops;         // units run by a graph while-loop (its independent stop)
 };
 
 // what the fold of a fine-level restriction decides
@@ -88,6 +88,9 @@ struct MgHierarchy {
   double rtol = 1e-6;
   int last_cycles = 0;  // queue size of the previous solve (cycles, or outer iterations)
   int inner = 4;        // mg-mixed: most FP32 V-cycles per FP64 residual
+  int guess = 0;        // 1: start from 2 p(n-1) - p(n-2)
+  double *p_prev = nullptr;  // padded copy of the previous solve's result (guess 1)
+  bool have_prev = false;
   double *h_ptrs[2 * kMaxLevels] = {};  // exposed through Solver::r / Solver::e
 };
 
@@ -107,6 +110,15 @@ __device__ __forceinline__ bool mg_done(const MgState *st)
 __device__ __forceinline__ bool solve_finished(const MgState *st)
 {
   return *reinterpret_cast<const volatile int *>(&st->done) != 0;
+}
+
+// x = 0 as a kernel (a plain kernel node wherever the launch is captured)
+template <typename T>
+__global__ void k_zero(T *__restrict__ x, int64_t n)
+{
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x)
+    x[q] = (T)0;
 }
 
 template <typename T>
@@ -647,6 +659,7 @@ __global__ void __launch_bounds__(kNT) k_mg_rhs_norm(View<double> f, MgState *st
     st->cycles = 0;
     st->outer = 0;
     st->inner_done = 0;
+    st->loops = 0;
     st->done = (total == 0.0);
     *ticket = 0;
   }
@@ -878,7 +891,10 @@ bool coarse_solve(const View<T> &v, int nsweeps, const MgState *st, const T *min
     return launched("k_mg_coarse");
   }
   // larger coarsest grids: sweeps in global memory
-  if (nsweeps == 0) return cuda_ok(cudaMemsetAsync(v.x, 0, n * sizeof(T), stream()), "zero x");
+  if (nsweeps == 0) {
+    k_zero<T><<<flat_blocks((int64_t)n), kNT, 0, stream()>>>(v.x, (int64_t)n);
+    return launched("k_zero");
+  }
   return sweeps<T>(v, nsweeps, true, nullptr, st);
 }
 
@@ -944,8 +960,9 @@ bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero, bool inner_test)
   }
   if (H->pre > 0) {
     if (!level_sweeps<T>(H, l, v, H->pre, zero, st)) return false;
-  } else if (zero && !cuda_ok(cudaMemsetAsync(xs[l], 0, n * sizeof(T), stream()), "zero x")) {
-    return false;
+  } else if (zero) {
+    k_zero<T><<<flat_blocks((int64_t)n), kNT, 0, stream()>>>(xs[l], (int64_t)n);
+    if (!launched("k_zero")) return false;
   }
   const bool ok = inner_test
                       ? restrict_to<T, FOLD_INNER>(v, bs[l + 1], H->lv[l + 1], nullptr, st, H->red)
@@ -957,6 +974,18 @@ bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero, bool inner_test)
 }
 
 // p += e (FP64) and Neumann ghosts of p, after the inner V-cycles
+// initial guess by linear extrapolation in time: p <- 2 p(n-1) - p(n-2), and
+// p(n-1) kept for the next solve (whole padded array, ghosts included)
+__global__ void k_extrapolate(double *__restrict__ p, double *__restrict__ p_prev, int64_t n)
+{
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const double cur = p[q];
+    p[q] = 2.0 * cur - p_prev[q];
+    p_prev[q] = cur;
+  }
+}
+
 __global__ void k_mx_fold(View<float> e, double *p, int p_sj, int p_sk, const MgState *st)
 {
   if (solve_finished(st)) return;
@@ -1025,6 +1054,12 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
   H->coarse_sweeps = x.mg_coarse_sweeps;
   H->maxcycles = x.mg_maxcycles;
   H->inner = x.mg_inner < 1 ? 1 : x.mg_inner;
+  H->guess = x.mg_guess == 1 ? 1 : 0;
+  if (H->guess == 1) {
+    const size_t padded =
+        (size_t)(d->grid.imax + 2) * (d->grid.jmax + 2) * (d->grid.kmax + 2) * sizeof(double);
+    if (!cuda_ok(cudaMalloc(&H->p_prev, padded), "cudaMalloc(p_prev)")) return false;
+  }
   H->rtol = x.rtol;
   if (H->pre < 0 || H->post < 0 || H->coarse_sweeps < 0 || H->maxcycles < 1 || !(H->rtol >= 0)) {
     fail(NUSIF_ERR_ARG, "multigrid: invalid mg_pre/mg_post/mg_coarse/mg_cycles/rtol");
@@ -1103,11 +1138,41 @@ __global__ void k_mg_state_init(MgState *st, double rtol2, int maxcycles)
   *st = s;
 }
 
-// after a captured solve: count a step whose queue ran out before rtol
+// after a captured solve: count a step whose last residual is above rtol (a
+// fixed queue that ran out, or the mg_cycles limit)
 __global__ void k_mg_count_unconverged(const MgState *st, int *counter, int *last_cycles)
 {
-  if (!st->done) *counter += 1;
+  if (!(st->res2 <= st->tol2)) *counter += 1;
   *last_cycles = st->cycles;
+}
+
+// end of one unit inside a graph while-loop: run another while the solve is
+// open. The unit count stops the loop on its own, whatever the flags say.
+__global__ void k_mg_continue(MgState *st, cudaGraphConditionalHandle h, int cap)
+{
+  const int n = st->loops + 1;
+  st->loops = n;
+  cudaGraphSetConditional(h, (st->done == 0 && n < cap) ? 1u : 0u);
+}
+
+bool enqueue_solve_head(MgHierarchy *H, const View<double> &v0)
+{
+  k_mg_state_init<<<1, 1, 0, stream()>>>(H->d_state, H->rtol * H->rtol, H->maxcycles);
+  if (!launched("k_mg_state_init")) return false;
+  const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
+  const int blocks = flat_blocks(n0);
+  k_mg_rhs_sum<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
+  if (!launched("k_mg_rhs_sum")) return false;
+  k_mg_rhs_norm<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
+  return launched("k_mg_rhs_norm");
+}
+
+bool enqueue_solve_tail(MgHierarchy *H, const View<double> &v0, double *p, int *unconverged,
+    int *last_cycles)
+{
+  if (!launch_pressure_ghosts(make_dims(v0.nx, v0.ny, v0.nz), p)) return false;
+  k_mg_count_unconverged<<<1, 1, 0, stream()>>>(H->d_state, unconverged, last_cycles);
+  return launched("k_mg_count_unconverged");
 }
 
 }  // namespace
@@ -1125,20 +1190,72 @@ bool mg_enqueue(SolverState *ss, double *p, const double *rhs, int queue, int *u
     fail(NUSIF_ERR_STATE, "mg enqueue without a hierarchy");
     return false;
   }
-  k_mg_state_init<<<1, 1, 0, stream()>>>(H->d_state, H->rtol * H->rtol, H->maxcycles);
-  if (!launched("k_mg_state_init")) return false;
   View<double> v0 = padded_view(H->lv[0], p, rhs);
-  const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
-  const int blocks = flat_blocks(n0);
-  k_mg_rhs_sum<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
-  if (!launched("k_mg_rhs_sum")) return false;
-  k_mg_rhs_norm<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
-  if (!launched("k_mg_rhs_norm")) return false;
+  if (!enqueue_solve_head(H, v0)) return false;
   for (int q = 0; q < queue; q++)
     if (!(H->mode == 0 ? cycle_fp64(H, p, rhs) : cycle_mixed(H, p, rhs))) return false;
-  if (!launch_pressure_ghosts(make_dims(v0.nx, v0.ny, v0.nz), p)) return false;
-  k_mg_count_unconverged<<<1, 1, 0, stream()>>>(H->d_state, unconverged, last_cycles);
-  return launched("k_mg_count_unconverged");
+  return enqueue_solve_tail(H, v0, p, unconverged, last_cycles);
+}
+
+// The same solve with its units in a CUDA graph while-loop, so that a step
+// runs exactly as many units as the host-driven solve: the loop body (one
+// unit and k_mg_continue) is captured on `body` into the conditional node's
+// graph, and the node joins the capture running on the library stream. The
+// loop ends when the solve is done, or after mg_cycles + 2 units whatever the
+// device flags say (the solve itself sets done by mg_cycles units).
+bool mg_enqueue_loop(SolverState *ss, double *p, const double *rhs, cudaStream_t body,
+    int *unconverged, int *last_cycles)
+{
+  MgHierarchy *H = ss->mg;
+  if (!H) {
+    fail(NUSIF_ERR_STATE, "mg enqueue without a hierarchy");
+    return false;
+  }
+  View<double> v0 = padded_view(H->lv[0], p, rhs);
+  if (!enqueue_solve_head(H, v0)) return false;
+  cudaStream_t outer = stream();
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t graph = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  const cudaGraphEdgeData *edges = nullptr;
+  size_t ndeps = 0;
+  if (!cuda_ok(cudaStreamGetCaptureInfo(outer, &cs, nullptr, &graph, &deps, &edges, &ndeps),
+          "capture info"))
+    return false;
+  if (cs != cudaStreamCaptureStatusActive) {
+    fail(NUSIF_ERR_STATE, "mg_enqueue_loop needs a stream capture in progress");
+    return false;
+  }
+  cudaGraphConditionalHandle handle;
+  if (!cuda_ok(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault),
+          "conditional handle"))
+    return false;
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = handle;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (!cuda_ok(cudaGraphAddNode(&node, graph, deps, edges, ndeps, &cp), "while node")) return false;
+  if (!cuda_ok(cudaStreamUpdateCaptureDependencies(outer, &node, nullptr, 1,
+                   cudaStreamSetCaptureDependencies),
+          "capture dependencies"))
+    return false;
+  cudaGraph_t loop = cp.conditional.phGraph_out[0];
+  if (!cuda_ok(cudaStreamBeginCaptureToGraph(body, loop, nullptr, nullptr, 0,
+                   cudaStreamCaptureModeThreadLocal),
+          "loop body capture"))
+    return false;
+  nusifSetStream(body);
+  bool ok = H->mode == 0 ? cycle_fp64(H, p, rhs) : cycle_mixed(H, p, rhs);
+  if (ok) {
+    k_mg_continue<<<1, 1, 0, stream()>>>(H->d_state, handle, H->maxcycles + 2);
+    ok = launched("k_mg_continue");
+  }
+  nusifSetStream(outer);
+  const bool ended = cuda_ok(cudaStreamEndCapture(body, &loop), "loop body end");
+  if (!ok || !ended) return false;
+  return enqueue_solve_tail(H, v0, p, unconverged, last_cycles);
 }
 
 // FP32 sweeps swap buffers on the host; a captured sequence must end with the
@@ -1168,6 +1285,18 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
   View<double> v0 = padded_view(H->lv[0], p, rhs);
   const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
   const int blocks = flat_blocks(n0);
+  if (H->guess == 1) {
+    const int64_t padded = (int64_t)(v0.nx + 2) * (v0.ny + 2) * (v0.nz + 2);
+    if (H->have_prev) {
+      k_extrapolate<<<flat_blocks(padded), kNT, 0, stream()>>>(p, H->p_prev, padded);
+      if (!launched("k_extrapolate")) return NAN;
+    } else if (!cuda_ok(cudaMemcpyAsync(H->p_prev, p, padded * sizeof(double),
+                            cudaMemcpyDeviceToDevice, stream()),
+                   "keep p")) {
+      return NAN;
+    }
+    H->have_prev = true;
+  }
   k_mg_rhs_sum<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
   if (!launched("k_mg_rhs_sum")) return NAN;
   k_mg_rhs_norm<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
@@ -1270,6 +1399,7 @@ void mg_free(Solver *s, SolverState *ss)
     if (H->x32b[l]) cudaFree(H->x32b[l]);
     if (H->b32[l]) cudaFree(H->b32[l]);
   }
+  if (H->p_prev) cudaFree(H->p_prev);
   if (H->minv64) cudaFree(H->minv64);
   if (H->minv32) cudaFree(H->minv32);
   if (H->d_state) cudaFree(H->d_state);

@@ -31,6 +31,7 @@ struct Extras {
   int mg_pre = 2, mg_post = 2;
   int mg_coarse_sweeps = 0;  // 0: exact coarsest solve (<= 1024 cells), else sweeps
   int mg_inner = 4;          // mg-mixed: most FP32 V-cycles per FP64 residual
+  int mg_guess = 0;          // initial guess: 0 previous p, 1 linear extrapolation in time
   int mg_maxcycles = 100;
 };
 Extras *extras_for(const Parameter *p, bool create);

@@ -54,6 +54,8 @@ bool mg_time_kernel(SolverState *ss, const double *p, const double *rhs, int whi
     double *ms_out);
 bool mg_enqueue(SolverState *ss, double *p, const double *rhs, int queue, int *unconverged,
     int *last_cycles);
+bool mg_enqueue_loop(SolverState *ss, double *p, const double *rhs, cudaStream_t body,
+    int *unconverged, int *last_cycles);
 bool mg_capture_ok(const SolverState *ss);
 
 }  // namespace nusif

@@ -23,12 +23,15 @@ class InstanceStats:
     dt: float
     nt: int
     cycles: int          # V-cycles of the last step
-    unconverged: int     # steps whose queue ended above rtol
+    unconverged: int     # steps whose solve ended above rtol
     fg_planes: int       # autotuned planes per block of the F/G/H kernel
 
 
 class Batch:
-    def __init__(self, cases: list[dict | str | Path], queue: int = 4, tune: bool = True):
+    def __init__(self, cases: list[dict | str | Path], queue: int = 0, tune: bool = True):
+        """queue = 0: each step's multigrid solve is a CUDA graph while-loop that
+        stops at rtol, as the host-driven solve does; queue > 0: a fixed number of
+        device-gated multigrid units per step (steps left above rtol are counted)."""
         self.lib = abi.load_library()
         self._tmp = tempfile.TemporaryDirectory(prefix="nusif_batch_")
         paths = []

@@ -192,9 +192,10 @@ NUSIF_API int nusifWriteVTK(const Discretization *d, const char *path, int binar
 /* Batched instances (no reference counterpart: the reference runs one case per
  * process). Each parameter file is one independent case (uneven grids welcome)
  * with the mg or mg-mixed solver (even mg_pre / mg_post). One time step of
- * every instance is captured as one CUDA graph (device-side dt, a queue of
- * `queue` device-gated multigrid units per step); tune != 0 times the F/G/H
- * tile depth per instance first. Returns NULL on error. */
+ * every instance is captured as one CUDA graph (device-side dt; the multigrid
+ * solve a graph while-loop that stops at rtol like the host-driven solve, or
+ * with queue > 0 a fixed `queue` device-gated units per step); tune != 0
+ * times the F/G/H tile depth per instance first. Returns NULL on error. */
 typedef struct NusifBatch NusifBatch;
 NUSIF_API NusifBatch *nusifBatchCreate(int n, const char *const *parfiles, int queue, int tune);
 /* advance every instance by `steps` time steps (one graph launch each) */
@@ -203,7 +204,8 @@ NUSIF_API int nusifBatchSize(const NusifBatch *b);
 /* the instance's Discretization / Solver, for nusifDownloadField and friends */
 NUSIF_API int nusifBatchInstance(NusifBatch *b, int idx, Discretization **d, Solver **s);
 /* per instance: time, last dt, steps, V-cycles of the last step, steps that
- * ended above rtol (queue too short), autotuned F/G/H planes per block */
+ * ended above rtol (fixed queue too short, or mg_cycles reached), autotuned
+ * F/G/H planes per block */
 NUSIF_API int nusifBatchStats(NusifBatch *b, int idx, double *t, double *dt, int *nt, int *cycles,
     int *unconverged, int *fg_planes);
 NUSIF_API void nusifBatchFree(NusifBatch *b);
