@@ -9,3 +9,4 @@ from .abi import NusifError, load_library, check, LIB_PATH  # noqa: F401
 from .params import write_par, cavity, config1, config2, channel, DCAVITY, CANAL  # noqa: F401
 from .sim import Simulation, StepInfo  # noqa: F401
 from .batch import Batch, InstanceStats  # noqa: F401
+from .unet import UNet  # noqa: F401

@@ -113,6 +113,17 @@ SIGNATURES = [
     ("nusifTimeKernel", C.c_int, [C.POINTER(Solver), c_double_p, c_double_p, C.c_int, C.c_int,
                                   C.POINTER(C.c_double)]),
     ("nusifVersion", C.c_char_p, []),
+    ("nusifUNetCreate", C.c_void_p, [C.c_ulonglong]),
+    ("nusifUNetFree", None, [C.c_void_p]),
+    ("nusifUNetParamCount", C.c_longlong, [C.c_void_p]),
+    ("nusifUNetGetParams", C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
+    ("nusifUNetSetParams", C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
+    ("nusifUNetGetGrads", C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
+    ("nusifUNetForward", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                   C.c_void_p]),
+    ("nusifUNetTrainStep", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                     C.c_int, C.c_int, C.c_float, C.c_int,
+                                     C.POINTER(C.c_float)]),
 ]
 
 _lib = None

@@ -222,6 +222,32 @@ NUSIF_API int nusifTimeKernel(Solver *s, const double *p, const double *rhs, int
 /* library version string */
 NUSIF_API const char *nusifVersion(void);
 
+/* Learned pressure warm start (no reference counterpart). A 3-level 3D U-Net
+ * (16/32/64 channels, 243,473 parameters; BF16 weights and activations, FP32
+ * accumulation and master weights) trained and run by this library's kernels.
+ * Volumes are device arrays, channels-last [B][Z][Y][X][C], every edge a
+ * multiple of 4; the input has 2 channels, the output 1. Parameters form one
+ * flat FP32 vector: per layer (e0a e0b e1a e1b e2a d1a d1b d0a d0b out)
+ * W[27][cout][cin] then b[cout]. */
+typedef struct NusifUNet NusifUNet;
+/* He-normal initial weights from `seed`, zero biases, Adam state zero */
+NUSIF_API NusifUNet *nusifUNetCreate(unsigned long long seed);
+NUSIF_API void nusifUNetFree(NusifUNet *net);
+NUSIF_API long long nusifUNetParamCount(const NusifUNet *net);
+NUSIF_API int nusifUNetGetParams(const NusifUNet *net, float *host, long long count);
+/* replaces the weights and clears the Adam state */
+NUSIF_API int nusifUNetSetParams(NusifUNet *net, const float *host, long long count);
+/* gradients of the last nusifUNetTrainStep (host copy) */
+NUSIF_API int nusifUNetGetGrads(const NusifUNet *net, float *host, long long count);
+/* out (device, [B][Z][Y][X]) = net(x) */
+NUSIF_API int nusifUNetForward(NusifUNet *net, const float *x, int B, int Z, int Y, int X,
+    float *out);
+/* forward, mean-squared-error loss against `target` (device), backward; with
+ * update != 0 one Adam step (lr, beta 0.9 / 0.999, eps 1e-8). loss_host may be
+ * NULL (no synchronisation). */
+NUSIF_API int nusifUNetTrainStep(NusifUNet *net, const float *x, const float *target, int B, int Z,
+    int Y, int X, float lr, int update, float *loss_host);
+
 #ifdef __cplusplus
 }
 #endif
