@@ -55,8 +55,14 @@ def parse_args():
     ap.add_argument("--guess", default="extrapolate", choices=["previous", "extrapolate"],
                     help="initial pressure of each V-cycle solve: p(n-1), or 2 p(n-1) - p(n-2)")
     ap.add_argument("--batch-n", type=int, default=96, help="instances of the batch workload")
-    ap.add_argument("--workload", default="cavity", choices=["cavity", "channel", "batch"],
-                    help="cavity: the 256^3 benchmark; channel: mixed vs FP64 error study")
+    ap.add_argument("--workload", default="cavity",
+                    choices=["cavity", "channel", "batch", "learned"],
+                    help="cavity: the 256^3 benchmark; channel: mixed vs FP64 error study; "
+                         "batch: 96 uneven cavities; learned: the U-Net warm start")
+    ap.add_argument("--learn-runs", type=int, default=64, help="training cavities (learned)")
+    ap.add_argument("--learn-n", type=int, default=128, help="training cavity edge (learned)")
+    ap.add_argument("--learn-steps", type=int, default=300, help="steps per training run")
+    ap.add_argument("--learn-iters", type=int, default=2000, help="Adam iterations (learned)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-roofline", action="store_true",
                     help="skip the per-kernel timing launches (clean launch lists for ncu)")
@@ -620,6 +626,83 @@ def run_batch(args, local):
     }
 
 
+LEARN_SEED = 20261204
+
+
+def run_learned(args, local):
+    """Learned warm start: pairs recorded by the solver on cavities at
+    args.learn_n^3 (Re ~ U[100, 5000], lid ~ U[0.5, 2], seeded), the U-Net
+    trained with the library's kernels, then evaluated as the warm start of
+    mixed-precision multigrid on a cavity at args.n^3 and an unseen Re / lid,
+    against the same run without the network (ms per step and V-cycles)."""
+    import numpy as np
+    import torch
+
+    import nusif
+    from nusif.learn import generate_pairs, train, training_cases
+    torch.cuda.set_device(local)
+    lib = nusif.load_library()
+    stream = torch.cuda.current_stream()
+    lib.nusifSetStream(C.c_void_p(stream.cuda_stream))
+    cases = training_cases(args.learn_runs, args.learn_n, LEARN_SEED, guess=args.guess)
+    data = generate_pairs(cases, steps=args.learn_steps, every=5, skip=10)
+    net = nusif.UNet(seed=LEARN_SEED)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    log = train(net, data, iters=args.learn_iters, batch=8, lr=1e-3,
+                log_every=max(args.learn_iters // 8, 1))
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    n = args.n
+    evals = {}
+    for use in (False, True):
+        vals = bench_case(n, "mg-mixed", args.itermax, args.guess)
+        vals.update(re=2750.0, lid=1.25)
+        sim = nusif.Simulation(vals)
+        if use:
+            sim.set_guess_net(net)
+        for _ in range(args.warmup):
+            sim.step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        its, taken, ratios = [], 0, []
+        ms = 0.0
+        for _ in range(args.steps):
+            e0.record(stream)
+            its.append(sim.step().it)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms += e0.elapsed_time(e1)
+            if use:
+                u, rw, rg = sim.guess_stats()
+                taken += int(u)
+                ratios.append(rg / rw if rw > 0 else 1.0)
+        sim.close()
+        evals[use] = {"ms_per_step": ms / args.steps, "v_cycles_per_step": its}
+        if use:
+            evals[use].update({"guess_taken_steps": taken,
+                               "restricted_residual_ratio_median": float(np.median(ratios))})
+    net.close()
+    return {
+        "metric": "learned warm start: ms/timestep at %d^3 to 1e-6, mixed-precision MG with vs "
+                  "without the trained U-Net" % n,
+        "value": evals[True]["ms_per_step"], "unit": "ms/timestep", "higher_is_better": False,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "dtype": "bf16 net, f64+f32 solve",
+        "data": "synthetic: pairs recorded by the solver on seeded cavities",
+        "config": {"workload": f"train on {args.learn_runs} cavities at {args.learn_n}^3 "
+                               f"(Re ~ U[100,5000], lid ~ U[0.5,2.0], seed {LEARN_SEED}), "
+                               f"snapshots every 5 steps from step 10 to {args.learn_steps}; "
+                               f"evaluate at {n}^3, Re 2750, lid 1.25",
+                   "warm_start_base": args.guess, "pairs": int(data.x.shape[0]),
+                   "train_iters": args.learn_iters, "batch": 8, "lr": "1e-3 cosine to 1e-4"},
+        "pair_generation_s": data.seconds, "train_s": train_s,
+        "train_ms_per_iter": train_s * 1e3 / max(args.learn_iters, 1),
+        "loss": log,
+        "with_net": evals[True], "without_net": evals[False],
+        "speedup_vs_without": evals[False]["ms_per_step"] / evals[True]["ms_per_step"],
+    }
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_info()
@@ -629,6 +712,8 @@ def main():
         out = run_channel(args, local) if rank == 0 else None
     elif args.workload == "batch":
         out = run_batch(args, local) if rank == 0 else None
+    elif args.workload == "learned":
+        out = run_learned(args, local) if rank == 0 else None
     else:
         out = run_gpu(args, rank, world, local)
     if out is not None and rank == 0:

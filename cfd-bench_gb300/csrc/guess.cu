@@ -1,0 +1,461 @@
+// Learned pressure warm start around a multigrid solve (no reference
+// counterpart). The network works on the half-resolution grid:
+//
+//   features  x = [R(b - s - A p0) / sigma_r, R(b - s) / sigma_b]
+//   target    t = R(p* - p0) * kappa / sigma_r
+//   guess     p1 = p0 + P(net(x) * sigma_r / kappa)
+//
+// p0 the warm start (previous or extrapolated p), p* the converged p, s the
+// mean of b, A the multigrid's ghost-free Neumann operator, kappa =
+// pi^2 (1/Lx^2 + 1/Ly^2 + 1/Lz^2) the scale of its smallest eigenvalues (so
+// that targets are O(1) and independent of the resolution),
+// R the 8-child mean, P trilinear interpolation (the multigrid's transfers),
+// sigma the RMS of each restricted field. The solver keeps p1 only when its
+// restricted residual ||R(b - s - A p1)|| is below that of p0, so the plain
+// warm start stays the fallback; the V-cycles then run to the same tolerance
+// either way.
+//
+// Every reduction folds per-block partials in a fixed order (deterministic).
+#include <cmath>
+
+#include "nusif_internal.h"
+#include "reduce.cuh"
+#include "solver_internal.h"
+#include "unet_internal.h"
+
+namespace nusif {
+
+struct GuessStats {
+  double shift;    // mean of b over the interior
+  double nb2;      // ||b - s||^2 (fine)
+  double r2_warm;  // ||b - s - A p0||^2 (fine)
+  double r2_cand;  // ||b - s - A p1||^2 (fine)
+  double rc2, bc2; // sums of squares of the restricted residual of p0 and of the rhs
+  double rc2_cand; // sum of squares of the restricted residual of p1 (the decision)
+  double sigma_r, sigma_b;
+  int used;        // p1 replaced p0
+  int pad;
+};
+
+struct GuessState {
+  NusifUNet *net = nullptr;
+  float *rec_x = nullptr, *rec_t = nullptr;  // caller's buffers of a recording request
+  bool recording = false;
+  int nx = 0, ny = 0, nz = 0;
+  float *x = nullptr;       // own feature buffer [nc][2]
+  double *aux = nullptr;    // padded: p0 (recording) or p1 (candidate)
+  double *partial = nullptr;
+  GuessStats *d_stats = nullptr, *h_stats = nullptr;
+  int64_t nc = 0;
+};
+
+namespace {
+
+constexpr int kNT = 256;
+constexpr int kBlocks = 4 * 152;  // partial slots per reduction
+
+struct GGeom {
+  int nx, ny, nz;     // fine interior
+  int sj, sk;         // padded strides
+  double ex, ey, ez;  // 1/h^2
+  double kappa;       // pi^2 (1/Lx^2 + 1/Ly^2 + 1/Lz^2): the operator's smallest-eigenvalue scale
+  __device__ int64_t pidx(int i, int j, int k) const
+  {
+    return (int64_t)(k + 1) * sk + (int64_t)(j + 1) * sj + (i + 1);
+  }
+};
+
+// b - s - A p at fine interior cell (i, j, k), Neumann operator without ghosts
+__device__ __forceinline__ double resid(const GGeom &g, const double *p, const double *b,
+    double s, int i, int j, int k)
+{
+  const int64_t c = g.pidx(i, j, k);
+  const double xc = p[c];
+  const double sx = (i > 0 ? p[c - 1] : xc) + (i < g.nx - 1 ? p[c + 1] : xc);
+  const double sy = (j > 0 ? p[c - g.sj] : xc) + (j < g.ny - 1 ? p[c + g.sj] : xc);
+  const double sz = (k > 0 ? p[c - g.sk] : xc) + (k < g.nz - 1 ? p[c + g.sk] : xc);
+  const double lap = g.ex * (sx - 2.0 * xc) + g.ey * (sy - 2.0 * xc) + g.ez * (sz - 2.0 * xc);
+  return (b[c] - s) - lap;
+}
+
+template <int K>
+__device__ __forceinline__ void block_partials(double (&v)[K], double *partial)
+{
+  __shared__ double sm[kNT / 32];
+#pragma unroll
+  for (int q = 0; q < K; q++) {
+    const double t = block_reduce_sum<kNT>(v[q], sm);
+    if (threadIdx.x == 0) partial[(int64_t)blockIdx.x * K + q] = t;
+  }
+}
+
+__global__ void __launch_bounds__(kNT) k_g_sum_b(GGeom g, const double *b, double *partial)
+{
+  const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+  double v[1] = { 0.0 };
+  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n; q += (int64_t)gridDim.x * kNT) {
+    const int i = (int)(q % g.nx);
+    const int64_t r = q / g.nx;
+    v[0] += b[g.pidx(i, (int)(r % g.ny), (int)(r / g.ny))];
+  }
+  block_partials<1>(v, partial);
+}
+
+__global__ void k_g_fold_shift(const double *partial, int nb, int64_t n, GuessStats *st)
+{
+  double s = 0.0;
+  for (int q = 0; q < nb; q++) s += partial[q];
+  st->shift = s / (double)n;
+}
+
+// one thread per coarse cell: restricted residual and rhs (unnormalised) into
+// x, and the four sums of squares
+__global__ void __launch_bounds__(kNT) k_g_features(GGeom g, const double *p, const double *b,
+    const GuessStats *st, float *x, double *partial)
+{
+  const int cx = g.nx / 2, cy = g.ny / 2, cz = g.nz / 2;
+  const int64_t n = (int64_t)cx * cy * cz;
+  const double s = st->shift;
+  double v[4] = { 0.0, 0.0, 0.0, 0.0 };
+  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n; q += (int64_t)gridDim.x * kNT) {
+    const int I = (int)(q % cx);
+    const int64_t r = q / cx;
+    const int J = (int)(r % cy), K = (int)(r / cy);
+    double rs = 0.0, bs = 0.0;
+    for (int c = 0; c < 8; c++) {
+      const int i = 2 * I + (c & 1), j = 2 * J + ((c >> 1) & 1), k = 2 * K + (c >> 2);
+      const double rr = resid(g, p, b, s, i, j, k);
+      const double bb = b[g.pidx(i, j, k)] - s;
+      rs += rr;
+      bs += bb;
+      v[0] += rr * rr;
+      v[1] += bb * bb;
+    }
+    rs *= 0.125;
+    bs *= 0.125;
+    v[2] += rs * rs;
+    v[3] += bs * bs;
+    x[2 * q] = (float)rs;
+    x[2 * q + 1] = (float)bs;
+  }
+  block_partials<4>(v, partial);
+}
+
+__global__ void k_g_fold_features(const double *partial, int nb, int64_t nc, GuessStats *st)
+{
+  double t[4] = { 0.0, 0.0, 0.0, 0.0 };
+  for (int q = 0; q < nb; q++)
+    for (int k = 0; k < 4; k++) t[k] += partial[4 * q + k];
+  st->r2_warm = t[0];
+  st->nb2 = t[1];
+  st->rc2 = t[2];
+  st->bc2 = t[3];
+  const double sr = sqrt(t[2] / (double)nc), sb = sqrt(t[3] / (double)nc);
+  st->sigma_r = sr > 0.0 ? sr : 1.0;
+  st->sigma_b = sb > 0.0 ? sb : 1.0;
+  st->used = 0;
+  st->r2_cand = 0.0;
+}
+
+__global__ void k_g_normalize(float *x, int64_t nc, const GuessStats *st)
+{
+  const float ir = (float)(1.0 / st->sigma_r), ib = (float)(1.0 / st->sigma_b);
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nc;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    x[2 * q] *= ir;
+    x[2 * q + 1] *= ib;
+  }
+}
+
+// t = R(p* - p0) * kappa / sigma_r
+__global__ void k_g_target(GGeom g, const double *pconv, const double *p0, const GuessStats *st,
+    float *t)
+{
+  const int cx = g.nx / 2, cy = g.ny / 2, cz = g.nz / 2;
+  const int64_t n = (int64_t)cx * cy * cz;
+  const double scale = g.kappa / st->sigma_r;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int I = (int)(q % cx);
+    const int64_t r = q / cx;
+    const int J = (int)(r % cy), K = (int)(r / cy);
+    double s = 0.0;
+    for (int c = 0; c < 8; c++) {
+      const int64_t f = g.pidx(2 * I + (c & 1), 2 * J + ((c >> 1) & 1), 2 * K + (c >> 2));
+      s += pconv[f] - p0[f];
+    }
+    t[q] = (float)(0.125 * s * scale);
+  }
+}
+
+// p1 = p0 + P(out * sigma_r / kappa) on the interior, Neumann ghosts from it;
+// trilinear weights 3/4 and 1/4 toward the coarse neighbour on the fine
+// cell's side (clamped at the walls), as the multigrid prolongation
+__global__ void k_g_candidate(GGeom g, const double *p0, const float *out, const GuessStats *st,
+    double *p1)
+{
+  const int cx = g.nx / 2, cy = g.ny / 2, cz = g.nz / 2;
+  const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+  const double scale = st->sigma_r / g.kappa;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q % g.nx);
+    const int64_t r = q / g.nx;
+    const int j = (int)(r % g.ny), k = (int)(r / g.ny);
+    const int P[3] = { i >> 1, j >> 1, k >> 1 };
+    const int C[3] = { cx, cy, cz };
+    const int F[3] = { i, j, k };
+    int Q[3];
+    for (int a = 0; a < 3; a++) {
+      const int nb = (F[a] & 1) ? P[a] + 1 : P[a] - 1;
+      Q[a] = (nb < 0 || nb >= C[a]) ? P[a] : nb;
+    }
+    double e = 0.0;
+    for (int c = 0; c < 8; c++) {
+      const int X = (c & 1) ? Q[0] : P[0], Y = ((c >> 1) & 1) ? Q[1] : P[1], Z = (c >> 2) ? Q[2] : P[2];
+      const double w = ((c & 1) ? 0.25 : 0.75) * (((c >> 1) & 1) ? 0.25 : 0.75) * ((c >> 2) ? 0.25 : 0.75);
+      e += w * (double)out[((int64_t)Z * cy + Y) * cx + X];
+    }
+    const int64_t pc = g.pidx(i, j, k);
+    const double v = p0[pc] + e * scale;
+    p1[pc] = v;
+    if (i == 0) p1[pc - 1] = v;
+    if (i == g.nx - 1) p1[pc + 1] = v;
+    if (j == 0) p1[pc - g.sj] = v;
+    if (j == g.ny - 1) p1[pc + g.sj] = v;
+    if (k == 0) p1[pc - g.sk] = v;
+    if (k == g.nz - 1) p1[pc + g.sk] = v;
+  }
+}
+
+// ||b - s - A p1||^2 summed in exactly the order k_g_features sums p0's (same
+// grid, same per-thread walk over coarse cells and children), so that p1 == p0
+// gives the same number bit for bit
+__global__ void __launch_bounds__(kNT) k_g_cand_norm(GGeom g, const double *p1, const double *b,
+    const GuessStats *st, double *partial)
+{
+  const int cx = g.nx / 2, cy = g.ny / 2, cz = g.nz / 2;
+  const int64_t n = (int64_t)cx * cy * cz;
+  const double s = st->shift;
+  double v[2] = { 0.0, 0.0 };
+  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n; q += (int64_t)gridDim.x * kNT) {
+    const int I = (int)(q % cx);
+    const int64_t r = q / cx;
+    const int J = (int)(r % cy), K = (int)(r / cy);
+    double rs = 0.0;
+    for (int c = 0; c < 8; c++) {
+      const double rr = resid(g, p1, b, s, 2 * I + (c & 1), 2 * J + ((c >> 1) & 1), 2 * K + (c >> 2));
+      rs += rr;
+      v[0] += rr * rr;
+    }
+    rs *= 0.125;
+    v[1] += rs * rs;
+  }
+  block_partials<2>(v, partial);
+}
+
+// the guess is kept when its restricted residual is smaller: the smooth error
+// is what the V-cycles pay for; the high-frequency residual that interpolating
+// a coarse correction leaves is removed by the first smoothing sweep
+__global__ void k_g_fold_select(const double *partial, int nb, GuessStats *st)
+{
+  double s = 0.0, sc = 0.0;
+  for (int q = 0; q < nb; q++) {
+    s += partial[2 * q];
+    sc += partial[2 * q + 1];
+  }
+  st->r2_cand = s;
+  st->rc2_cand = sc;
+  st->used = sc < st->rc2 ? 1 : 0;
+}
+
+// p = p1 over the whole padded array when the guess won
+__global__ void k_g_take(double *p, const double *p1, int64_t n, const GuessStats *st)
+{
+  if (!st->used) return;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x)
+    p[q] = p1[q];
+}
+
+GGeom geom(const Grid *grid)
+{
+  GGeom g;
+  g.nx = grid->imax;
+  g.ny = grid->jmax;
+  g.nz = grid->kmax;
+  g.sj = grid->imax + 2;
+  g.sk = (grid->imax + 2) * (grid->jmax + 2);
+  g.ex = 1.0 / (grid->dx * grid->dx);
+  g.ey = 1.0 / (grid->dy * grid->dy);
+  g.ez = 1.0 / (grid->dz * grid->dz);
+  const double lx = grid->imax * grid->dx, ly = grid->jmax * grid->dy, lz = grid->kmax * grid->dz;
+  g.kappa = 9.869604401089358 * (1.0 / (lx * lx) + 1.0 / (ly * ly) + 1.0 / (lz * lz));
+  return g;
+}
+
+int flat(int64_t n)
+{
+  int64_t b = (n + 255) / 256;
+  return (int)(b > kBlocks ? kBlocks : (b < 1 ? 1 : b));
+}
+
+bool ensure(GuessState *gs, const Grid *grid)
+{
+  if (grid->imax % 8 || grid->jmax % 8 || grid->kmax % 8) {
+    fail(NUSIF_ERR_ARG, "learned warm start: grid %dx%dx%d needs every edge a multiple of 8",
+        grid->imax, grid->jmax, grid->kmax);
+    return false;
+  }
+  if (gs->nx == grid->imax && gs->ny == grid->jmax && gs->nz == grid->kmax) return true;
+  if (gs->nx) {
+    fail(NUSIF_ERR_STATE, "learned warm start: grid changed");
+    return false;
+  }
+  gs->nx = grid->imax;
+  gs->ny = grid->jmax;
+  gs->nz = grid->kmax;
+  gs->nc = (int64_t)gs->nx * gs->ny * gs->nz / 8;
+  const size_t padded = (size_t)(gs->nx + 2) * (gs->ny + 2) * (gs->nz + 2);
+  return cuda_ok(cudaMalloc(&gs->x, gs->nc * 2 * sizeof(float)), "cudaMalloc(guess)") &&
+         cuda_ok(cudaMalloc(&gs->aux, padded * sizeof(double)), "cudaMalloc(guess)") &&
+         cuda_ok(cudaMalloc(&gs->partial, kBlocks * 4 * sizeof(double)), "cudaMalloc(guess)") &&
+         cuda_ok(cudaMalloc(&gs->d_stats, sizeof(GuessStats)), "cudaMalloc(guess)") &&
+         cuda_ok(cudaMallocHost(&gs->h_stats, sizeof(GuessStats)), "cudaMallocHost(guess)") &&
+         cuda_ok(cudaMemsetAsync(gs->d_stats, 0, sizeof(GuessStats), stream()), "guess init");
+}
+
+// shift, then the features of p into x (normalised); returns the block count
+bool features(GuessState *gs, const GGeom &g, const double *p, const double *rhs, float *x)
+{
+  const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+  const int nb = flat(n);
+  k_g_sum_b<<<nb, kNT, 0, stream()>>>(g, rhs, gs->partial);
+  if (!launched("k_g_sum_b")) return false;
+  k_g_fold_shift<<<1, 1, 0, stream()>>>(gs->partial, nb, n, gs->d_stats);
+  if (!launched("k_g_fold_shift")) return false;
+  const int nbc = flat(gs->nc);
+  k_g_features<<<nbc, kNT, 0, stream()>>>(g, p, rhs, gs->d_stats, x, gs->partial);
+  if (!launched("k_g_features")) return false;
+  k_g_fold_features<<<1, 1, 0, stream()>>>(gs->partial, nbc, gs->nc, gs->d_stats);
+  if (!launched("k_g_fold_features")) return false;
+  k_g_normalize<<<flat(gs->nc), 256, 0, stream()>>>(x, gs->nc, gs->d_stats);
+  return launched("k_g_normalize");
+}
+
+}  // namespace
+
+bool guess_before_solve(GuessState *gs, const Grid *grid, double *p, const double *rhs)
+{
+  if (!gs || (!gs->net && !gs->recording)) return true;
+  if (!ensure(gs, grid)) return false;
+  const GGeom g = geom(grid);
+  const int64_t padded = (int64_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+  float *x = gs->recording ? gs->rec_x : gs->x;
+  if (!features(gs, g, p, rhs, x)) return false;
+  if (gs->recording) {
+    // the target needs p0 after the solve
+    return cuda_ok(cudaMemcpyAsync(gs->aux, p, padded * sizeof(double), cudaMemcpyDeviceToDevice,
+                       stream()),
+        "keep p0");
+  }
+  const float *out = nullptr;
+  if (!unet_infer(gs->net, x, g.nz / 2, g.ny / 2, g.nx / 2, &out)) return false;
+  const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+  k_g_candidate<<<flat(n), 256, 0, stream()>>>(g, p, out, gs->d_stats, gs->aux);
+  if (!launched("k_g_candidate")) return false;
+  const int nb = flat(gs->nc);  // the features' grid (same summation order)
+  k_g_cand_norm<<<nb, kNT, 0, stream()>>>(g, gs->aux, rhs, gs->d_stats, gs->partial);
+  if (!launched("k_g_cand_norm")) return false;
+  k_g_fold_select<<<1, 1, 0, stream()>>>(gs->partial, nb, gs->d_stats);
+  if (!launched("k_g_fold_select")) return false;
+  k_g_take<<<flat(padded), 256, 0, stream()>>>(p, gs->aux, padded, gs->d_stats);
+  return launched("k_g_take");
+}
+
+bool guess_after_solve(GuessState *gs, const Grid *grid, const double *p)
+{
+  if (!gs || !gs->recording) return true;
+  gs->recording = false;
+  const GGeom g = geom(grid);
+  k_g_target<<<flat(gs->nc), 256, 0, stream()>>>(g, p, gs->aux, gs->d_stats, gs->rec_t);
+  return launched("k_g_target");
+}
+
+void guess_free(GuessState *gs)
+{
+  if (!gs) return;
+  if (gs->x) cudaFree(gs->x);
+  if (gs->aux) cudaFree(gs->aux);
+  if (gs->partial) cudaFree(gs->partial);
+  if (gs->d_stats) cudaFree(gs->d_stats);
+  if (gs->h_stats) cudaFreeHost(gs->h_stats);
+  delete gs;
+}
+
+namespace {
+
+GuessState *guess_state_for(Solver *s)
+{
+  SolverState *ss = s ? solver_state(s) : nullptr;
+  if (!ss || !ss->mg) {
+    fail(NUSIF_ERR_STATE, "learned warm start: needs a solver initialised with mg or mg-mixed");
+    return nullptr;
+  }
+  if (!ss->guess) ss->guess = new GuessState();
+  return ss->guess;
+}
+
+}  // namespace
+}  // namespace nusif
+
+using namespace nusif;
+
+extern "C" {
+
+int nusifSolverSetGuessNet(Solver *s, NusifUNet *net)
+{
+  GuessState *gs = guess_state_for(s);
+  if (!gs) return NUSIF_ERR_STATE;
+  gs->net = net;
+  return NUSIF_OK;
+}
+
+int nusifSolverRecordPair(Solver *s, float *x, float *t)
+{
+  GuessState *gs = guess_state_for(s);
+  if (!gs) return NUSIF_ERR_STATE;
+  if (!x || !t) {
+    fail(NUSIF_ERR_ARG, "nusifSolverRecordPair: null buffer");
+    return NUSIF_ERR_ARG;
+  }
+  gs->rec_x = x;
+  gs->rec_t = t;
+  gs->recording = true;
+  return NUSIF_OK;
+}
+
+int nusifSolverGuessStats(Solver *s, int *used, double *rel_warm, double *rel_guess)
+{
+  GuessState *gs = guess_state_for(s);
+  if (!gs) return NUSIF_ERR_STATE;
+  if (!gs->d_stats) {
+    if (used) *used = 0;
+    if (rel_warm) *rel_warm = 0.0;
+    if (rel_guess) *rel_guess = 0.0;
+    return NUSIF_OK;
+  }
+  if (!cuda_ok(cudaMemcpyAsync(gs->h_stats, gs->d_stats, sizeof(GuessStats), cudaMemcpyDeviceToHost,
+                   stream()),
+          "guess stats") ||
+      !cuda_ok(cudaStreamSynchronize(stream()), "guess stats"))
+    return NUSIF_ERR_CUDA;
+  const GuessStats &h = *gs->h_stats;
+  const double nb = h.bc2 > 0.0 ? h.bc2 : 1.0;
+  if (used) *used = h.used;
+  if (rel_warm) *rel_warm = sqrt(h.rc2 / nb);
+  if (rel_guess) *rel_guess = sqrt(h.rc2_cand / nb);
+  return NUSIF_OK;
+}
+
+}  // extern "C"

@@ -28,6 +28,7 @@
 #include "nusif_internal.h"
 #include "reduce.cuh"
 #include "solver_internal.h"
+#include "unet_internal.h"
 
 namespace nusif {
 
@@ -1274,7 +1275,6 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
     fail(NUSIF_ERR_STATE, "mg solve without a hierarchy");
     return NAN;
   }
-  (void)s;
   MgState *h = H->h_state;
   memset(h, 0, sizeof(*h));
   h->rtol2 = H->rtol * H->rtol;
@@ -1297,6 +1297,8 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
     }
     H->have_prev = true;
   }
+  // learned warm start: may replace p by the network's guess (never a worse residual)
+  if (ss->guess && !guess_before_solve(ss->guess, s->grid, p, rhs)) return NAN;
   k_mg_rhs_sum<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
   if (!launched("k_mg_rhs_sum")) return NAN;
   k_mg_rhs_norm<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
@@ -1317,6 +1319,7 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
     chunk = 2;
   }
   if (!launch_pressure_ghosts(make_dims(v0.nx, v0.ny, v0.nz), p)) return NAN;
+  if (ss->guess && !guess_after_solve(ss->guess, s->grid, p)) return NAN;
   // queue as many units next time: V-cycles (mg) or residual evaluations (mg-mixed)
   H->last_cycles = H->mode == 0 ? h->cycles : h->outer + 1;
   ss->last_iterations = h->cycles;

@@ -28,6 +28,7 @@
 #include "nusif_internal.h"
 #include "reduce.cuh"
 #include "solver_internal.h"
+#include "unet_internal.h"
 
 namespace nusif {
 
@@ -464,6 +465,8 @@ void nusifFreeSolver(Solver *s)
   SolverState *ss = solver_state(s);
   if (!ss) return;
   cudaStreamSynchronize(stream());
+  guess_free(ss->guess);
+  ss->guess = nullptr;
   mg_free(s, ss);
   if (ss->d_state) cudaFree(ss->d_state);
   if (ss->h_state) cudaFreeHost(ss->h_state);

@@ -43,6 +43,7 @@ struct SolverState {
   ReduceScratch red;
   int last_iterations = 0;
   MgHierarchy *mg = nullptr;
+  struct GuessState *guess = nullptr;  // learned warm start (guess.cu)
 };
 
 SolverState *solver_state(const Solver *s);

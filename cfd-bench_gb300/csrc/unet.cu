@@ -993,6 +993,19 @@ NusifUNet *checked(NusifUNet *n)
 
 }  // namespace
 
+namespace nusif {
+
+bool unet_infer(NusifUNet *net, const float *x, int Z, int Y, int X, const float **out)
+{
+  UNetState *u = &net->s;
+  const Vol v = { 1, Z, Y, X };
+  if (!unet_set_input(u, x, v) || !unet_forward(u)) return false;
+  *out = u->out;
+  return true;
+}
+
+}  // namespace nusif
+
 extern "C" {
 
 NusifUNet *nusifUNetCreate(unsigned long long seed)

@@ -124,6 +124,10 @@ SIGNATURES = [
     ("nusifUNetTrainStep", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                      C.c_int, C.c_int, C.c_float, C.c_int,
                                      C.POINTER(C.c_float)]),
+    ("nusifSolverSetGuessNet", C.c_int, [C.POINTER(Solver), C.c_void_p]),
+    ("nusifSolverRecordPair", C.c_int, [C.POINTER(Solver), C.c_void_p, C.c_void_p]),
+    ("nusifSolverGuessStats", C.c_int, [C.POINTER(Solver), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 ]
 
 _lib = None

@@ -105,6 +105,25 @@ class Simulation:
     def normalize_pressure(self): self._call("normalizePressure")
     def adapt_uv(self): self._call("adaptUV")
 
+    def set_guess_net(self, net) -> None:
+        """Warm-start every later solve with the network (None: plain warm start)."""
+        self.lib.nusifSolverSetGuessNet(C.byref(self.s), net.handle if net is not None else None)
+        abi.check(self.lib)
+
+    def record_pair(self, x, t) -> None:
+        """The next solve writes its features into x and its target into t
+        (float32 CUDA tensors [kmax/2][jmax/2][imax/2][2] and [..])."""
+        self.lib.nusifSolverRecordPair(C.byref(self.s), C.c_void_p(x.data_ptr()),
+                                       C.c_void_p(t.data_ptr()))
+        abi.check(self.lib)
+
+    def guess_stats(self) -> tuple[bool, float, float]:
+        """(guess taken, relative residual of the plain warm start, of the guess)."""
+        used, rw, rg = C.c_int(), C.c_double(), C.c_double()
+        self.lib.nusifSolverGuessStats(C.byref(self.s), C.byref(used), C.byref(rw), C.byref(rg))
+        abi.check(self.lib)
+        return bool(used.value), rw.value, rg.value
+
     def solve(self) -> float:
         res = self.lib.solve(C.byref(self.s), self.d.p, self.d.rhs)
         abi.check(self.lib)

@@ -247,6 +247,23 @@ NUSIF_API int nusifUNetForward(NusifUNet *net, const float *x, int B, int Z, int
  * NULL (no synchronisation). */
 NUSIF_API int nusifUNetTrainStep(NusifUNet *net, const float *x, const float *target, int B, int Z,
     int Y, int X, float lr, int update, float *loss_host);
+/* Warm start of an mg / mg-mixed solver (grid edges multiples of 8). Each
+ * solve then computes, on the half-resolution grid, the features of its warm
+ * start p0 (restricted residual and restricted mean-free rhs, each over its
+ * RMS), runs the network, forms p1 = p0 + trilinear(net * sigma / kappa),
+ * kappa = pi^2 (1/Lx^2 + 1/Ly^2 + 1/Lz^2) for the domain lengths L,
+ * and keeps p1 only if its restricted residual ||R(b - A p1)|| (R the 8-cell
+ * mean, so the smooth error the V-cycles pay for) is below p0's; the V-cycles then run to
+ * the same rtol. net = NULL detaches (the network is borrowed, not owned). */
+NUSIF_API int nusifSolverSetGuessNet(Solver *s, NusifUNet *net);
+/* The next solve of s also writes its training pair to device buffers:
+ * x [kmax/2][jmax/2][imax/2][2] features of its warm start and, after it
+ * converged, t [kmax/2][jmax/2][imax/2] = restricted (p* - p0) * kappa / sigma. */
+NUSIF_API int nusifSolverRecordPair(Solver *s, float *x, float *t);
+/* last solve with a network: whether its guess was taken, and the relative
+ * restricted residuals ||R(b - A p)|| / ||R b|| (b mean-free) of the plain
+ * warm start and of the guess (the decision criterion) */
+NUSIF_API int nusifSolverGuessStats(Solver *s, int *used, double *rel_warm, double *rel_guess);
 
 #ifdef __cplusplus
 }

@@ -254,12 +254,16 @@ def features(p_warm, rhs, dx, dy, dz):
     return x.astype(np.float32), sr
 
 
-def diag(dx, dy, dz):
-    return 2.0 / dx ** 2 + 2.0 / dy ** 2 + 2.0 / dz ** 2
+def kappa(shape, dx, dy, dz):
+    """pi^2 (1/Lx^2 + 1/Ly^2 + 1/Lz^2) for the interior shape (K, J, I): the
+    scale of the Neumann operator's smallest non-zero eigenvalues."""
+    K, J, I = shape
+    return np.pi ** 2 * (1.0 / (I * dx) ** 2 + 1.0 / (J * dy) ** 2 + 1.0 / (K * dz) ** 2)
 
 
 def target(p_warm, p_conv, sigma, dx, dy, dz):
     """Training target: restricted correction p_conv - p_warm in the network's
-    units (times the operator's diagonal, over sigma)."""
+    units (times kappa, over sigma)."""
     e = p_conv[1:-1, 1:-1, 1:-1] - p_warm[1:-1, 1:-1, 1:-1]
-    return (restrict(e) * diag(dx, dy, dz) / (sigma if sigma > 0 else 1.0)).astype(np.float32)
+    k = kappa(e.shape, dx, dy, dz)
+    return (restrict(e) * k / (sigma if sigma > 0 else 1.0)).astype(np.float32)

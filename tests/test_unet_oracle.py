@@ -69,7 +69,8 @@ def test_features_and_target_definitions():
     lap = U.laplacian(p, h, h, h)
     assert np.allclose(U.restrict(b - lap) / s, x[..., 0], atol=1e-5)
     t = U.target(p, p + 1.0, s, h, h, h)
-    assert np.allclose(t, U.diag(h, h, h) / s)
+    assert np.allclose(t, U.kappa((n, n, n), h, h, h) / s)
+    assert U.kappa((n, n, n), h, h, h) == pytest.approx(3 * np.pi ** 2)
 
 
 def test_adam_step():
