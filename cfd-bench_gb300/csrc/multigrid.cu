@@ -49,6 +49,8 @@ struct MgState {
   int done;          // the solve is finished: every kernel returns at once
   int inner_done;    // mg-mixed: this outer iteration's correction is good enough
   int loops;         // units run by a graph while-loop (its independent stop)
+  int inner_it;      // mg-mixed: FP32 V-cycles of the current correction (graph inner loop)
+  int pad;
 };
 
 // what the fold of a fine-level restriction decides
@@ -92,6 +94,11 @@ struct MgHierarchy {
   int guess = 0;        // 1: start from 2 p(n-1) - p(n-2)
   double *p_prev = nullptr;  // padded copy of the previous solve's result (guess 1)
   bool have_prev = false;
+  // the solve as one CUDA graph (head, while-loops, tail) for fixed p / rhs
+  cudaGraphExec_t graph = nullptr;
+  const double *graph_p = nullptr, *graph_rhs = nullptr;
+  cudaStream_t cap[3] = {};  // capture streams: graph, outer body, inner body
+  bool use_graph = true;     // mg_graph: the host-driven solve runs as one graph
   double *h_ptrs[2 * kMaxLevels] = {};  // exposed through Solver::r / Solver::e
 };
 
@@ -274,9 +281,11 @@ __global__ void __launch_bounds__(kNT) k_mg_restrict(View<T> f, T *bc, int cnx, 
 // its FP64 norm folded by the last block: the mixed-precision stop test. It
 // also opens the next correction (inner_done = 0). count_cycles: one FP32
 // V-cycle per outer iteration is counted here (single-level grids, where no
-// fine restriction counts them).
+// fine restriction counts them). e_zero (may be null): the FP32 correction,
+// set to zero for the V-cycles that follow (the graph's inner loop, whose
+// V-cycles all start from the current correction).
 __global__ void __launch_bounds__(kNT) k_mx_residual(View<double> f, float *r32, MgState *st,
-    double *partials, unsigned *ticket, int count_cycles)
+    double *partials, unsigned *ticket, int count_cycles, float *e_zero)
 {
   if (solve_finished(st)) return;
   const int64_t n = (int64_t)f.nx * f.ny * f.nz;
@@ -291,6 +300,7 @@ __global__ void __launch_bounds__(kNT) k_mx_residual(View<double> f, float *r32,
     const int64_t c = f.off + (int64_t)k * f.sz + (int64_t)j * f.sy + i;
     const double r = (f.b[c] - sh) - lap_at(f, f.x, i, j, k, c, f.x[c]);
     r32[q] = (float)r;
+    if (e_zero) e_zero[q] = 0.0f;
     acc += r * r;
   }
   __shared__ double sm[kNT / 32];
@@ -310,6 +320,7 @@ __global__ void __launch_bounds__(kNT) k_mx_residual(View<double> f, float *r32,
     if (!st->done) {
       st->outer = m + 1;
       st->inner_done = 0;
+      st->inner_it = 0;
       if (count_cycles) st->cycles += 1;
     }
     *ticket = 0;
@@ -363,31 +374,27 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong(View<T> f, const T *xc, int 
 // One whole red-black Gauss-Seidel sweep in one kernel, exact: reads x_old,
 // writes x_new (ping-pong), so no block ever reads a value another block
 // writes. A block owns a 64 x 8 tile of (i, j) columns and a chunk of planes;
-// per plane it relaxes the odd ("red") cells on the tile plus a one-cell ring
-// (from old even values: exactly what the first pass of a two-pass sweep
-// computes there), then the even cells of the previous plane on the tile
-// (from the new odd values and their own old value), and writes both colours
-// of that plane. Planes walk with a one-plane lag (odd at k, even at k-1); the
-// odd planes just outside the chunk are recomputed, so chunks are
-// independent. x_old (tile + two-cell ring) and b (tile + one-cell ring) are
-// staged in shared memory by asynchronous copies issued one plane ahead
-// (cp.async, completed by cp.async.wait_group), so global latency overlaps
-// the arithmetic of the plane before. One sweep reads x and b once and
-// writes x once. ZERO: x_old is zero (not read).
+// per plane it relaxes the first-colour cells ((i + j + k) even, 0-based) on
+// the tile plus a one-cell ring (from old second-colour values: exactly what
+// the first pass of a two-pass sweep computes there), then the second-colour
+// cells of the previous plane on the tile (from the new first-colour values
+// and their own old value), and writes both colours of that plane. Planes
+// walk with a one-plane lag; the first-colour planes just outside the chunk
+// are recomputed, so chunks are independent.
+//
+// Shared memory holds every staged row split by parity (the cells at even x,
+// then the cells at odd x), so that one colour and all its neighbours are read
+// at unit stride: no bank conflicts. x_old (tile + two-cell ring) and b (tile
+// + one-cell ring) are loaded as 16-byte chunks into registers one plane
+// ahead and de-interleaved into shared memory after the plane's arithmetic,
+// so global latency overlaps that arithmetic. One sweep reads x and b once
+// and writes x once. ZERO: x_old is zero (not read).
 constexpr int kSX = 64, kSY = 8;  // tile (cells)
 constexpr int kWX = kSX + 8;      // staged row: tile + 4 cells each side (16-byte chunks)
+constexpr int kHX = kWX / 2;      // cells of one parity in a staged row (36)
 constexpr int kRY = kSY + 4;      // staged x_old rows: tile + 2-row ring
-constexpr int kBYr = kSY + 2;     // staged b rows and odd values: tile + 1-row ring
-constexpr int kQX = kSX + 2;      // odd values: tile + 1-cell ring
-
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
-{
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+constexpr int kBYr = kSY + 2;     // staged b rows and first-colour values: tile + 1-row ring
+constexpr int kRedRow = kSX / 2 + 1;  // first-colour cells per row on tile + ring (33)
 
 // FP32 levels with nx % 4 == 0 (rows start on 16-byte boundaries): every
 // staged row is 18 chunks of four cells starting 4 cells left of the tile,
@@ -398,9 +405,10 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
     int kc, const MgState *st)
 {
   if (mg_done(st)) return;
-  __shared__ __align__(16) float xo[4][kRY][kWX];   // x_old planes, slot = plane & 3
-  __shared__ __align__(16) float bs[3][kBYr][kWX];  // b planes, slot = plane % 3
-  __shared__ float xr[3][kBYr][kQX];                // new odd values, slot = plane % 3
+  // [slot][row][parity][x / 2]
+  __shared__ __align__(16) float xo[4][kRY][2][kHX];   // x_old planes, slot = plane & 3
+  __shared__ __align__(16) float bs[3][kBYr][2][kHX];  // b planes, slot = plane % 3
+  __shared__ float xr[3][kBYr][kHX];                   // new first-colour values, slot = plane % 3
   const float *__restrict__ xold = v.x;
   const float *__restrict__ b = v.b;
   const int nx = v.nx, ny = v.ny, nz = v.nz;
@@ -414,78 +422,90 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
   const bool x_lane = cr < kRY, b_lane = cr < kBYr;
   const int gjx = min(max(j0 - 2 + cr, 0), ny - 1), gjb = min(max(j0 - 1 + cr, 0), ny - 1);
   const int64_t xoff = (int64_t)gjx * v.sy + gic, boff = (int64_t)gjb * v.sy + gic;
-  auto stage = [&](int kx, int kb) {
+  float4 px = make_float4(0.f, 0.f, 0.f, 0.f), pb = px;  // prefetched chunks
+  auto fetch = [&](int kx, int kb) {
     if (!ZERO && x_lane && kx >= 0 && kx < nz)
-      cp_async16(&xo[kx & 3][cr][4 * cc], xold + (int64_t)kx * v.sz + xoff);
+      px = __ldg(reinterpret_cast<const float4 *>(xold + (int64_t)kx * v.sz + xoff));
     if (b_lane && kb >= 0 && kb < nz)
-      cp_async16(&bs[kb % 3][cr][4 * cc], b + (int64_t)kb * v.sz + boff);
+      pb = __ldg(reinterpret_cast<const float4 *>(b + (int64_t)kb * v.sz + boff));
+  };
+  auto place = [&](int kx, int kb) {  // de-interleave into the split rows
+    if (!ZERO && x_lane && kx >= 0 && kx < nz) {
+      *reinterpret_cast<float2 *>(&xo[kx & 3][cr][0][2 * cc]) = make_float2(px.x, px.z);
+      *reinterpret_cast<float2 *>(&xo[kx & 3][cr][1][2 * cc]) = make_float2(px.y, px.w);
+    }
+    if (b_lane && kb >= 0 && kb < nz) {
+      *reinterpret_cast<float2 *>(&bs[kb % 3][cr][0][2 * cc]) = make_float2(pb.x, pb.z);
+      *reinterpret_cast<float2 *>(&bs[kb % 3][cr][1][2 * cc]) = make_float2(pb.y, pb.w);
+    }
   };
   if (ZERO) {
-    for (int q = tid; q < 4 * kRY * kWX; q += 256) (&xo[0][0][0])[q] = 0.0f;
+    for (int q = tid; q < 4 * kRY * 2 * kHX; q += 256) (&xo[0][0][0][0])[q] = 0.0f;
   }
-  stage(k0 - 2, -1);
-  stage(k0 - 1, k0 - 1);
-  stage(k0, -1);
-  cp_async_commit();
-  constexpr int kOdd = (kQX / 2) * kBYr;  // odd cells per plane on tile + ring (330)
+  fetch(k0 - 2, -1);
+  place(k0 - 2, -1);
+  fetch(k0 - 1, k0 - 1);
+  place(k0 - 1, k0 - 1);
+  fetch(k0, -1);
+  place(k0, -1);
+  constexpr int kRed = kRedRow * kBYr;  // first-colour cells per plane on tile + ring (330)
   for (int k = k0 - 1; k <= k1; k++) {
-    stage(k + 2, k + 1);  // prefetch: completes during this plane's arithmetic
-    cp_async_commit();
-    cp_async_wait<1>();   // all but the prefetch: x_old(k+1), b(k) are in
+    fetch(k + 2, k + 1);  // lands in registers during this plane's arithmetic
     __syncthreads();
     if (k >= 0 && k < nz) {
-      float(*rq)[kQX] = xr[k % 3];
-      const float(*xk)[kWX] = xo[k & 3];
-      const float(*xkm)[kWX] = xo[(k + 3) & 3];
-      const float(*xkp)[kWX] = xo[(k + 1) & 3];
-      const float(*bk)[kWX] = bs[k % 3];
-      for (int q = tid; q < kOdd; q += 256) {
-        const int lj = q / (kQX / 2), pi = q - lj * (kQX / 2);
+      float(*rq)[kHX] = xr[k % 3];
+      const float(*xk)[2][kHX] = xo[k & 3];
+      const float(*xkm)[2][kHX] = xo[(k + 3) & 3];
+      const float(*xkp)[2][kHX] = xo[(k + 1) & 3];
+      const float(*bk)[2][kHX] = bs[k % 3];
+      for (int q = tid; q < kRed; q += 256) {
+        const int lj = q / kRedRow, m = q - lj * kRedRow;
         const int gj = j0 - 1 + lj;
-        const int li = 2 * pi + ((i0 + gj + k) & 1 ? 0 : 1);  // odd cell column
-        const int gi = i0 - 1 + li;
+        const int p = (gj + k) & 1;        // parity of x of this row's first-colour cells
+        const int h = (p ? 1 : 2) + m;     // staged x = 2h + p, tile x - 1 .. tile x + 64
+        const int gi = i0 - 4 + 2 * h + p;
         if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
-        const int si = li + 3, sj = lj + 1;  // staged x_old column / row
-        const float xc = xk[sj][si];
-        const float sx = (gi > 0 ? xk[sj][si - 1] : xc) + (gi < nx - 1 ? xk[sj][si + 1] : xc);
-        const float sy = (gj > 0 ? xk[sj - 1][si] : xc) + (gj < ny - 1 ? xk[sj + 1][si] : xc);
-        const float sz = (k > 0 ? xkm[sj][si] : xc) + (k < nz - 1 ? xkp[sj][si] : xc);
+        const int sj = lj + 1;  // staged x_old row
+        const float xc = xk[sj][p][h];
+        const float sx = (gi > 0 ? xk[sj][1 - p][h - 1 + p] : xc) +
+                         (gi < nx - 1 ? xk[sj][1 - p][h + p] : xc);
+        const float sy = (gj > 0 ? xk[sj - 1][p][h] : xc) + (gj < ny - 1 ? xk[sj + 1][p][h] : xc);
+        const float sz = (k > 0 ? xkm[sj][p][h] : xc) + (k < nz - 1 ? xkp[sj][p][h] : xc);
         const float lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
-        rq[lj][li] = xc - (bk[lj][li + 3] - lap) * v.inv_diag;
+        rq[lj][h] = xc - (bk[lj][p][h] - lap) * v.inv_diag;
       }
     }
     __syncthreads();
-    // even cells of plane k-1 on the tile: one cell pair per thread, both
-    // cells stored as one 8-byte vector
+    // second-colour cells of plane k-1 on the tile: one per thread, stored
+    // with its first-colour neighbour in the same aligned pair as 8 bytes
     const int ke = k - 1;
     if (ke >= k0 && ke < k1) {
-      const float(*rm)[kQX] = xr[(ke + 2) % 3];
-      const float(*r0)[kQX] = xr[ke % 3];
-      const float(*rp)[kQX] = xr[(ke + 1) % 3];
-      const float(*xe)[kWX] = xo[ke & 3];
-      const float(*be)[kWX] = bs[ke % 3];
-      const int tj = tid >> 5, pi = tid & 31;
+      const float(*rm)[kHX] = xr[(ke + 2) % 3];
+      const float(*r0)[kHX] = xr[ke % 3];
+      const float(*rp)[kHX] = xr[(ke + 1) % 3];
+      const float(*xe)[2][kHX] = xo[ke & 3];
+      const float(*be)[2][kHX] = bs[ke % 3];
+      const int tj = tid >> 5, h = 2 + (tid & 31);
       const int gj = j0 + tj;
-      const int e = (i0 + gj + ke + 1) & 1;  // position of the even cell in the pair
-      const int te = 2 * pi + e;
-      const int gi = i0 + te;
-      if (gj < ny && i0 + 2 * pi < nx) {
-        const int li = te + 1, lj = tj + 1;
-        const float xc = xe[lj + 1][te + 4];
-        const float sx = (gi > 0 ? r0[lj][li - 1] : xc) + (gi < nx - 1 ? r0[lj][li + 1] : xc);
-        const float sy = (gj > 0 ? r0[lj - 1][li] : xc) + (gj < ny - 1 ? r0[lj + 1][li] : xc);
-        const float sz = (ke > 0 ? rm[lj][li] : xc) + (ke < nz - 1 ? rp[lj][li] : xc);
+      const int pe = (gj + ke + 1) & 1;  // parity of x of this row's second-colour cells
+      const int gi = i0 - 4 + 2 * h + pe;
+      const int gpair = i0 - 4 + 2 * h;
+      if (gj < ny && gpair < nx) {
+        const int lj = tj + 1;  // first-colour / b row
+        const float xc = xe[lj + 1][pe][h];
+        const float left = r0[lj][h - 1 + pe], right = r0[lj][h + pe];
+        const float sx = (gi > 0 ? left : xc) + (gi < nx - 1 ? right : xc);
+        const float sy = (gj > 0 ? r0[lj - 1][h] : xc) + (gj < ny - 1 ? r0[lj + 1][h] : xc);
+        const float sz = (ke > 0 ? rm[lj][h] : xc) + (ke < nz - 1 ? rp[lj][h] : xc);
         const float lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
-        const float even = xc - (be[lj][te + 4] - lap) * v.inv_diag;
-        const float odd = r0[lj][(te ^ 1) + 1];
-        const float2 pair = e ? make_float2(odd, even) : make_float2(even, odd);
-        *reinterpret_cast<float2 *>(xnew + (int64_t)ke * v.sz + (int64_t)gj * v.sy + i0 + 2 * pi) =
-            pair;
+        const float second = xc - (be[lj][pe][h] - lap) * v.inv_diag;
+        const float first = r0[lj][h];
+        const float2 pair = pe ? make_float2(first, second) : make_float2(second, first);
+        *reinterpret_cast<float2 *>(xnew + (int64_t)ke * v.sz + (int64_t)gj * v.sy + gpair) = pair;
       }
     }
-    __syncthreads();
+    place(k + 2, k + 1);  // slots no thread reads in this iteration
   }
-  cp_async_wait<0>();
 }
 
 // x_f += trilinear interpolation of x_c when x was coarsened (rx == 2): one
@@ -1032,7 +1052,7 @@ bool cycle_mixed(MgHierarchy *H, double *p, const double *rhs)
   View<double> v0 = padded_view(H->lv[0], p, rhs);
   const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
   k_mx_residual<<<flat_blocks(n0), kNT, 0, stream()>>>(v0, H->b32[0], st, H->red.partials,
-      H->red.ticket, H->nl == 1 ? 1 : 0);
+      H->red.ticket, H->nl == 1 ? 1 : 0, nullptr);
   if (!launched("k_mx_residual")) return false;
   const int inner = H->nl == 1 ? 1 : H->inner;
   for (int q = 0; q < inner; q++)
@@ -1056,6 +1076,10 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
   H->maxcycles = x.mg_maxcycles;
   H->inner = x.mg_inner < 1 ? 1 : x.mg_inner;
   H->guess = x.mg_guess == 1 ? 1 : 0;
+  H->use_graph = x.mg_graph != 0;
+  for (cudaStream_t &c : H->cap)
+    if (!cuda_ok(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking), "mg capture stream"))
+      return false;
   if (H->guess == 1) {
     const size_t padded =
         (size_t)(d->grid.imax + 2) * (d->grid.jmax + 2) * (d->grid.kmax + 2) * sizeof(double);
@@ -1156,6 +1180,21 @@ __global__ void k_mg_continue(MgState *st, cudaGraphConditionalHandle h, int cap
   cudaGraphSetConditional(h, (st->done == 0 && n < cap) ? 1u : 0u);
 }
 
+// before the inner loop of one refinement step: enter it while the solve is open
+__global__ void k_inner_open(const MgState *st, cudaGraphConditionalHandle h)
+{
+  cudaGraphSetConditional(h, st->done == 0 ? 1u : 0u);
+}
+
+// end of one FP32 V-cycle of the inner loop: another while the correction is
+// not yet good enough and fewer than `inner` V-cycles ran
+__global__ void k_inner_continue(MgState *st, cudaGraphConditionalHandle h, int inner)
+{
+  const int n = st->inner_it + 1;
+  st->inner_it = n;
+  cudaGraphSetConditional(h, (st->done == 0 && st->inner_done == 0 && n < inner) ? 1u : 0u);
+}
+
 bool enqueue_solve_head(MgHierarchy *H, const View<double> &v0)
 {
   k_mg_state_init<<<1, 1, 0, stream()>>>(H->d_state, H->rtol * H->rtol, H->maxcycles);
@@ -1174,6 +1213,134 @@ bool enqueue_solve_tail(MgHierarchy *H, const View<double> &v0, double *p, int *
   if (!launch_pressure_ghosts(make_dims(v0.nx, v0.ny, v0.nz), p)) return false;
   k_mg_count_unconverged<<<1, 1, 0, stream()>>>(H->d_state, unconverged, last_cycles);
   return launched("k_mg_count_unconverged");
+}
+
+// a conditional handle of the graph being captured on s
+bool make_handle(cudaStream_t s, unsigned dflt, unsigned flags, cudaGraphConditionalHandle *h)
+{
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t graph = nullptr;
+  if (!cuda_ok(cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, nullptr, nullptr, nullptr),
+          "capture info"))
+    return false;
+  if (cs != cudaStreamCaptureStatusActive) {
+    fail(NUSIF_ERR_STATE, "multigrid graph: no stream capture in progress");
+    return false;
+  }
+  return cuda_ok(cudaGraphConditionalHandleCreate(h, graph, dflt, flags), "conditional handle");
+}
+
+// A while node with handle h appended to the graph being captured on s (after
+// everything captured so far); its body is whatever `fill` launches, captured
+// on `body` with the library stream set to `body`.
+template <typename F>
+bool capture_while(cudaStream_t s, cudaStream_t body, cudaGraphConditionalHandle h, F &&fill)
+{
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t graph = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  const cudaGraphEdgeData *edges = nullptr;
+  size_t ndeps = 0;
+  if (!cuda_ok(cudaStreamGetCaptureInfo(s, &cs, nullptr, &graph, &deps, &edges, &ndeps),
+          "capture info"))
+    return false;
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (!cuda_ok(cudaGraphAddNode(&node, graph, deps, edges, ndeps, &cp), "while node")) return false;
+  if (!cuda_ok(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1,
+                   cudaStreamSetCaptureDependencies),
+          "capture dependencies"))
+    return false;
+  cudaGraph_t loop = cp.conditional.phGraph_out[0];
+  if (!cuda_ok(cudaStreamBeginCaptureToGraph(body, loop, nullptr, nullptr, 0,
+                   cudaStreamCaptureModeThreadLocal),
+          "loop body capture"))
+    return false;
+  nusifSetStream(body);
+  const bool ok = fill();
+  nusifSetStream(s);
+  const bool ended = cuda_ok(cudaStreamEndCapture(body, &loop), "loop body end");
+  return ok && ended;
+}
+
+// One refinement step for a graph: FP64 residual (zeroing the correction),
+// an inner while-loop of FP32 V-cycles that ends as soon as the correction
+// meets its target (no V-cycle is launched past that point), p += e.
+bool cycle_mixed_nested(MgHierarchy *H, double *p, const double *rhs, cudaStream_t inner_body)
+{
+  MgState *st = H->d_state;
+  View<double> v0 = padded_view(H->lv[0], p, rhs);
+  const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
+  k_mx_residual<<<flat_blocks(n0), kNT, 0, stream()>>>(v0, H->b32[0], st, H->red.partials,
+      H->red.ticket, 0, H->x32[0]);
+  if (!launched("k_mx_residual")) return false;
+  cudaStream_t s = stream();
+  cudaGraphConditionalHandle h;
+  if (!make_handle(s, 0, 0, &h)) return false;
+  k_inner_open<<<1, 1, 0, s>>>(st, h);
+  if (!launched("k_inner_open")) return false;
+  const int inner = H->inner;
+  if (!capture_while(s, inner_body, h, [&] {
+        if (!vcycle<float>(H, 0, H->x32, H->b32, false, true)) return false;
+        k_inner_continue<<<1, 1, 0, stream()>>>(st, h, inner);
+        return launched("k_inner_continue");
+      }))
+    return false;
+  View<float> e = compact_view<float>(H->lv[0], H->x32[0], H->b32[0]);
+  k_mx_fold<<<flat_blocks(n0), kNT, 0, stream()>>>(e, p, v0.sy, v0.sz, st);
+  return launched("k_mx_fold");
+}
+
+// The solve's units as a while-loop of the graph captured on the library
+// stream: one unit per iteration (an FP64 V-cycle, or one refinement step
+// with its own inner loop), ended by the device once the solve is done, or
+// after mg_cycles + 2 units whatever the device flags say (the solve itself
+// sets done by mg_cycles units).
+bool enqueue_units_loop(MgHierarchy *H, double *p, const double *rhs, cudaStream_t outer_body,
+    cudaStream_t inner_body)
+{
+  cudaStream_t s = stream();
+  cudaGraphConditionalHandle h;
+  if (!make_handle(s, 1, cudaGraphCondAssignDefault, &h)) return false;
+  return capture_while(s, outer_body, h, [&] {
+    bool ok;
+    if (H->mode == 0) ok = cycle_fp64(H, p, rhs);
+    else if (H->nl == 1) ok = cycle_mixed(H, p, rhs);
+    else ok = cycle_mixed_nested(H, p, rhs, inner_body);
+    if (!ok) return false;
+    k_mg_continue<<<1, 1, 0, stream()>>>(H->d_state, h, H->maxcycles + 2);
+    return launched("k_mg_continue");
+  });
+}
+
+// the whole solve (head, units loop, pressure ghosts) as one graph for p, rhs
+bool build_solve_graph(MgHierarchy *H, double *p, const double *rhs)
+{
+  if (H->graph) {
+    cudaGraphExecDestroy(H->graph);
+    H->graph = nullptr;
+  }
+  cudaStream_t lib = stream();
+  cudaGraph_t g = nullptr;
+  if (!cuda_ok(cudaStreamBeginCapture(H->cap[0], cudaStreamCaptureModeThreadLocal), "capture"))
+    return false;
+  nusifSetStream(H->cap[0]);
+  View<double> v0 = padded_view(H->lv[0], p, rhs);
+  bool ok = enqueue_solve_head(H, v0) && enqueue_units_loop(H, p, rhs, H->cap[1], H->cap[2]) &&
+            launch_pressure_ghosts(make_dims(v0.nx, v0.ny, v0.nz), p);
+  nusifSetStream(lib);
+  const bool ended = cuda_ok(cudaStreamEndCapture(H->cap[0], &g), "capture end");
+  ok = ok && ended && cuda_ok(cudaGraphInstantiate(&H->graph, g, 0), "solve graph");
+  if (g) cudaGraphDestroy(g);
+  if (ok) {
+    H->graph_p = p;
+    H->graph_rhs = rhs;
+  }
+  return ok;
 }
 
 }  // namespace
@@ -1198,12 +1365,10 @@ bool mg_enqueue(SolverState *ss, double *p, const double *rhs, int queue, int *u
   return enqueue_solve_tail(H, v0, p, unconverged, last_cycles);
 }
 
-// The same solve with its units in a CUDA graph while-loop, so that a step
-// runs exactly as many units as the host-driven solve: the loop body (one
-// unit and k_mg_continue) is captured on `body` into the conditional node's
-// graph, and the node joins the capture running on the library stream. The
-// loop ends when the solve is done, or after mg_cycles + 2 units whatever the
-// device flags say (the solve itself sets done by mg_cycles units).
+// The same solve with its units in graph while-loops (mg_solve's graph), so
+// that a step runs exactly the units of the host-driven solve; `body`
+// captures the outer loop's body. Needs a capture in progress on the library
+// stream.
 bool mg_enqueue_loop(SolverState *ss, double *p, const double *rhs, cudaStream_t body,
     int *unconverged, int *last_cycles)
 {
@@ -1213,59 +1378,17 @@ bool mg_enqueue_loop(SolverState *ss, double *p, const double *rhs, cudaStream_t
     return false;
   }
   View<double> v0 = padded_view(H->lv[0], p, rhs);
-  if (!enqueue_solve_head(H, v0)) return false;
-  cudaStream_t outer = stream();
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  cudaGraph_t graph = nullptr;
-  const cudaGraphNode_t *deps = nullptr;
-  const cudaGraphEdgeData *edges = nullptr;
-  size_t ndeps = 0;
-  if (!cuda_ok(cudaStreamGetCaptureInfo(outer, &cs, nullptr, &graph, &deps, &edges, &ndeps),
-          "capture info"))
-    return false;
-  if (cs != cudaStreamCaptureStatusActive) {
-    fail(NUSIF_ERR_STATE, "mg_enqueue_loop needs a stream capture in progress");
-    return false;
-  }
-  cudaGraphConditionalHandle handle;
-  if (!cuda_ok(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault),
-          "conditional handle"))
-    return false;
-  cudaGraphNodeParams cp = {};
-  cp.type = cudaGraphNodeTypeConditional;
-  cp.conditional.handle = handle;
-  cp.conditional.type = cudaGraphCondTypeWhile;
-  cp.conditional.size = 1;
-  cudaGraphNode_t node;
-  if (!cuda_ok(cudaGraphAddNode(&node, graph, deps, edges, ndeps, &cp), "while node")) return false;
-  if (!cuda_ok(cudaStreamUpdateCaptureDependencies(outer, &node, nullptr, 1,
-                   cudaStreamSetCaptureDependencies),
-          "capture dependencies"))
-    return false;
-  cudaGraph_t loop = cp.conditional.phGraph_out[0];
-  if (!cuda_ok(cudaStreamBeginCaptureToGraph(body, loop, nullptr, nullptr, 0,
-                   cudaStreamCaptureModeThreadLocal),
-          "loop body capture"))
-    return false;
-  nusifSetStream(body);
-  bool ok = H->mode == 0 ? cycle_fp64(H, p, rhs) : cycle_mixed(H, p, rhs);
-  if (ok) {
-    k_mg_continue<<<1, 1, 0, stream()>>>(H->d_state, handle, H->maxcycles + 2);
-    ok = launched("k_mg_continue");
-  }
-  nusifSetStream(outer);
-  const bool ended = cuda_ok(cudaStreamEndCapture(body, &loop), "loop body end");
-  if (!ok || !ended) return false;
-  return enqueue_solve_tail(H, v0, p, unconverged, last_cycles);
+  return enqueue_solve_head(H, v0) && enqueue_units_loop(H, p, rhs, body, H->cap[2]) &&
+         enqueue_solve_tail(H, v0, p, unconverged, last_cycles);
 }
 
 // FP32 sweeps swap buffers on the host; a captured sequence must end with the
-// same buffer current as it started, so it needs an even number of sweeps per
-// level in every V-cycle (the default V(2,2) has)
+// same buffer current as it started, so every level needs an even number of
+// sweeps per V-cycle (pre + post even)
 bool mg_capture_ok(const SolverState *ss)
 {
   const MgHierarchy *H = ss->mg;
-  return H && (H->mode == 0 || (H->pre % 2 == 0 && H->post % 2 == 0));
+  return H && (H->mode == 0 || (H->pre + H->post) % 2 == 0);
 }
 
 double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
@@ -1276,12 +1399,6 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
     return NAN;
   }
   MgState *h = H->h_state;
-  memset(h, 0, sizeof(*h));
-  h->rtol2 = H->rtol * H->rtol;
-  h->maxcycles = H->maxcycles;
-  if (!cuda_ok(cudaMemcpyAsync(H->d_state, h, sizeof(MgState), cudaMemcpyHostToDevice, stream()),
-          "mg state upload"))
-    return NAN;
   View<double> v0 = padded_view(H->lv[0], p, rhs);
   const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
   const int blocks = flat_blocks(n0);
@@ -1299,26 +1416,46 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
   }
   // learned warm start: may replace p by the network's guess (never a worse residual)
   if (ss->guess && !guess_before_solve(ss->guess, s->grid, p, rhs)) return NAN;
-  k_mg_rhs_sum<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
-  if (!launched("k_mg_rhs_sum")) return NAN;
-  k_mg_rhs_norm<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
-  if (!launched("k_mg_rhs_norm")) return NAN;
 
-  int chunk = H->last_cycles > 0 ? H->last_cycles : 4;
-  for (;;) {
-    for (int q = 0; q < chunk; q++) {
-      const bool ok = H->mode == 0 ? cycle_fp64(H, p, rhs) : cycle_mixed(H, p, rhs);
-      if (!ok) return NAN;
-    }
-    if (!cuda_ok(cudaMemcpyAsync(h, H->d_state, sizeof(MgState), cudaMemcpyDeviceToHost,
-                     stream()),
-            "mg state download"))
+  if (H->use_graph && mg_capture_ok(ss)) {
+    // one graph launch: head, while-loops of units (and of FP32 V-cycles),
+    // pressure ghosts; captured once per (p, rhs)
+    if ((!H->graph || H->graph_p != p || H->graph_rhs != rhs) && !build_solve_graph(H, p, rhs))
       return NAN;
-    if (!cuda_ok(cudaStreamSynchronize(stream()), "mg sync")) return NAN;
-    if (h->done) break;
-    chunk = 2;
+    if (!cuda_ok(cudaGraphLaunch(H->graph, stream()), "solve graph launch") ||
+        !cuda_ok(cudaMemcpyAsync(h, H->d_state, sizeof(MgState), cudaMemcpyDeviceToHost,
+                     stream()),
+            "mg state download") ||
+        !cuda_ok(cudaStreamSynchronize(stream()), "mg sync"))
+      return NAN;
+  } else {
+    memset(h, 0, sizeof(*h));
+    h->rtol2 = H->rtol * H->rtol;
+    h->maxcycles = H->maxcycles;
+    if (!cuda_ok(cudaMemcpyAsync(H->d_state, h, sizeof(MgState), cudaMemcpyHostToDevice,
+                     stream()),
+            "mg state upload"))
+      return NAN;
+    k_mg_rhs_sum<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
+    if (!launched("k_mg_rhs_sum")) return NAN;
+    k_mg_rhs_norm<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
+    if (!launched("k_mg_rhs_norm")) return NAN;
+    int chunk = H->last_cycles > 0 ? H->last_cycles : 4;
+    for (;;) {
+      for (int q = 0; q < chunk; q++) {
+        const bool ok = H->mode == 0 ? cycle_fp64(H, p, rhs) : cycle_mixed(H, p, rhs);
+        if (!ok) return NAN;
+      }
+      if (!cuda_ok(cudaMemcpyAsync(h, H->d_state, sizeof(MgState), cudaMemcpyDeviceToHost,
+                       stream()),
+              "mg state download"))
+        return NAN;
+      if (!cuda_ok(cudaStreamSynchronize(stream()), "mg sync")) return NAN;
+      if (h->done) break;
+      chunk = 2;
+    }
+    if (!launch_pressure_ghosts(make_dims(v0.nx, v0.ny, v0.nz), p)) return NAN;
   }
-  if (!launch_pressure_ghosts(make_dims(v0.nx, v0.ny, v0.nz), p)) return NAN;
   if (ss->guess && !guess_after_solve(ss->guess, s->grid, p)) return NAN;
   // queue as many units next time: V-cycles (mg) or residual evaluations (mg-mixed)
   H->last_cycles = H->mode == 0 ? h->cycles : h->outer + 1;
@@ -1367,7 +1504,7 @@ bool mg_time_kernel(SolverState *ss, const double *p, const double *rhs, int whi
       if (q == 1) cudaEventRecord(e0, stream());
       if (which == 1 && H->mode == 1) {
         k_mx_residual<<<flat_blocks(n0), kNT, 0, stream()>>>(v0, H->b32[0], tst, H->red.partials,
-            H->red.ticket, 0);
+            H->red.ticket, 0, nullptr);
         ok = launched("k_mx_residual");
       } else if (H->mode == 1) {
         ok = fused_sweeps(H, 0, 1, false, tst);  // one whole sweep
@@ -1402,6 +1539,9 @@ void mg_free(Solver *s, SolverState *ss)
     if (H->x32b[l]) cudaFree(H->x32b[l]);
     if (H->b32[l]) cudaFree(H->b32[l]);
   }
+  if (H->graph) cudaGraphExecDestroy(H->graph);
+  for (cudaStream_t c : H->cap)
+    if (c) cudaStreamDestroy(c);
   if (H->p_prev) cudaFree(H->p_prev);
   if (H->minv64) cudaFree(H->minv64);
   if (H->minv32) cudaFree(H->minv32);
@@ -1417,3 +1557,53 @@ void mg_free(Solver *s, SolverState *ss)
 }
 
 }  // namespace nusif
+
+using namespace nusif;
+
+extern "C" {
+
+// One or more exact red-black Gauss-Seidel sweeps of the multigrid's FP32
+// smoother (the one-kernel sweep; ghost-free Neumann operator) on compact
+// device arrays x[nz][ny][nx] -> xout; first colour (i + j + k) even, 0-based.
+int nusifSmoothRBF32(const float *x, const float *b, float *xout, int nx, int ny, int nz,
+    double hx, double hy, double hz, int sweeps)
+{
+  if (!x || !b || !xout || nx < 4 || ny < 1 || nz < 1 || nx % 4 || sweeps < 1 || !(hx > 0) ||
+      !(hy > 0) || !(hz > 0)) {
+    fail(NUSIF_ERR_ARG, "nusifSmoothRBF32: needs device arrays, nx a multiple of 4, sweeps >= 1");
+    return NUSIF_ERR_ARG;
+  }
+  MgHierarchy H;
+  H.nl = 1;
+  MgLevelDesc &L = H.lv[0];
+  L.n[0] = nx;
+  L.n[1] = ny;
+  L.n[2] = nz;
+  L.r[0] = L.r[1] = L.r[2] = 1;
+  L.ih2[0] = 1.0 / (hx * hx);
+  L.ih2[1] = 1.0 / (hy * hy);
+  L.ih2[2] = 1.0 / (hz * hz);
+  const size_t n = (size_t)nx * ny * nz;
+  float *scratch = nullptr;
+  MgState *st = nullptr;
+  bool ok = cuda_ok(cudaMalloc(&scratch, 2 * n * sizeof(float)), "cudaMalloc(smooth)") &&
+            cuda_ok(cudaMalloc(&st, sizeof(MgState)), "cudaMalloc(smooth)") &&
+            cuda_ok(cudaMemsetAsync(st, 0, sizeof(MgState), stream()), "smooth state") &&
+            cuda_ok(cudaMemcpyAsync(scratch, x, n * sizeof(float), cudaMemcpyDeviceToDevice,
+                        stream()),
+                "smooth copy");
+  H.x32[0] = scratch;
+  H.x32b[0] = scratch + n;
+  H.b32[0] = const_cast<float *>(b);
+  ok = ok && fused_sweeps(&H, 0, sweeps, false, st) &&
+       cuda_ok(cudaMemcpyAsync(xout, H.x32[0], n * sizeof(float), cudaMemcpyDeviceToDevice,
+                   stream()),
+           "smooth copy") &&
+       cuda_ok(cudaStreamSynchronize(stream()), "smooth");
+  H.x32[0] = H.x32b[0] = H.b32[0] = nullptr;
+  if (scratch) cudaFree(scratch);
+  if (st) cudaFree(st);
+  return ok ? NUSIF_OK : NUSIF_ERR_CUDA;
+}
+
+}  // extern "C"

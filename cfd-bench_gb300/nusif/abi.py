@@ -124,6 +124,8 @@ SIGNATURES = [
     ("nusifUNetTrainStep", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                      C.c_int, C.c_int, C.c_float, C.c_int,
                                      C.POINTER(C.c_float)]),
+    ("nusifSmoothRBF32", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                   C.c_int, C.c_double, C.c_double, C.c_double, C.c_int]),
     ("nusifSolverSetGuessNet", C.c_int, [C.POINTER(Solver), C.c_void_p]),
     ("nusifSolverRecordPair", C.c_int, [C.POINTER(Solver), C.c_void_p, C.c_void_p]),
     ("nusifSolverGuessStats", C.c_int, [C.POINTER(Solver), C.POINTER(C.c_int),

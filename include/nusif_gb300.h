@@ -221,6 +221,13 @@ NUSIF_API int nusifTimeKernel(Solver *s, const double *p, const double *rhs, int
     double *ms_out);
 /* library version string */
 NUSIF_API const char *nusifVersion(void);
+/* `sweeps` exact red-black Gauss-Seidel sweeps of the mixed-precision
+ * multigrid's FP32 smoother (one kernel per sweep) on compact device arrays
+ * x, b [nz][ny][nx] (nx a multiple of 4) -> xout: ghost-free Neumann
+ * operator with spacings hx, hy, hz; first colour (i + j + k) even, 0-based.
+ * No reference counterpart (the smoother of the corrected multigrid). */
+NUSIF_API int nusifSmoothRBF32(const float *x, const float *b, float *xout, int nx, int ny, int nz,
+    double hx, double hy, double hz, int sweeps);
 
 /* Learned pressure warm start (no reference counterpart). A 3-level 3D U-Net
  * (16/32/64 channels, 243,473 parameters; BF16 weights and activations, FP32

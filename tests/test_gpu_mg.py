@@ -145,3 +145,66 @@ def test_mg_extrapolated_guess(nusif_lib, solver):
     assert cycles["extrapolate"] < cycles["previous"]
     for f in "uvw":
         assert rel_err(fields["extrapolate"][f], fields["previous"][f]) < 1e-5, f
+
+
+def _rb_sweep_f32(x, b, h):
+    """Two-pass red-black Gauss-Seidel (first colour (i+j+k) even, 0-based),
+    ghost-free Neumann operator, float32 with float64 sums (numpy)."""
+    x = x.astype(np.float32).copy()
+    ex, ey, ez = (np.float32(1.0 / (s * s)) for s in h)
+    diag = np.float32(2.0 * (1.0 / h[0] ** 2 + 1.0 / h[1] ** 2 + 1.0 / h[2] ** 2))
+    k, j, i = np.meshgrid(*[np.arange(n) for n in x.shape], indexing="ij")
+    for colour in (0, 1):
+        xp = np.pad(x, 1, mode="edge")
+        c = xp[1:-1, 1:-1, 1:-1]
+        lap = (ex * (xp[1:-1, 1:-1, :-2] + xp[1:-1, 1:-1, 2:]) + ey * (xp[1:-1, :-2, 1:-1] +
+               xp[1:-1, 2:, 1:-1]) + ez * (xp[:-2, 1:-1, 1:-1] + xp[2:, 1:-1, 1:-1]) - diag * c)
+        new = c - (b - lap) / diag
+        m = ((i + j + k) & 1) == colour
+        x[m] = new[m]
+    return x
+
+
+@pytest.mark.parametrize("dims", [(64, 16, 8), (128, 24, 40), (20, 12, 16), (36, 9, 70), (4, 3, 5)])
+def test_fp32_one_kernel_sweep_is_exact_red_black(nusif_lib, dims):
+    """The one-kernel FP32 sweep equals two red-black passes (to FP32 rounding:
+    contraction and summation order), on ragged tiles and chunk edges."""
+    import ctypes as C
+
+    import torch
+    nx, ny, nz = dims
+    rng = np.random.default_rng(31)
+    x = rng.standard_normal((nz, ny, nx)).astype(np.float32)
+    b = rng.standard_normal((nz, ny, nx)).astype(np.float32)
+    h = (1.0 / nx, 0.8 / ny, 1.2 / nz)
+    want = x
+    for s in (1, 2, 3):
+        want = _rb_sweep_f32(want, b, h)
+        xd, bd = torch.from_numpy(x).cuda(), torch.from_numpy(b).cuda()
+        out = torch.empty_like(xd)
+        rc = nusif_lib.nusifSmoothRBF32(C.c_void_p(xd.data_ptr()), C.c_void_p(bd.data_ptr()),
+                                        C.c_void_p(out.data_ptr()), nx, ny, nz, *h, s)
+        assert rc == 0
+        got = out.cpu().numpy()
+        scale = np.abs(want).max()
+        assert np.max(np.abs(got - want)) <= 2e-5 * scale, (s, np.max(np.abs(got - want)) / scale)
+
+
+@pytest.mark.parametrize("solver,pre,post", [("mg", 2, 2), ("mg-mixed", 2, 2), ("mg-mixed", 3, 3),
+                                             ("mg-mixed", 3, 1), ("mg-mixed", 2, 1)])
+def test_graph_solve_matches_host_driven_solve(nusif_lib, solver, pre, post):
+    """The solve as one CUDA graph (while-loops over units and over FP32
+    V-cycles) is the host-driven solve launch for launch: same V-cycles, same
+    fields bit for bit. (2, 1) has an odd sweep count per level and keeps
+    the host-driven path in both runs.)"""
+    from nusif import Simulation
+    from nusif.params import cavity
+    base = cavity((32, 24, 16), re=900.0, te=1e9, solver=solver, rtol=1e-7, mg_pre=pre,
+                  mg_post=post, mg_guess="extrapolate")
+    with Simulation(dict(base, mg_graph=1)) as a, Simulation(dict(base, mg_graph=0)) as b:
+        for _ in range(6):
+            ia, ib = a.step(), b.step()
+            assert ia.it == ib.it
+            assert ia.res == ib.res
+        for f in "uvwp":
+            np.testing.assert_array_equal(a.field(f), b.field(f))
