@@ -66,6 +66,9 @@ def parse_args():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-roofline", action="store_true",
                     help="skip the per-kernel timing launches (clean launch lists for ncu)")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="host-driven solves instead of one graph per solve (the same kernels, "
+                         "visible one by one to a profiler's launch list)")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the FP64 multigrid comparison run")
     ap.add_argument("--itermax", type=int, default=None,
@@ -143,15 +146,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# V-cycle shape of each solver in the benchmark: the FP64 arm keeps the V(2,2)
+# of the reference configuration; the mixed-precision solver runs V(3,3) with up
+# to 4 FP32 V-cycles per FP64 residual (fastest of the shapes measured at 256^3)
+MG_SHAPE = {"mg": (2, 2, 4), "mg-mixed": (3, 3, 4)}
+
+
 def bench_case(n: int, solver: str, itermax: int | None = None,
-               guess: str = "previous") -> dict:
+               guess: str = "previous", shape: tuple[int, int, int] | None = None,
+               graph: bool = True) -> dict:
     from nusif.params import config2
     vals = config2(solver=solver)
     vals.update(imax=n, jmax=n, kmax=n)
     if itermax is not None:
         vals["itermax"] = itermax
     if solver in ("mg", "mg-mixed"):
-        vals["mg_guess"] = guess
+        pre, post, inner = shape or MG_SHAPE[solver]
+        vals.update(mg_guess=guess, mg_pre=pre, mg_post=post, mg_inner=inner,
+                    mg_graph=1 if graph else 0)
     return vals
 
 
@@ -216,7 +228,7 @@ def run_gpu(args, rank, world, local):
     lib.nusifSetStream(C.c_void_p(stream.cuda_stream))
 
     solver = pick_solver(args.solver)
-    vals = bench_case(args.n, solver, args.itermax, args.guess)
+    vals = bench_case(args.n, solver, args.itermax, args.guess, graph=not args.no_graph)
     sim = nusif.Simulation(vals)
     i, j, k = sim.dims
     ncell = i * j * k
@@ -237,11 +249,14 @@ def run_gpu(args, rank, world, local):
     compare = None
     if solver == "mg-mixed" and not args.no_compare:
         compare = []
-        for g in dict.fromkeys(["previous", args.guess]):
-            sim64 = nusif.Simulation(bench_case(args.n, "mg", args.itermax, g))
+        arms = [("previous", (2, 2, 4)), (args.guess, (2, 2, 4)), (args.guess, (3, 3, 4))]
+        for g, shape in dict.fromkeys(arms):
+            sim64 = nusif.Simulation(bench_case(args.n, "mg", args.itermax, g, shape,
+                                                graph=not args.no_graph))
             ref64 = timed_steps(sim64, args, stream, local, world)
             sim64.close()
             compare.append({"solver": "mg (FP64 V-cycles, same rtol 1e-6)", "guess": g,
+                            "v_cycle": "V(%d,%d)" % shape[:2],
                             "ms_per_step": ref64["ms_per_step"],
                             "v_cycles_per_step": ref64["iters"],
                             "residual_per_step": ref64["res"],
@@ -273,6 +288,11 @@ def run_gpu(args, rank, world, local):
                    "cells": ncell, "solver": solver, "tolerance": tol,
                    "learned_warm_start": False,
                    "initial_guess": (args.guess if solver in ("mg", "mg-mixed") else "previous"),
+                   "v_cycle": ("V(%d,%d), up to %d FP32 V-cycles per FP64 residual"
+                               % MG_SHAPE["mg-mixed"] if solver == "mg-mixed" else
+                               "V(%d,%d)" % MG_SHAPE["mg"][:2] if solver == "mg" else None),
+                   "solve_launch": ("host-driven launches" if args.no_graph else
+                                    "one CUDA graph per solve (device while-loops)"),
                    "l2": "no flush: 8 FP64 fields of %.0f MB each, far larger than L2" % (padded * 8 / 1e6),
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "solver_iterations_per_step": head["iters"],

@@ -99,6 +99,10 @@ struct MgHierarchy {
   const double *graph_p = nullptr, *graph_rhs = nullptr;
   cudaStream_t cap[3] = {};  // capture streams: graph, outer body, inner body
   bool use_graph = true;     // mg_graph: the host-driven solve runs as one graph
+  // kernels per part of the graph (counted at capture): head, one outer unit
+  // without its inner loop, one inner V-cycle, tail
+  int n_head = 0, n_outer = 0, n_inner = 0, n_tail = 0;
+  int n_inner_capture = 0;  // scratch while capturing
   double *h_ptrs[2 * kMaxLevels] = {};  // exposed through Solver::r / Solver::e
 };
 
@@ -374,27 +378,31 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong(View<T> f, const T *xc, int 
 // One whole red-black Gauss-Seidel sweep in one kernel, exact: reads x_old,
 // writes x_new (ping-pong), so no block ever reads a value another block
 // writes. A block owns a 64 x 8 tile of (i, j) columns and a chunk of planes;
-// per plane it relaxes the first-colour cells ((i + j + k) even, 0-based) on
-// the tile plus a one-cell ring (from old second-colour values: exactly what
-// the first pass of a two-pass sweep computes there), then the second-colour
-// cells of the previous plane on the tile (from the new first-colour values
-// and their own old value), and writes both colours of that plane. Planes
-// walk with a one-plane lag; the first-colour planes just outside the chunk
-// are recomputed, so chunks are independent.
-//
-// Shared memory holds every staged row split by parity (the cells at even x,
-// then the cells at odd x), so that one colour and all its neighbours are read
-// at unit stride: no bank conflicts. x_old (tile + two-cell ring) and b (tile
-// + one-cell ring) are loaded as 16-byte chunks into registers one plane
-// ahead and de-interleaved into shared memory after the plane's arithmetic,
-// so global latency overlaps that arithmetic. One sweep reads x and b once
-// and writes x once. ZERO: x_old is zero (not read).
+// per plane it relaxes the odd ("red") cells on the tile plus a one-cell ring
+// (from old even values: exactly what the first pass of a two-pass sweep
+// computes there), then the even cells of the previous plane on the tile
+// (from the new odd values and their own old value), and writes both colours
+// of that plane. Planes walk with a one-plane lag (odd at k, even at k-1); the
+// odd planes just outside the chunk are recomputed, so chunks are
+// independent. x_old (tile + two-cell ring) and b (tile + one-cell ring) are
+// staged in shared memory by asynchronous copies issued one plane ahead
+// (cp.async, completed by cp.async.wait_group), so global latency overlaps
+// the arithmetic of the plane before. One sweep reads x and b once and
+// writes x once. ZERO: x_old is zero (not read).
 constexpr int kSX = 64, kSY = 8;  // tile (cells)
 constexpr int kWX = kSX + 8;      // staged row: tile + 4 cells each side (16-byte chunks)
-constexpr int kHX = kWX / 2;      // cells of one parity in a staged row (36)
 constexpr int kRY = kSY + 4;      // staged x_old rows: tile + 2-row ring
-constexpr int kBYr = kSY + 2;     // staged b rows and first-colour values: tile + 1-row ring
-constexpr int kRedRow = kSX / 2 + 1;  // first-colour cells per row on tile + ring (33)
+constexpr int kBYr = kSY + 2;     // staged b rows and odd values: tile + 1-row ring
+constexpr int kQX = kSX + 2;      // odd values: tile + 1-cell ring
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // FP32 levels with nx % 4 == 0 (rows start on 16-byte boundaries): every
 // staged row is 18 chunks of four cells starting 4 cells left of the tile,
@@ -405,10 +413,9 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
     int kc, const MgState *st)
 {
   if (mg_done(st)) return;
-  // [slot][row][parity][x / 2]
-  __shared__ __align__(16) float xo[4][kRY][2][kHX];   // x_old planes, slot = plane & 3
-  __shared__ __align__(16) float bs[3][kBYr][2][kHX];  // b planes, slot = plane % 3
-  __shared__ float xr[3][kBYr][kHX];                   // new first-colour values, slot = plane % 3
+  __shared__ __align__(16) float xo[4][kRY][kWX];   // x_old planes, slot = plane & 3
+  __shared__ __align__(16) float bs[3][kBYr][kWX];  // b planes, slot = plane % 3
+  __shared__ float xr[3][kBYr][kQX];                // new odd values, slot = plane % 3
   const float *__restrict__ xold = v.x;
   const float *__restrict__ b = v.b;
   const int nx = v.nx, ny = v.ny, nz = v.nz;
@@ -422,90 +429,78 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
   const bool x_lane = cr < kRY, b_lane = cr < kBYr;
   const int gjx = min(max(j0 - 2 + cr, 0), ny - 1), gjb = min(max(j0 - 1 + cr, 0), ny - 1);
   const int64_t xoff = (int64_t)gjx * v.sy + gic, boff = (int64_t)gjb * v.sy + gic;
-  float4 px = make_float4(0.f, 0.f, 0.f, 0.f), pb = px;  // prefetched chunks
-  auto fetch = [&](int kx, int kb) {
+  auto stage = [&](int kx, int kb) {
     if (!ZERO && x_lane && kx >= 0 && kx < nz)
-      px = __ldg(reinterpret_cast<const float4 *>(xold + (int64_t)kx * v.sz + xoff));
+      cp_async16(&xo[kx & 3][cr][4 * cc], xold + (int64_t)kx * v.sz + xoff);
     if (b_lane && kb >= 0 && kb < nz)
-      pb = __ldg(reinterpret_cast<const float4 *>(b + (int64_t)kb * v.sz + boff));
-  };
-  auto place = [&](int kx, int kb) {  // de-interleave into the split rows
-    if (!ZERO && x_lane && kx >= 0 && kx < nz) {
-      *reinterpret_cast<float2 *>(&xo[kx & 3][cr][0][2 * cc]) = make_float2(px.x, px.z);
-      *reinterpret_cast<float2 *>(&xo[kx & 3][cr][1][2 * cc]) = make_float2(px.y, px.w);
-    }
-    if (b_lane && kb >= 0 && kb < nz) {
-      *reinterpret_cast<float2 *>(&bs[kb % 3][cr][0][2 * cc]) = make_float2(pb.x, pb.z);
-      *reinterpret_cast<float2 *>(&bs[kb % 3][cr][1][2 * cc]) = make_float2(pb.y, pb.w);
-    }
+      cp_async16(&bs[kb % 3][cr][4 * cc], b + (int64_t)kb * v.sz + boff);
   };
   if (ZERO) {
-    for (int q = tid; q < 4 * kRY * 2 * kHX; q += 256) (&xo[0][0][0][0])[q] = 0.0f;
+    for (int q = tid; q < 4 * kRY * kWX; q += 256) (&xo[0][0][0])[q] = 0.0f;
   }
-  fetch(k0 - 2, -1);
-  place(k0 - 2, -1);
-  fetch(k0 - 1, k0 - 1);
-  place(k0 - 1, k0 - 1);
-  fetch(k0, -1);
-  place(k0, -1);
-  constexpr int kRed = kRedRow * kBYr;  // first-colour cells per plane on tile + ring (330)
+  stage(k0 - 2, -1);
+  stage(k0 - 1, k0 - 1);
+  stage(k0, -1);
+  cp_async_commit();
+  constexpr int kOdd = (kQX / 2) * kBYr;  // odd cells per plane on tile + ring (330)
   for (int k = k0 - 1; k <= k1; k++) {
-    fetch(k + 2, k + 1);  // lands in registers during this plane's arithmetic
+    stage(k + 2, k + 1);  // prefetch: completes during this plane's arithmetic
+    cp_async_commit();
+    cp_async_wait<1>();   // all but the prefetch: x_old(k+1), b(k) are in
     __syncthreads();
     if (k >= 0 && k < nz) {
-      float(*rq)[kHX] = xr[k % 3];
-      const float(*xk)[2][kHX] = xo[k & 3];
-      const float(*xkm)[2][kHX] = xo[(k + 3) & 3];
-      const float(*xkp)[2][kHX] = xo[(k + 1) & 3];
-      const float(*bk)[2][kHX] = bs[k % 3];
-      for (int q = tid; q < kRed; q += 256) {
-        const int lj = q / kRedRow, m = q - lj * kRedRow;
+      float(*rq)[kQX] = xr[k % 3];
+      const float(*xk)[kWX] = xo[k & 3];
+      const float(*xkm)[kWX] = xo[(k + 3) & 3];
+      const float(*xkp)[kWX] = xo[(k + 1) & 3];
+      const float(*bk)[kWX] = bs[k % 3];
+      for (int q = tid; q < kOdd; q += 256) {
+        const int lj = q / (kQX / 2), pi = q - lj * (kQX / 2);
         const int gj = j0 - 1 + lj;
-        const int p = (gj + k) & 1;        // parity of x of this row's first-colour cells
-        const int h = (p ? 1 : 2) + m;     // staged x = 2h + p, tile x - 1 .. tile x + 64
-        const int gi = i0 - 4 + 2 * h + p;
+        const int li = 2 * pi + ((i0 + gj + k) & 1 ? 0 : 1);  // odd cell column
+        const int gi = i0 - 1 + li;
         if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
-        const int sj = lj + 1;  // staged x_old row
-        const float xc = xk[sj][p][h];
-        const float sx = (gi > 0 ? xk[sj][1 - p][h - 1 + p] : xc) +
-                         (gi < nx - 1 ? xk[sj][1 - p][h + p] : xc);
-        const float sy = (gj > 0 ? xk[sj - 1][p][h] : xc) + (gj < ny - 1 ? xk[sj + 1][p][h] : xc);
-        const float sz = (k > 0 ? xkm[sj][p][h] : xc) + (k < nz - 1 ? xkp[sj][p][h] : xc);
+        const int si = li + 3, sj = lj + 1;  // staged x_old column / row
+        const float xc = xk[sj][si];
+        const float sx = (gi > 0 ? xk[sj][si - 1] : xc) + (gi < nx - 1 ? xk[sj][si + 1] : xc);
+        const float sy = (gj > 0 ? xk[sj - 1][si] : xc) + (gj < ny - 1 ? xk[sj + 1][si] : xc);
+        const float sz = (k > 0 ? xkm[sj][si] : xc) + (k < nz - 1 ? xkp[sj][si] : xc);
         const float lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
-        rq[lj][h] = xc - (bk[lj][p][h] - lap) * v.inv_diag;
+        rq[lj][li] = xc - (bk[lj][li + 3] - lap) * v.inv_diag;
       }
     }
     __syncthreads();
-    // second-colour cells of plane k-1 on the tile: one per thread, stored
-    // with its first-colour neighbour in the same aligned pair as 8 bytes
+    // even cells of plane k-1 on the tile: one cell pair per thread, both
+    // cells stored as one 8-byte vector
     const int ke = k - 1;
     if (ke >= k0 && ke < k1) {
-      const float(*rm)[kHX] = xr[(ke + 2) % 3];
-      const float(*r0)[kHX] = xr[ke % 3];
-      const float(*rp)[kHX] = xr[(ke + 1) % 3];
-      const float(*xe)[2][kHX] = xo[ke & 3];
-      const float(*be)[2][kHX] = bs[ke % 3];
-      const int tj = tid >> 5, h = 2 + (tid & 31);
+      const float(*rm)[kQX] = xr[(ke + 2) % 3];
+      const float(*r0)[kQX] = xr[ke % 3];
+      const float(*rp)[kQX] = xr[(ke + 1) % 3];
+      const float(*xe)[kWX] = xo[ke & 3];
+      const float(*be)[kWX] = bs[ke % 3];
+      const int tj = tid >> 5, pi = tid & 31;
       const int gj = j0 + tj;
-      const int pe = (gj + ke + 1) & 1;  // parity of x of this row's second-colour cells
-      const int gi = i0 - 4 + 2 * h + pe;
-      const int gpair = i0 - 4 + 2 * h;
-      if (gj < ny && gpair < nx) {
-        const int lj = tj + 1;  // first-colour / b row
-        const float xc = xe[lj + 1][pe][h];
-        const float left = r0[lj][h - 1 + pe], right = r0[lj][h + pe];
-        const float sx = (gi > 0 ? left : xc) + (gi < nx - 1 ? right : xc);
-        const float sy = (gj > 0 ? r0[lj - 1][h] : xc) + (gj < ny - 1 ? r0[lj + 1][h] : xc);
-        const float sz = (ke > 0 ? rm[lj][h] : xc) + (ke < nz - 1 ? rp[lj][h] : xc);
+      const int e = (i0 + gj + ke + 1) & 1;  // position of the even cell in the pair
+      const int te = 2 * pi + e;
+      const int gi = i0 + te;
+      if (gj < ny && i0 + 2 * pi < nx) {
+        const int li = te + 1, lj = tj + 1;
+        const float xc = xe[lj + 1][te + 4];
+        const float sx = (gi > 0 ? r0[lj][li - 1] : xc) + (gi < nx - 1 ? r0[lj][li + 1] : xc);
+        const float sy = (gj > 0 ? r0[lj - 1][li] : xc) + (gj < ny - 1 ? r0[lj + 1][li] : xc);
+        const float sz = (ke > 0 ? rm[lj][li] : xc) + (ke < nz - 1 ? rp[lj][li] : xc);
         const float lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
-        const float second = xc - (be[lj][pe][h] - lap) * v.inv_diag;
-        const float first = r0[lj][h];
-        const float2 pair = pe ? make_float2(first, second) : make_float2(second, first);
-        *reinterpret_cast<float2 *>(xnew + (int64_t)ke * v.sz + (int64_t)gj * v.sy + gpair) = pair;
+        const float even = xc - (be[lj][te + 4] - lap) * v.inv_diag;
+        const float odd = r0[lj][(te ^ 1) + 1];
+        const float2 pair = e ? make_float2(odd, even) : make_float2(even, odd);
+        *reinterpret_cast<float2 *>(xnew + (int64_t)ke * v.sz + (int64_t)gj * v.sy + i0 + 2 * pi) =
+            pair;
       }
     }
-    place(k + 2, k + 1);  // slots no thread reads in this iteration
+    __syncthreads();
   }
+  cp_async_wait<0>();
 }
 
 // x_f += trilinear interpolation of x_c when x was coarsened (rx == 2): one
@@ -1284,12 +1279,14 @@ bool cycle_mixed_nested(MgHierarchy *H, double *p, const double *rhs, cudaStream
   k_inner_open<<<1, 1, 0, s>>>(st, h);
   if (!launched("k_inner_open")) return false;
   const int inner = H->inner;
+  const unsigned long long c0 = launch_count();
   if (!capture_while(s, inner_body, h, [&] {
         if (!vcycle<float>(H, 0, H->x32, H->b32, false, true)) return false;
         k_inner_continue<<<1, 1, 0, stream()>>>(st, h, inner);
         return launched("k_inner_continue");
       }))
     return false;
+  H->n_inner_capture = (int)(launch_count() - c0);
   View<float> e = compact_view<float>(H->lv[0], H->x32[0], H->b32[0]);
   k_mx_fold<<<flat_blocks(n0), kNT, 0, stream()>>>(e, p, v0.sy, v0.sz, st);
   return launched("k_mx_fold");
@@ -1306,7 +1303,9 @@ bool enqueue_units_loop(MgHierarchy *H, double *p, const double *rhs, cudaStream
   cudaStream_t s = stream();
   cudaGraphConditionalHandle h;
   if (!make_handle(s, 1, cudaGraphCondAssignDefault, &h)) return false;
-  return capture_while(s, outer_body, h, [&] {
+  const unsigned long long c0 = launch_count();
+  H->n_inner_capture = 0;
+  const bool ok = capture_while(s, outer_body, h, [&] {
     bool ok;
     if (H->mode == 0) ok = cycle_fp64(H, p, rhs);
     else if (H->nl == 1) ok = cycle_mixed(H, p, rhs);
@@ -1315,6 +1314,9 @@ bool enqueue_units_loop(MgHierarchy *H, double *p, const double *rhs, cudaStream
     k_mg_continue<<<1, 1, 0, stream()>>>(H->d_state, h, H->maxcycles + 2);
     return launched("k_mg_continue");
   });
+  H->n_inner = H->n_inner_capture;
+  H->n_outer = (int)(launch_count() - c0) - H->n_inner;
+  return ok;
 }
 
 // the whole solve (head, units loop, pressure ghosts) as one graph for p, rhs
@@ -1326,12 +1328,18 @@ bool build_solve_graph(MgHierarchy *H, double *p, const double *rhs)
   }
   cudaStream_t lib = stream();
   cudaGraph_t g = nullptr;
+  const unsigned long long c0 = launch_count();
   if (!cuda_ok(cudaStreamBeginCapture(H->cap[0], cudaStreamCaptureModeThreadLocal), "capture"))
     return false;
   nusifSetStream(H->cap[0]);
   View<double> v0 = padded_view(H->lv[0], p, rhs);
-  bool ok = enqueue_solve_head(H, v0) && enqueue_units_loop(H, p, rhs, H->cap[1], H->cap[2]) &&
-            launch_pressure_ghosts(make_dims(v0.nx, v0.ny, v0.nz), p);
+  bool ok = enqueue_solve_head(H, v0);
+  H->n_head = (int)(launch_count() - c0);
+  ok = ok && enqueue_units_loop(H, p, rhs, H->cap[1], H->cap[2]);
+  const unsigned long long c1 = launch_count();
+  ok = ok && launch_pressure_ghosts(make_dims(v0.nx, v0.ny, v0.nz), p);
+  H->n_tail = (int)(launch_count() - c1);
+  set_launch_count(c0);  // nothing ran yet
   nusifSetStream(lib);
   const bool ended = cuda_ok(cudaStreamEndCapture(H->cap[0], &g), "capture end");
   ok = ok && ended && cuda_ok(cudaGraphInstantiate(&H->graph, g, 0), "solve graph");
@@ -1428,6 +1436,10 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
             "mg state download") ||
         !cuda_ok(cudaStreamSynchronize(stream()), "mg sync"))
       return NAN;
+    // the kernels the graph ran: head, outer units, inner V-cycles, tail
+    const bool nested = H->mode == 1 && H->nl > 1;
+    set_launch_count(launch_count() + H->n_head + (unsigned long long)h->loops * H->n_outer +
+                     (nested ? (unsigned long long)h->cycles * H->n_inner : 0ull) + H->n_tail);
   } else {
     memset(h, 0, sizeof(*h));
     h->rtol2 = H->rtol * H->rtol;

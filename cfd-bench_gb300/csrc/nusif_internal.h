@@ -16,6 +16,8 @@ bool has_error();                              // an error is pending (record mo
 cudaStream_t stream();
 // after every kernel launch: counts it and checks the launch error
 bool launched(const char *what);
+unsigned long long launch_count();
+void set_launch_count(unsigned long long n);
 
 // ---- problem kinds and solver kinds ----
 enum Problem { PROBLEM_NONE = 0, PROBLEM_DCAVITY = 1, PROBLEM_CANAL = 2 };

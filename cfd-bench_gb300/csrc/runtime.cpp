@@ -48,6 +48,11 @@ cudaStream_t stream() { return g_stream; }
 
 static unsigned long long g_launches = 0;
 
+unsigned long long launch_count() { return g_launches; }
+// kernels captured into a graph are not launched at capture time; a graph's
+// executed kernels are added when it has run
+void set_launch_count(unsigned long long n) { g_launches = n; }
+
 bool launched(const char *what)
 {
   g_launches++;
