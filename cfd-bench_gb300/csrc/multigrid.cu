@@ -92,8 +92,9 @@ struct MgHierarchy {
   int last_cycles = 0;  // queue size of the previous solve (cycles, or outer iterations)
   int inner = 4;        // mg-mixed: most FP32 V-cycles per FP64 residual
   int guess = 0;        // 1: start from 2 p(n-1) - p(n-2)
-  double *p_prev = nullptr;  // padded copy of the previous solve's result (guess 1)
-  bool have_prev = false;
+  double *p_prev = nullptr;   // padded copy of the previous solve's result (guess >= 1)
+  double *p_prev2 = nullptr;  // and of the one before (guess 2)
+  int n_hist = 0;             // earlier solutions kept (0, 1, 2)
   // the solve as one CUDA graph (head, while-loops, tail) for fixed p / rhs
   cudaGraphExec_t graph = nullptr;
   const double *graph_p = nullptr, *graph_rhs = nullptr;
@@ -989,15 +990,21 @@ bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero, bool inner_test)
   return level_sweeps<T>(H, l, v, H->post, false, st);
 }
 
-// p += e (FP64) and Neumann ghosts of p, after the inner V-cycles
-// initial guess by linear extrapolation in time: p <- 2 p(n-1) - p(n-2), and
-// p(n-1) kept for the next solve (whole padded array, ghosts included)
-__global__ void k_extrapolate(double *__restrict__ p, double *__restrict__ p_prev, int64_t n)
+// initial guess by extrapolation in time (whole padded arrays, ghosts
+// included): linear p <- 2 p(n-1) - p(n-2), or with p2 (the solve before)
+// quadratic p <- 3 p(n-1) - 3 p(n-2) + p(n-3); the history shifts by one
+__global__ void k_extrapolate(double *__restrict__ p, double *__restrict__ p_prev,
+    double *__restrict__ p2, int64_t n)
 {
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x) {
-    const double cur = p[q];
-    p[q] = 2.0 * cur - p_prev[q];
+    const double cur = p[q], prev = p_prev[q];
+    if (p2) {
+      p[q] = 3.0 * (cur - prev) + p2[q];
+      p2[q] = prev;
+    } else {
+      p[q] = 2.0 * cur - prev;
+    }
     p_prev[q] = cur;
   }
 }
@@ -1070,15 +1077,17 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
   H->coarse_sweeps = x.mg_coarse_sweeps;
   H->maxcycles = x.mg_maxcycles;
   H->inner = x.mg_inner < 1 ? 1 : x.mg_inner;
-  H->guess = x.mg_guess == 1 ? 1 : 0;
+  H->guess = x.mg_guess == 1 || x.mg_guess == 2 ? x.mg_guess : 0;
   H->use_graph = x.mg_graph != 0;
   for (cudaStream_t &c : H->cap)
     if (!cuda_ok(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking), "mg capture stream"))
       return false;
-  if (H->guess == 1) {
+  if (H->guess >= 1) {
     const size_t padded =
         (size_t)(d->grid.imax + 2) * (d->grid.jmax + 2) * (d->grid.kmax + 2) * sizeof(double);
     if (!cuda_ok(cudaMalloc(&H->p_prev, padded), "cudaMalloc(p_prev)")) return false;
+    if (H->guess == 2 && !cuda_ok(cudaMalloc(&H->p_prev2, padded), "cudaMalloc(p_prev2)"))
+      return false;
   }
   H->rtol = x.rtol;
   if (H->pre < 0 || H->post < 0 || H->coarse_sweeps < 0 || H->maxcycles < 1 || !(H->rtol >= 0)) {
@@ -1410,17 +1419,24 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
   View<double> v0 = padded_view(H->lv[0], p, rhs);
   const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
   const int blocks = flat_blocks(n0);
-  if (H->guess == 1) {
+  if (H->guess >= 1) {
     const int64_t padded = (int64_t)(v0.nx + 2) * (v0.ny + 2) * (v0.nz + 2);
-    if (H->have_prev) {
-      k_extrapolate<<<flat_blocks(padded), kNT, 0, stream()>>>(p, H->p_prev, padded);
+    if (H->n_hist >= 1) {
+      // quadratic once two earlier solutions exist (guess 2), else linear
+      double *p2 = H->guess == 2 && H->n_hist >= 2 ? H->p_prev2 : nullptr;
+      if (H->guess == 2 && H->n_hist == 1 &&
+          !cuda_ok(cudaMemcpyAsync(H->p_prev2, H->p_prev, padded * sizeof(double),
+                       cudaMemcpyDeviceToDevice, stream()),
+              "keep p(n-2)"))
+        return NAN;
+      k_extrapolate<<<flat_blocks(padded), kNT, 0, stream()>>>(p, H->p_prev, p2, padded);
       if (!launched("k_extrapolate")) return NAN;
     } else if (!cuda_ok(cudaMemcpyAsync(H->p_prev, p, padded * sizeof(double),
                             cudaMemcpyDeviceToDevice, stream()),
                    "keep p")) {
       return NAN;
     }
-    H->have_prev = true;
+    H->n_hist = H->n_hist < 2 ? H->n_hist + 1 : 2;
   }
   // learned warm start: may replace p by the network's guess (never a worse residual)
   if (ss->guess && !guess_before_solve(ss->guess, s->grid, p, rhs)) return NAN;
@@ -1555,6 +1571,7 @@ void mg_free(Solver *s, SolverState *ss)
   for (cudaStream_t c : H->cap)
     if (c) cudaStreamDestroy(c);
   if (H->p_prev) cudaFree(H->p_prev);
+  if (H->p_prev2) cudaFree(H->p_prev2);
   if (H->minv64) cudaFree(H->minv64);
   if (H->minv32) cudaFree(H->minv32);
   if (H->d_state) cudaFree(H->d_state);

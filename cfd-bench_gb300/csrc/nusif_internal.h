@@ -33,7 +33,7 @@ struct Extras {
   int mg_pre = 2, mg_post = 2;
   int mg_coarse_sweeps = 0;  // 0: exact coarsest solve (<= 1024 cells), else sweeps
   int mg_inner = 4;          // mg-mixed: most FP32 V-cycles per FP64 residual
-  int mg_guess = 0;          // initial guess: 0 previous p, 1 linear extrapolation in time
+  int mg_guess = 0;          // initial guess: 0 previous p, 1 linear, 2 quadratic extrapolation in time
   int mg_graph = 1;          // 1: each solve is one CUDA graph launch (while-loops on the device)
   int mg_maxcycles = 100;
 };

@@ -123,28 +123,30 @@ def test_mg_time_loop_matches_oracle(nusif_lib, oracle_mod, solver):
                 assert rel_err(sim.field(f), run.field(f)) < tol, (s, f)
 
 
-@pytest.mark.parametrize("solver", ["mg", "mg-mixed"])
-def test_mg_extrapolated_guess(nusif_lib, solver):
-    """mg_guess extrapolate starts each solve from 2 p(n-1) - p(n-2): every
-    step still ends at rtol, the velocities stay those of the previous-p guess
-    to the solver tolerance, and the time loop needs fewer V-cycles."""
+@pytest.mark.parametrize("solver,guess", [("mg", "extrapolate"), ("mg-mixed", "extrapolate"),
+                                          ("mg-mixed", "quadratic")])
+def test_mg_extrapolated_guess(nusif_lib, solver, guess):
+    """mg_guess extrapolate / quadratic start each solve from 2 p(n-1) - p(n-2)
+    / 3 p(n-1) - 3 p(n-2) + p(n-3): every step still ends at rtol, the
+    velocities stay those of the previous-p guess to the solver tolerance, and
+    the time loop needs fewer V-cycles."""
     from nusif import Simulation
     from nusif.params import cavity
     base = cavity(32, re=1000.0, te=1e9, solver=solver, rtol=1e-8)
     cycles = {}
     fields = {}
-    for guess in ("previous", "extrapolate"):
-        with Simulation(dict(base, mg_guess=guess)) as sim:
+    for g in ("previous", guess):
+        with Simulation(dict(base, mg_guess=g)) as sim:
             its = []
             for _ in range(12):
                 a = sim.step()
                 assert a.res <= 1e-8
                 its.append(a.it)
-            cycles[guess] = sum(its[4:])
-            fields[guess] = {f: sim.field(f) for f in "uvw"}
-    assert cycles["extrapolate"] < cycles["previous"]
+            cycles[g] = sum(its[4:])
+            fields[g] = {f: sim.field(f) for f in "uvw"}
+    assert cycles[guess] < cycles["previous"]
     for f in "uvw":
-        assert rel_err(fields["extrapolate"][f], fields["previous"][f]) < 1e-5, f
+        assert rel_err(fields[guess][f], fields["previous"][f]) < 1e-5, f
 
 
 def _rb_sweep_f32(x, b, h):
