@@ -407,8 +407,15 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 
 // FP32 levels with nx % 4 == 0 (rows start on 16-byte boundaries): every
 // staged row is 18 chunks of four cells starting 4 cells left of the tile,
-// one chunk per thread per array per plane. Chunks outside the domain copy
-// the nearest in-domain chunk and are never read (boundary tests below).
+// one chunk per thread per array per plane.
+//
+// Walls cost no tests per neighbour: the Neumann operator replaces a missing
+// neighbour by the cell itself, and the staged x_old already holds that value
+// outside the domain (planes beyond a wall are staged as the wall plane, rows
+// beyond a wall as the wall row, and the column beyond a wall is patched to
+// the wall column); a first-colour ring cell outside the domain stores that
+// mirrored old value instead of a relaxed one, which is exactly what its
+// second-colour neighbour inside the domain must see there.
 template <bool ZERO>
 __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__restrict__ xnew,
     int kc, const MgState *st)
@@ -431,73 +438,99 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
   const int gjx = min(max(j0 - 2 + cr, 0), ny - 1), gjb = min(max(j0 - 1 + cr, 0), ny - 1);
   const int64_t xoff = (int64_t)gjx * v.sy + gic, boff = (int64_t)gjb * v.sy + gic;
   auto stage = [&](int kx, int kb) {
-    if (!ZERO && x_lane && kx >= 0 && kx < nz)
-      cp_async16(&xo[kx & 3][cr][4 * cc], xold + (int64_t)kx * v.sz + xoff);
+    if (!ZERO && x_lane && kx <= k1 + 1) {
+      const int kk = min(max(kx, 0), nz - 1);  // mirror planes beyond the walls
+      cp_async16(&xo[kx & 3][cr][4 * cc], xold + (int64_t)kk * v.sz + xoff);
+    }
     if (b_lane && kb >= 0 && kb < nz)
       cp_async16(&bs[kb % 3][cr][4 * cc], b + (int64_t)kb * v.sz + boff);
   };
+  // staged columns of the ghosts beyond the x walls, when inside this window
+  const bool wl = i0 == 0;             // gi = -1 at column 3, wall column 4
+  const int wr = nx - (i0 - 4);        // column of gi = nx
+  const bool patch = !ZERO && (wl || wr < kWX);
   if (ZERO) {
     for (int q = tid; q < 4 * kRY * kWX; q += 256) (&xo[0][0][0])[q] = 0.0f;
   }
+  // this thread's first-colour items (at most two per plane): row, pair index
+  constexpr int kRow = kQX / 2;           // 33 per row
+  constexpr int kOdd = kRow * kBYr;       // 330 per plane
+  const int qa = tid, qb = tid + 256;
+  const int lja = qa / kRow, pia = qa - lja * kRow;
+  const int ljb = qb / kRow, pib = qb - ljb * kRow;
+  const bool has_b = qb < kOdd;
+  const int gja = j0 - 1 + lja, gjb2 = j0 - 1 + ljb;
+  const bool rowa = gja >= 0 && gja < ny, rowb = gjb2 >= 0 && gjb2 < ny;
+  // second-colour item: one cell per thread
+  const int tj = tid >> 5, ep = tid & 31;
+  const int gje = j0 + tj;
+  const bool even_ok = gje < ny && i0 + 2 * ep < nx;
+  const float ex = v.ex, ey = v.ey, ez = v.ez, dg = v.diag, idg = v.inv_diag;
+
   stage(k0 - 2, -1);
   stage(k0 - 1, k0 - 1);
   stage(k0, -1);
   cp_async_commit();
-  constexpr int kOdd = (kQX / 2) * kBYr;  // odd cells per plane on tile + ring (330)
   for (int k = k0 - 1; k <= k1; k++) {
     stage(k + 2, k + 1);  // prefetch: completes during this plane's arithmetic
     cp_async_commit();
     cp_async_wait<1>();   // all but the prefetch: x_old(k+1), b(k) are in
     __syncthreads();
-    if (k >= 0 && k < nz) {
-      float(*rq)[kQX] = xr[k % 3];
+    if (patch) {  // ghost columns of plane k (read as x-neighbours below)
+      if (tid < kRY) {
+        float *row = xo[k & 3][tid];
+        if (wl) row[3] = row[4];
+        if (wr < kWX) row[wr] = row[wr - 1];
+      }
+      __syncthreads();
+    }
+    {
+      // k >= -1: (k + 3) % 3 is plane k's slot, never negative
+      float(*rq)[kQX] = xr[(k + 3) % 3];
       const float(*xk)[kWX] = xo[k & 3];
       const float(*xkm)[kWX] = xo[(k + 3) & 3];
       const float(*xkp)[kWX] = xo[(k + 1) & 3];
-      const float(*bk)[kWX] = bs[k % 3];
-      for (int q = tid; q < kOdd; q += 256) {
-        const int lj = q / (kQX / 2), pi = q - lj * (kQX / 2);
-        const int gj = j0 - 1 + lj;
-        const int li = 2 * pi + ((i0 + gj + k) & 1 ? 0 : 1);  // odd cell column
+      const float(*bk)[kWX] = bs[(k + 3) % 3];
+      const bool kin = k >= 0 && k < nz;
+      auto red = [&](int lj, int pi, int gj, bool rowin) {
+        const int li = 2 * pi + (((i0 + gj + k) & 1) ^ 1);  // first-colour column
         const int gi = i0 - 1 + li;
-        if (gi < 0 || gi >= nx || gj < 0 || gj >= ny) continue;
         const int si = li + 3, sj = lj + 1;  // staged x_old column / row
         const float xc = xk[sj][si];
-        const float sx = (gi > 0 ? xk[sj][si - 1] : xc) + (gi < nx - 1 ? xk[sj][si + 1] : xc);
-        const float sy = (gj > 0 ? xk[sj - 1][si] : xc) + (gj < ny - 1 ? xk[sj + 1][si] : xc);
-        const float sz = (k > 0 ? xkm[sj][si] : xc) + (k < nz - 1 ? xkp[sj][si] : xc);
-        const float lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
-        rq[lj][li] = xc - (bk[lj][li + 3] - lap) * v.inv_diag;
-      }
+        const float sx = xk[sj][si - 1] + xk[sj][si + 1];
+        const float sy = xk[sj - 1][si] + xk[sj + 1][si];
+        const float sz = xkm[sj][si] + xkp[sj][si];
+        const float lap = sx * ex + sy * ey + sz * ez - dg * xc;
+        const float relaxed = xc - (bk[lj][si] - lap) * idg;
+        const bool in = kin && rowin && gi >= 0 && gi < nx;
+        rq[lj][li] = in ? relaxed : xc;
+      };
+      red(lja, pia, gja, rowa);
+      if (has_b) red(ljb, pib, gjb2, rowb);
     }
     __syncthreads();
-    // even cells of plane k-1 on the tile: one cell pair per thread, both
-    // cells stored as one 8-byte vector
+    // second-colour cells of plane k-1 on the tile: one cell pair per thread,
+    // both cells stored as one 8-byte vector
     const int ke = k - 1;
-    if (ke >= k0 && ke < k1) {
+    if (ke >= k0 && ke < k1 && even_ok) {
       const float(*rm)[kQX] = xr[(ke + 2) % 3];
       const float(*r0)[kQX] = xr[ke % 3];
       const float(*rp)[kQX] = xr[(ke + 1) % 3];
       const float(*xe)[kWX] = xo[ke & 3];
       const float(*be)[kWX] = bs[ke % 3];
-      const int tj = tid >> 5, pi = tid & 31;
-      const int gj = j0 + tj;
-      const int e = (i0 + gj + ke + 1) & 1;  // position of the even cell in the pair
-      const int te = 2 * pi + e;
-      const int gi = i0 + te;
-      if (gj < ny && i0 + 2 * pi < nx) {
-        const int li = te + 1, lj = tj + 1;
-        const float xc = xe[lj + 1][te + 4];
-        const float sx = (gi > 0 ? r0[lj][li - 1] : xc) + (gi < nx - 1 ? r0[lj][li + 1] : xc);
-        const float sy = (gj > 0 ? r0[lj - 1][li] : xc) + (gj < ny - 1 ? r0[lj + 1][li] : xc);
-        const float sz = (ke > 0 ? rm[lj][li] : xc) + (ke < nz - 1 ? rp[lj][li] : xc);
-        const float lap = sx * v.ex + sy * v.ey + sz * v.ez - v.diag * xc;
-        const float even = xc - (be[lj][te + 4] - lap) * v.inv_diag;
-        const float odd = r0[lj][(te ^ 1) + 1];
-        const float2 pair = e ? make_float2(odd, even) : make_float2(even, odd);
-        *reinterpret_cast<float2 *>(xnew + (int64_t)ke * v.sz + (int64_t)gj * v.sy + i0 + 2 * pi) =
-            pair;
-      }
+      const int e = (i0 + gje + ke + 1) & 1;  // position of the second-colour cell in the pair
+      const int te = 2 * ep + e;
+      const int li = te + 1, lj = tj + 1;
+      const float xc = xe[lj + 1][te + 4];
+      const float sx = r0[lj][li - 1] + r0[lj][li + 1];
+      const float sy = r0[lj - 1][li] + r0[lj + 1][li];
+      const float sz = rm[lj][li] + rp[lj][li];
+      const float lap = sx * ex + sy * ey + sz * ez - dg * xc;
+      const float even = xc - (be[lj][te + 4] - lap) * idg;
+      const float odd = r0[lj][(te ^ 1) + 1];
+      const float2 pair = e ? make_float2(odd, even) : make_float2(even, odd);
+      *reinterpret_cast<float2 *>(xnew + (int64_t)ke * v.sz + (int64_t)gje * v.sy + i0 + 2 * ep) =
+          pair;
     }
     __syncthreads();
   }
