@@ -231,6 +231,7 @@ __global__ void __launch_bounds__(kFX *kFY) k_fgh_flux(FluxArgs A, const double 
     double *__restrict__ gg, double *__restrict__ h)
 {
   __shared__ XFace ys[2][kFY][kFX];
+  __shared__ XFace xs[2][kFY][kFX + 1];  // [row][1 + tx]: plus face of cell tx; [row][0]: the row's left halo face
   const Dims &g = A.g;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int i_raw = blockIdx.x * kFX + tx + 1;
@@ -241,20 +242,24 @@ __global__ void __launch_bounds__(kFX *kFY) k_fgh_flux(FluxArgs A, const double 
   const int k1 = min(k0 + A.kb - 1, g.kmax);
   const int sj = g.sj, sk = g.sk;
   const int64_t col = (int64_t)j * sj + i;
+  // the left halo face of row `tx` (lanes 0..kFY-1 of the first warp): the
+  // minus face of the row's first cell, computed once per row and plane
+  const bool halo = ty == 0 && tx < kFY;
+  const int64_t halo_col =
+      (int64_t)min((int)(blockIdx.y * kFY) + tx + 1, g.jmax) * sj +
+      min((int)(blockIdx.x * kFX) + 1, g.imax) - 1;
   const double dt = A.sp ? A.sp->dt : A.dt;
   ZFace zm = z_face(u, v, w, (int64_t)(k0 - 1) * sk + col, sj, sk, A.az);
   int buf = 0;
   for (int k = k0; k <= k1; k++, buf ^= 1) {
     const int64_t c = (int64_t)k * sk + col;
     const XFace xp = x_face(u, v, w, c, sj, sk, A.ax);
-    XFace xm;
-    xm.f = __shfl_up_sync(0xffffffffu, xp.f, 1);
-    xm.g = __shfl_up_sync(0xffffffffu, xp.g, 1);
-    xm.h = __shfl_up_sync(0xffffffffu, xp.h, 1);
-    if (tx == 0) xm = x_face(u, v, w, c - 1, sj, sk, A.ax);
+    xs[buf][ty][tx + 1] = xp;
+    if (halo) xs[buf][tx][0] = x_face(u, v, w, (int64_t)k * sk + halo_col, sj, sk, A.ax);
     const XFace yp = y_face(u, v, w, c, sj, sk, A.ay);
     ys[buf][ty][tx] = yp;
     __syncthreads();
+    const XFace xm = xs[buf][ty][tx];
     const XFace ym = ty > 0 ? ys[buf][ty - 1][tx] : y_face(u, v, w, c - sj, sj, sk, A.ay);
     const ZFace zp = z_face(u, v, w, c, sj, sk, A.az);
     if (active) {
