@@ -282,6 +282,61 @@ __global__ void __launch_bounds__(kNT) k_mg_restrict(View<T> f, T *bc, int cnx, 
   }
 }
 
+// The same restriction when x is halved (rx == 2), one thread per coarse cell
+// on a 3-D grid (32 x 8 coarse (I, J) per block, planes K strided by the
+// grid): no index division, children in the same order as k_mg_restrict.
+template <typename T, int FOLD>
+__global__ void __launch_bounds__(kNT) k_mg_restrict_x2(View<T> f, T *bc, int cnx, int cny,
+    int cnz, int ry, int rz, T inv_count, const double *shift, MgState *st, double *partials,
+    unsigned *ticket)
+{
+  constexpr bool ACCUM = FOLD != FOLD_NONE;
+  if (mg_done(st)) return;
+  const T sh = shift ? (T)(*shift) : (T)0;
+  const int I = blockIdx.x * 32 + threadIdx.x, J = blockIdx.y * 8 + threadIdx.y;
+  double acc = 0.0;
+  if (I < cnx && J < cny) {
+    for (int K = blockIdx.z; K < cnz; K += gridDim.z) {
+      T sum = 0;
+      for (int dk = 0; dk < rz; dk++)
+        for (int dj = 0; dj < ry; dj++)
+#pragma unroll
+          for (int di = 0; di < 2; di++) {
+            const int i = 2 * I + di, j = J * ry + dj, k = K * rz + dk;
+            const int64_t c = f.off + (int64_t)k * f.sz + (int64_t)j * f.sy + i;
+            const T r = (f.b[c] - sh) - lap_at(f, f.x, i, j, k, c, f.x[c]);
+            sum += r;
+            if (ACCUM) acc += (double)r * (double)r;
+          }
+      if (bc) bc[((int64_t)K * cny + J) * cnx + I] = sum * inv_count;
+    }
+  }
+  if (!ACCUM) return;
+  __shared__ double sm[kNT / 32];
+  acc = block_reduce_sum<kNT>(acc, sm);
+  __shared__ bool last;
+  const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (flat_tid() == 0) {
+    partials[bid] = acc;
+    last = ticket_is_last(ticket);
+  }
+  __syncthreads();
+  if (!last) return;
+  const double total = fold_partials<kNT>(partials, gridDim.x * gridDim.y * gridDim.z, sm);
+  if (flat_tid() == 0) {
+    const int c = st->cycles + 1;
+    st->cycles = c;
+    if (FOLD == FOLD_OUTER) {
+      st->res2 = total;
+      st->done = (total <= st->tol2) || (c >= st->maxcycles);
+    } else {
+      st->res2_inner = total;
+      st->inner_done = total <= st->tol_inner;
+    }
+    *ticket = 0;
+  }
+}
+
 // FP64 residual of p (padded layout) into the FP32 fine right-hand side, with
 // its FP64 norm folded by the last block: the mixed-precision stop test. It
 // also opens the next correction (inner_done = 0). count_cycles: one FP32
@@ -373,6 +428,77 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong(View<T> f, const T *xc, int 
     const T y1 = v[1][0] + w[1] * (v[1][1] - v[1][0]);
     const int64_t c = f.off + (int64_t)fi[2] * f.sz + (int64_t)fi[1] * f.sy + fi[0];
     f.x[c] += y0 + w[2] * (y1 - y0);
+  }
+}
+
+// x_f += trilinear interpolation of x_c when x was coarsened (rx == 2) and
+// the fine rows hold a multiple of four cells: one thread per four
+// consecutive fine cells (two coarse x-positions), so the four coarse values
+// of each (y, z) line are loaded once for four cells, and (VEC, FP32 compact
+// rows) the fine cells move as one 16-byte vector. Same interpolation order
+// as k_mg_prolong_x2 (x, then y, then z).
+template <typename T, bool VEC>
+__global__ void __launch_bounds__(kNT) k_mg_prolong_x4(View<T> f, const T *__restrict__ xc,
+    int cnx, int cny, int cnz, int ry, int rz, const MgState *st)
+{
+  if (mg_done(st)) return;
+  const int Q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z;
+  if (4 * Q >= f.nx || j >= f.ny || k >= f.nz) return;
+  int Py, Qy, Pz, Qz;
+  T wy, wz;
+  if (ry == 2) {
+    Py = j >> 1;
+    const int nb = (j & 1) ? Py + 1 : Py - 1;
+    Qy = (nb < 0 || nb >= cny) ? Py : nb;
+    wy = (T)0.25;
+  } else {
+    Py = Qy = j;
+    wy = (T)0;
+  }
+  if (rz == 2) {
+    Pz = k >> 1;
+    const int nb = (k & 1) ? Pz + 1 : Pz - 1;
+    Qz = (nb < 0 || nb >= cnz) ? Pz : nb;
+    wz = (T)0.25;
+  } else {
+    Pz = Qz = k;
+    wz = (T)0;
+  }
+  const int X0 = 2 * Q, X1 = X0 + 1;
+  const int Xm = X0 > 0 ? X0 - 1 : X0, Xp = X1 < cnx - 1 ? X1 + 1 : X1;
+  const int64_t sy = cnx, sz = (int64_t)cnx * cny;
+  T o[4][2][2];  // per fine cell, per (z, y) line: the x-interpolated value
+#pragma unroll
+  for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+    for (int dy = 0; dy < 2; dy++) {
+      const int64_t base = (int64_t)(dz ? Qz : Pz) * sz + (int64_t)(dy ? Qy : Py) * sy;
+      const T am = xc[base + Xm], a0 = xc[base + X0], a1 = xc[base + X1], ap = xc[base + Xp];
+      o[0][dz][dy] = a0 + (T)0.25 * (am - a0);
+      o[1][dz][dy] = a0 + (T)0.25 * (a1 - a0);
+      o[2][dz][dy] = a1 + (T)0.25 * (a0 - a1);
+      o[3][dz][dy] = a1 + (T)0.25 * (ap - a1);
+    }
+  T add[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) {
+    const T y0 = o[q][0][0] + wy * (o[q][0][1] - o[q][0][0]);
+    const T y1 = o[q][1][0] + wy * (o[q][1][1] - o[q][1][0]);
+    add[q] = y0 + wz * (y1 - y0);
+  }
+  const int64_t c = f.off + (int64_t)k * f.sz + (int64_t)j * f.sy + 4 * Q;
+  if constexpr (VEC) {
+    float4 v = *reinterpret_cast<const float4 *>(f.x + c);
+    v.x += add[0];
+    v.y += add[1];
+    v.z += add[2];
+    v.w += add[3];
+    *reinterpret_cast<float4 *>(f.x + c) = v;
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; q++) f.x[c + q] += add[q];
   }
 }
 
@@ -905,6 +1031,16 @@ bool restrict_to(const View<T> &f, T *bc, const MgLevelDesc &C, const double *sh
     return false;
   }
   const T inv = (T)(1.0 / (C.r[0] * C.r[1] * C.r[2]));
+  // 3-D grid; planes strided so that the blocks fit the reduction scratch
+  const int gx = (C.n[0] + 31) / 32, gy = (C.n[1] + 7) / 8;
+  const int cap = FOLD != FOLD_NONE ? red.capacity : 8 * sm_count_mg();
+  if (C.r[0] == 2 && (int64_t)gx * gy <= cap) {
+    int gz = C.n[2];
+    while (gz > 1 && (int64_t)gx * gy * gz > cap) gz = (gz + 1) / 2;
+    k_mg_restrict_x2<T, FOLD><<<dim3(gx, gy, gz), dim3(32, 8), 0, stream()>>>(f, bc, C.n[0],
+        C.n[1], C.n[2], C.r[1], C.r[2], inv, shift, st, red.partials, red.ticket);
+    return launched("k_mg_restrict_x2");
+  }
   k_mg_restrict<T, FOLD><<<blocks, kNT, 0, stream()>>>(f, bc, C.n[0], C.n[1], C.n[2], C.r[0],
       C.r[1], C.r[2], inv, shift, st, red.partials, red.ticket);
   return launched("k_mg_restrict");
@@ -913,6 +1049,18 @@ bool restrict_to(const View<T> &f, T *bc, const MgLevelDesc &C, const double *sh
 template <typename T>
 bool prolong_to(const View<T> &f, const T *xc, const MgLevelDesc &C, const MgState *st)
 {
+  if (C.r[0] == 2 && f.nx % 4 == 0) {
+    const dim3 blk(32, 8, 1);
+    const dim3 grid((f.nx / 4 + 31) / 32, (f.ny + 7) / 8, f.nz);
+    const bool vec = sizeof(T) == 4 && f.off % 4 == 0 && f.sy % 4 == 0 && f.sz % 4 == 0;
+    if (vec)
+      k_mg_prolong_x4<T, true><<<grid, blk, 0, stream()>>>(f, xc, C.n[0], C.n[1], C.n[2], C.r[1],
+          C.r[2], st);
+    else
+      k_mg_prolong_x4<T, false><<<grid, blk, 0, stream()>>>(f, xc, C.n[0], C.n[1], C.n[2],
+          C.r[1], C.r[2], st);
+    return launched("k_mg_prolong_x4");
+  }
   if (C.r[0] == 2) {
     const dim3 blk(32, 4, 2);
     const dim3 grid((C.n[0] + 31) / 32, (f.ny + 3) / 4, (f.nz + 1) / 2);
