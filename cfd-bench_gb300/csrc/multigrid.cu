@@ -94,7 +94,7 @@ struct MgHierarchy {
   int guess = 0;        // 1: start from 2 p(n-1) - p(n-2)
   double *p_prev = nullptr;   // padded copy of the previous solve's result (guess >= 1)
   double *p_prev2 = nullptr;  // and of the one before (guess 2)
-  int n_hist = 0;             // earlier solutions kept (0, 1, 2)
+  int *d_hist = nullptr;      // device: earlier solutions kept (0, 1, 2)
   // the solve as one CUDA graph (head, while-loops, tail) for fixed p / rhs
   cudaGraphExec_t graph = nullptr;
   const double *graph_p = nullptr, *graph_rhs = nullptr;
@@ -1172,22 +1172,35 @@ bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero, bool inner_test)
 }
 
 // initial guess by extrapolation in time (whole padded arrays, ghosts
-// included): linear p <- 2 p(n-1) - p(n-2), or with p2 (the solve before)
-// quadratic p <- 3 p(n-1) - 3 p(n-2) + p(n-3); the history shifts by one
+// included): linear p <- 2 p(n-1) - p(n-2), or (quadratic, once two earlier
+// solutions exist) p <- 3 p(n-1) - 3 p(n-2) + p(n-3); the history shifts by
+// one. *hist counts the earlier solutions kept (0, 1, 2) on the device, so the
+// same launches serve host-driven and graph-captured steps.
 __global__ void k_extrapolate(double *__restrict__ p, double *__restrict__ p_prev,
-    double *__restrict__ p2, int64_t n)
+    double *__restrict__ p2, int64_t n, const int *hist, int quadratic)
 {
+  const int h = *hist;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x) {
-    const double cur = p[q], prev = p_prev[q];
-    if (p2) {
+    const double cur = p[q];
+    if (h == 0) {
+      p_prev[q] = cur;
+      continue;
+    }
+    const double prev = p_prev[q];
+    if (quadratic && h >= 2) {
       p[q] = 3.0 * (cur - prev) + p2[q];
-      p2[q] = prev;
     } else {
       p[q] = 2.0 * cur - prev;
     }
+    if (quadratic) p2[q] = prev;
     p_prev[q] = cur;
   }
+}
+
+__global__ void k_hist_advance(int *hist)
+{
+  if (*hist < 2) *hist += 1;
 }
 
 __global__ void k_mx_fold(View<float> e, double *p, int p_sj, int p_sk, const MgState *st)
@@ -1268,6 +1281,9 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
         (size_t)(d->grid.imax + 2) * (d->grid.jmax + 2) * (d->grid.kmax + 2) * sizeof(double);
     if (!cuda_ok(cudaMalloc(&H->p_prev, padded), "cudaMalloc(p_prev)")) return false;
     if (H->guess == 2 && !cuda_ok(cudaMalloc(&H->p_prev2, padded), "cudaMalloc(p_prev2)"))
+      return false;
+    if (!cuda_ok(cudaMalloc(&H->d_hist, sizeof(int)), "cudaMalloc(hist)") ||
+        !cuda_ok(cudaMemset(H->d_hist, 0, sizeof(int)), "hist init"))
       return false;
   }
   H->rtol = x.rtol;
@@ -1378,6 +1394,18 @@ __global__ void k_inner_continue(MgState *st, cudaGraphConditionalHandle h, int 
   const int n = st->inner_it + 1;
   st->inner_it = n;
   cudaGraphSetConditional(h, (st->done == 0 && st->inner_done == 0 && n < inner) ? 1u : 0u);
+}
+
+// the extrapolated warm start of p (mg_guess 1 / 2), before the solve
+bool enqueue_warm_start(MgHierarchy *H, const View<double> &v0, double *p)
+{
+  if (H->guess < 1) return true;
+  const int64_t padded = (int64_t)(v0.nx + 2) * (v0.ny + 2) * (v0.nz + 2);
+  k_extrapolate<<<flat_blocks(padded), kNT, 0, stream()>>>(p, H->p_prev, H->p_prev2, padded,
+      H->d_hist, H->guess == 2 ? 1 : 0);
+  if (!launched("k_extrapolate")) return false;
+  k_hist_advance<<<1, 1, 0, stream()>>>(H->d_hist);
+  return launched("k_hist_advance");
 }
 
 bool enqueue_solve_head(MgHierarchy *H, const View<double> &v0)
@@ -1557,7 +1585,7 @@ bool mg_enqueue(SolverState *ss, double *p, const double *rhs, int queue, int *u
     return false;
   }
   View<double> v0 = padded_view(H->lv[0], p, rhs);
-  if (!enqueue_solve_head(H, v0)) return false;
+  if (!enqueue_warm_start(H, v0, p) || !enqueue_solve_head(H, v0)) return false;
   for (int q = 0; q < queue; q++)
     if (!(H->mode == 0 ? cycle_fp64(H, p, rhs) : cycle_mixed(H, p, rhs))) return false;
   return enqueue_solve_tail(H, v0, p, unconverged, last_cycles);
@@ -1576,7 +1604,8 @@ bool mg_enqueue_loop(SolverState *ss, double *p, const double *rhs, cudaStream_t
     return false;
   }
   View<double> v0 = padded_view(H->lv[0], p, rhs);
-  return enqueue_solve_head(H, v0) && enqueue_units_loop(H, p, rhs, body, H->cap[2]) &&
+  return enqueue_warm_start(H, v0, p) && enqueue_solve_head(H, v0) &&
+         enqueue_units_loop(H, p, rhs, body, H->cap[2]) &&
          enqueue_solve_tail(H, v0, p, unconverged, last_cycles);
 }
 
@@ -1600,25 +1629,7 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
   View<double> v0 = padded_view(H->lv[0], p, rhs);
   const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
   const int blocks = flat_blocks(n0);
-  if (H->guess >= 1) {
-    const int64_t padded = (int64_t)(v0.nx + 2) * (v0.ny + 2) * (v0.nz + 2);
-    if (H->n_hist >= 1) {
-      // quadratic once two earlier solutions exist (guess 2), else linear
-      double *p2 = H->guess == 2 && H->n_hist >= 2 ? H->p_prev2 : nullptr;
-      if (H->guess == 2 && H->n_hist == 1 &&
-          !cuda_ok(cudaMemcpyAsync(H->p_prev2, H->p_prev, padded * sizeof(double),
-                       cudaMemcpyDeviceToDevice, stream()),
-              "keep p(n-2)"))
-        return NAN;
-      k_extrapolate<<<flat_blocks(padded), kNT, 0, stream()>>>(p, H->p_prev, p2, padded);
-      if (!launched("k_extrapolate")) return NAN;
-    } else if (!cuda_ok(cudaMemcpyAsync(H->p_prev, p, padded * sizeof(double),
-                            cudaMemcpyDeviceToDevice, stream()),
-                   "keep p")) {
-      return NAN;
-    }
-    H->n_hist = H->n_hist < 2 ? H->n_hist + 1 : 2;
-  }
+  if (!enqueue_warm_start(H, v0, p)) return NAN;
   // learned warm start: may replace p by the network's guess (never a worse residual)
   if (ss->guess && !guess_before_solve(ss->guess, s->grid, p, rhs)) return NAN;
 
@@ -1753,6 +1764,7 @@ void mg_free(Solver *s, SolverState *ss)
     if (c) cudaStreamDestroy(c);
   if (H->p_prev) cudaFree(H->p_prev);
   if (H->p_prev2) cudaFree(H->p_prev2);
+  if (H->d_hist) cudaFree(H->d_hist);
   if (H->minv64) cudaFree(H->minv64);
   if (H->minv32) cudaFree(H->minv32);
   if (H->d_state) cudaFree(H->d_state);

@@ -50,6 +50,16 @@ def test_batch_matches_single_instances(nusif_lib, tune):
         _compare(batch, cases, steps)
 
 
+def test_batch_warm_start_matches(nusif_lib):
+    """The extrapolated warm starts run inside the captured step too."""
+    from nusif import Batch
+    cases = [dict(c, mg_guess=g) for c, g in zip(_cases(), ["quadratic", "extrapolate",
+                                                             "quadratic", "previous"])]
+    with Batch(cases, tune=False) as batch:
+        batch.step(7)
+        _compare(batch, cases, 7)
+
+
 def test_batch_fixed_queue_long_enough_matches(nusif_lib):
     from nusif import Batch
     cases = _cases()
