@@ -444,10 +444,9 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong_x4(View<T> f, const T *__res
   if (mg_done(st)) return;
   const int Q = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
-  const int k = blockIdx.z;
-  if (4 * Q >= f.nx || j >= f.ny || k >= f.nz) return;
-  int Py, Qy, Pz, Qz;
-  T wy, wz;
+  if (4 * Q >= f.nx || j >= f.ny) return;
+  int Py, Qy;
+  T wy;
   if (ry == 2) {
     Py = j >> 1;
     const int nb = (j & 1) ? Py + 1 : Py - 1;
@@ -457,6 +456,10 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong_x4(View<T> f, const T *__res
     Py = Qy = j;
     wy = (T)0;
   }
+  // planes strided by the grid: a few blocks per SM, each over several planes
+  for (int k = blockIdx.z; k < f.nz; k += gridDim.z) {
+  int Pz, Qz;
+  T wz;
   if (rz == 2) {
     Pz = k >> 1;
     const int nb = (k & 1) ? Pz + 1 : Pz - 1;
@@ -499,6 +502,7 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong_x4(View<T> f, const T *__res
   } else {
 #pragma unroll
     for (int q = 0; q < 4; q++) f.x[c + q] += add[q];
+  }
   }
 }
 
@@ -1051,7 +1055,10 @@ bool prolong_to(const View<T> &f, const T *xc, const MgLevelDesc &C, const MgSta
 {
   if (C.r[0] == 2 && f.nx % 4 == 0) {
     const dim3 blk(32, 8, 1);
-    const dim3 grid((f.nx / 4 + 31) / 32, (f.ny + 7) / 8, f.nz);
+    const int gx = (f.nx / 4 + 31) / 32, gy = (f.ny + 7) / 8;
+    int gz = f.nz;
+    while (gz > 1 && (int64_t)gx * gy * gz > 8 * sm_count_mg()) gz = (gz + 1) / 2;
+    const dim3 grid(gx, gy, gz);
     const bool vec = sizeof(T) == 4 && f.off % 4 == 0 && f.sy % 4 == 0 && f.sz % 4 == 0;
     if (vec)
       k_mg_prolong_x4<T, true><<<grid, blk, 0, stream()>>>(f, xc, C.n[0], C.n[1], C.n[2], C.r[1],
