@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(kNT) k_mg_restrict_x2(View<T> f, T *bc, int cn
   double acc = 0.0;
   if (I < cnx && J < cny) {
     for (int K = blockIdx.z; K < cnz; K += gridDim.z) {
-      T sum = 0;
+      T sum = 0, sq = 0;
       for (int dk = 0; dk < rz; dk++)
         for (int dj = 0; dj < ry; dj++)
 #pragma unroll
@@ -306,8 +306,17 @@ __global__ void __launch_bounds__(kNT) k_mg_restrict_x2(View<T> f, T *bc, int cn
             const int64_t c = f.off + (int64_t)k * f.sz + (int64_t)j * f.sy + i;
             const T r = (f.b[c] - sh) - lap_at(f, f.x, i, j, k, c, f.x[c]);
             sum += r;
-            if (ACCUM) acc += (double)r * (double)r;
+            // FP32 levels: a coarse cell's (at most 8) squares summed in FP32,
+            // then one FP64 add (the FP64 pipe would bound this kernel)
+            if constexpr (sizeof(T) == sizeof(float)) {
+              if (ACCUM) sq += r * r;
+            } else {
+              if (ACCUM) acc += (double)r * (double)r;
+            }
           }
+      if constexpr (sizeof(T) == sizeof(float)) {
+        if (ACCUM) acc += (double)sq;
+      }
       if (bc) bc[((int64_t)K * cny + J) * cnx + I] = sum * inv_count;
     }
   }
