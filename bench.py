@@ -110,7 +110,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -119,9 +119,12 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
-    def stop(self) -> dict:
+    def stop(self, window: tuple[float, float] | None = None) -> dict:
+        """Median SM clock and the throttle reasons seen; with a window (host
+        perf_counter times of the timed region), only the samples inside it
+        (or the one nearest to it when none falls inside)."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -132,7 +135,11 @@ class ClockSampler:
         self.thread.join(timeout=2)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines
+        if window is not None and lines:
+            inside = [x for x in lines if window[0] <= x[0] <= window[1]]
+            lines = inside or [min(lines, key=lambda x: abs(x[0] - 0.5 * (window[0] + window[1])))]
+        for _, ln in lines:
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -181,24 +188,26 @@ def timed_steps(sim, args, stream, local, world):
     """W untimed steps, then K steps between CUDA events (max over ranks)."""
     import torch
     lib = sim.lib
+    clocks = ClockSampler(local)  # started early: nvidia-smi takes a while to report
+    clocks.start()
     for _ in range(args.warmup):
         sim.step()
     torch.cuda.synchronize()
-    clocks = ClockSampler(local)
-    clocks.start()
     launches0 = lib.nusifLaunchCount()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
     e0.record(stream)
     infos = [sim.step() for _ in range(args.steps)]
     e1.record(stream)
     torch.cuda.synchronize()
+    t1 = time.perf_counter()
     if world > 1:
         torch.distributed.barrier()
     launches = lib.nusifLaunchCount() - launches0
-    clk = clocks.stop()
+    clk = clocks.stop((t0, t1))
     ms = max_over_ranks(e0.elapsed_time(e1), world, "cuda")
     return {"ms_per_step": ms / args.steps, "iters": [i.it for i in infos],
             "res": [i.res for i in infos], "launches": int(launches), "clocks": clk}
