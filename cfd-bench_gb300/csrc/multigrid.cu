@@ -100,6 +100,7 @@ struct MgHierarchy {
   const double *graph_p = nullptr, *graph_rhs = nullptr;
   cudaStream_t cap[3] = {};  // capture streams: graph, outer body, inner body
   bool use_graph = true;     // mg_graph: the host-driven solve runs as one graph
+  int tail_l0 = 0;           // first level of the one-kernel coarse tail (0: none)
   // kernels per part of the graph (counted at capture): head, one outer unit
   // without its inner loop, one inner V-cycle, tail
   int n_head = 0, n_outer = 0, n_inner = 0, n_tail = 0;
@@ -786,6 +787,164 @@ __global__ void __launch_bounds__(128) k_mg_direct(const T *__restrict__ minv,
   if (lane == 0) x[row] = acc;
 }
 
+// The coarse end of a V-cycle in one kernel: one block of 1024 threads
+// smooths, restricts, solves the coarsest level and prolongates through every
+// level from `lv[0]` down (the small levels, where a launch per step costs
+// more than the work), with __syncthreads between the steps. Same operations
+// and colour order as the per-level kernels: red-black Gauss-Seidel (first the
+// cells with (i + j + k) even), residual restriction, exact coarsest solve
+// (or sweeps), trilinear prolongation.
+template <typename T>
+struct TailLevel {
+  int n[3];
+  int r[3];  // coarsening ratio from the level above
+  T ex, ey, ez, diag, inv_diag;
+  T *x, *b;
+};
+
+template <typename T>
+struct TailArgs {
+  int count;  // levels in the tail (the last one is the coarsest)
+  TailLevel<T> lv[kMaxLevels];
+  const T *minv;  // exact coarsest solve, or null (coarse_sweeps sweeps)
+  int pre, post, coarse_sweeps, zero_top;
+  const MgState *st;
+};
+
+template <typename T>
+__device__ __forceinline__ View<T> tail_view(const TailLevel<T> &L)
+{
+  View<T> v;
+  v.x = L.x;
+  v.b = L.b;
+  v.nx = L.n[0];
+  v.ny = L.n[1];
+  v.nz = L.n[2];
+  v.sy = L.n[0];
+  v.sz = L.n[0] * L.n[1];
+  v.off = 0;
+  v.ex = L.ex;
+  v.ey = L.ey;
+  v.ez = L.ez;
+  v.diag = L.diag;
+  v.inv_diag = L.inv_diag;
+  return v;
+}
+
+template <typename T>
+__device__ void tail_smooth(const View<T> &v, int count, bool zero_first)
+{
+  const int n = v.nx * v.ny * v.nz;
+  if (count == 0 && zero_first) {
+    for (int q = threadIdx.x; q < n; q += blockDim.x) v.x[q] = (T)0;
+    __syncthreads();
+    return;
+  }
+  for (int s = 0; s < count; s++) {
+    const bool z = zero_first && s == 0;
+    for (int colour = 1; colour >= 0; colour--) {  // colour 1: (i + j + k) even
+      for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int i = q % v.nx, j = (q / v.nx) % v.ny, k = q / (v.nx * v.ny);
+        if (((i + j + k + 1) & 1) != colour) continue;
+        if (z && colour == 1) {
+          v.x[q] = -v.b[q] * v.inv_diag;
+        } else {
+          const T xc = z ? (T)0 : v.x[q];
+          const T r = v.b[q] - lap_at(v, v.x, i, j, k, q, xc);
+          v.x[q] = xc - r * v.inv_diag;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_mg_tail(TailArgs<T> a)
+{
+  if (mg_done(a.st)) return;
+  const int m = a.count;
+  for (int l = 0; l < m - 1; l++) {
+    const View<T> v = tail_view(a.lv[l]);
+    tail_smooth(v, a.pre, l > 0 || a.zero_top);
+    // residual restriction into the next level's right-hand side
+    const TailLevel<T> &C = a.lv[l + 1];
+    const int rx = C.r[0], ry = C.r[1], rz = C.r[2];
+    const T inv = (T)(1.0 / (rx * ry * rz));
+    const int nc = C.n[0] * C.n[1] * C.n[2];
+    for (int q = threadIdx.x; q < nc; q += blockDim.x) {
+      const int I = q % C.n[0], J = (q / C.n[0]) % C.n[1], K = q / (C.n[0] * C.n[1]);
+      T sum = 0;
+      for (int dk = 0; dk < rz; dk++)
+        for (int dj = 0; dj < ry; dj++)
+          for (int di = 0; di < rx; di++) {
+            const int i = I * rx + di, j = J * ry + dj, k = K * rz + dk;
+            const int c = (k * v.ny + j) * v.nx + i;
+            sum += v.b[c] - lap_at(v, v.x, i, j, k, c, v.x[c]);
+          }
+      C.b[q] = sum * inv;
+    }
+    __syncthreads();
+  }
+  // coarsest level
+  {
+    const View<T> v = tail_view(a.lv[m - 1]);
+    const int n = v.nx * v.ny * v.nz;
+    if (a.minv) {
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+      for (int row = warp; row < n; row += nw) {
+        const T *mrow = a.minv + (int64_t)row * n;
+        T acc = 0;
+        for (int q = lane; q < n; q += 32) acc += mrow[q] * v.b[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) v.x[row] = acc;
+      }
+      __syncthreads();
+    } else {
+      tail_smooth(v, a.coarse_sweeps, true);
+    }
+  }
+  for (int l = m - 2; l >= 0; l--) {
+    const View<T> f = tail_view(a.lv[l]);
+    const TailLevel<T> &C = a.lv[l + 1];
+    const int cn[3] = { C.n[0], C.n[1], C.n[2] };
+    const int n = f.nx * f.ny * f.nz;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+      const int fi[3] = { q % f.nx, (q / f.nx) % f.ny, q / (f.nx * f.ny) };
+      int P[3], Q[3];
+      T w[3];
+#pragma unroll
+      for (int ax = 0; ax < 3; ax++) {
+        if (C.r[ax] == 2) {
+          P[ax] = fi[ax] >> 1;
+          const int nb = (fi[ax] & 1) ? P[ax] + 1 : P[ax] - 1;
+          Q[ax] = (nb < 0 || nb >= cn[ax]) ? P[ax] : nb;
+          w[ax] = (T)0.25;
+        } else {
+          P[ax] = Q[ax] = fi[ax];
+          w[ax] = (T)0;
+        }
+      }
+      const int sy = cn[0], sz = cn[0] * cn[1];
+      T vv[2][2];
+#pragma unroll
+      for (int dz = 0; dz < 2; dz++)
+#pragma unroll
+        for (int dy = 0; dy < 2; dy++) {
+          const int base = (dz ? Q[2] : P[2]) * sz + (dy ? Q[1] : P[1]) * sy;
+          const T a0 = C.x[base + P[0]], a1 = C.x[base + Q[0]];
+          vv[dz][dy] = a0 + w[0] * (a1 - a0);
+        }
+      const T y0 = vv[0][0] + w[1] * (vv[0][1] - vv[0][0]);
+      const T y1 = vv[1][0] + w[1] * (vv[1][1] - vv[1][0]);
+      f.x[q] += y0 + w[2] * (y1 - y0);
+    }
+    __syncthreads();
+    tail_smooth(f, a.post, false);
+  }
+}
+
 // mean of the right-hand side, then ||rhs - mean||^2; initialises the state
 __global__ void __launch_bounds__(kNT) k_mg_rhs_sum(View<double> f, MgState *st,
     double *partials, unsigned *ticket)
@@ -1157,6 +1316,41 @@ bool level_sweeps(MgHierarchy *H, int l, View<T> &v, int count, bool zero_first,
   }
 }
 
+// levels l .. nl-1 in one kernel (k_mg_tail)
+template <typename T>
+bool tail_vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero)
+{
+  TailArgs<T> a;
+  a.count = H->nl - l;
+  for (int q = 0; q < a.count; q++) {
+    const MgLevelDesc &L = H->lv[l + q];
+    TailLevel<T> &t = a.lv[q];
+    for (int ax = 0; ax < 3; ax++) {
+      t.n[ax] = L.n[ax];
+      t.r[ax] = L.r[ax];
+    }
+    const double d = 2.0 * (L.ih2[0] + L.ih2[1] + L.ih2[2]);
+    t.ex = (T)L.ih2[0];
+    t.ey = (T)L.ih2[1];
+    t.ez = (T)L.ih2[2];
+    t.diag = (T)d;
+    t.inv_diag = (T)(1.0 / d);
+    t.x = xs[l + q];
+    t.b = bs[l + q];
+  }
+  if constexpr (sizeof(T) == sizeof(double))
+    a.minv = reinterpret_cast<const T *>(H->minv64);
+  else
+    a.minv = reinterpret_cast<const T *>(H->minv32);
+  a.pre = H->pre;
+  a.post = H->post;
+  a.coarse_sweeps = H->coarse_sweeps;
+  a.zero_top = zero ? 1 : 0;
+  a.st = H->d_state;
+  k_mg_tail<T><<<1, 1024, 0, stream()>>>(a);
+  return launched("k_mg_tail");
+}
+
 template <typename T>
 bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero, bool inner_test)
 {
@@ -1164,6 +1358,7 @@ bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero, bool inner_test)
   View<T> v = compact_view<T>(L, xs[l], bs[l]);
   const size_t n = (size_t)L.n[0] * L.n[1] * L.n[2];
   MgState *st = H->d_state;
+  if (H->tail_l0 > 0 && l == H->tail_l0) return tail_vcycle<T>(H, l, xs, bs, zero);
   if (l == H->nl - 1) {
     const T *minv = nullptr;
     if constexpr (sizeof(T) == sizeof(double))
@@ -1308,6 +1503,15 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
     return false;
   }
   H->nl = build_levels(&d->grid, x.mg_levels, H->lv);
+  // the coarse tail: from the first level below the finest with at most
+  // mg_tail cells (0: off), when it leaves at least two levels to it
+  H->tail_l0 = 0;
+  for (int l = 1; x.mg_tail > 0 && l < H->nl - 1; l++) {
+    if ((int64_t)H->lv[l].n[0] * H->lv[l].n[1] * H->lv[l].n[2] <= x.mg_tail) {
+      H->tail_l0 = l;
+      break;
+    }
+  }
   for (int l = 0; l < H->nl; l++) {
     const size_t n = (size_t)H->lv[l].n[0] * H->lv[l].n[1] * H->lv[l].n[2];
     if (H->mode == 0 && l > 0) {

@@ -210,3 +210,18 @@ def test_graph_solve_matches_host_driven_solve(nusif_lib, solver, pre, post):
             assert ia.res == ib.res
         for f in "uvwp":
             np.testing.assert_array_equal(a.field(f), b.field(f))
+
+
+@pytest.mark.parametrize("solver", ["mg", "mg-mixed"])
+def test_one_kernel_coarse_tail_matches(nusif_lib, solver):
+    """mg_tail runs the small levels of each V-cycle in one single-block
+    kernel with the per-level kernels' arithmetic: the same fields bit for bit."""
+    from nusif import Simulation
+    from nusif.params import cavity
+    base = cavity(64, re=700.0, te=1e9, solver=solver, rtol=1e-7, mg_guess="quadratic")
+    with Simulation(dict(base, mg_tail=0)) as a, Simulation(dict(base, mg_tail=4096)) as b:
+        for _ in range(5):
+            ia, ib = a.step(), b.step()
+            assert ia.it == ib.it
+        for f in "uvwp":
+            np.testing.assert_array_equal(a.field(f), b.field(f))
