@@ -397,7 +397,7 @@ def kernel_rooflines(sim, solver, stream, ncell):
     torch.cuda.synchronize()
     out.append(_roof("k_fgh_flux: computeFG (FP64)", "k_fgh_flux",
                      e0.elapsed_time(e1) / reps, 48.0 * ncell, ncell, peak, src,
-                     note="FP64-pipe bound: about 85 FP64 instructions per cell"))
+                     note="FP64-pipe bound: about 73 FP64 instructions per cell"))
     return out
 
 

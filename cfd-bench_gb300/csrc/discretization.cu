@@ -11,6 +11,7 @@
 #include <cstring>
 
 #include "nusif_internal.h"
+#include "fp_bits.cuh"
 #include "reduce.cuh"
 
 namespace nusif {
@@ -43,13 +44,16 @@ __global__ void k_fill(double *a, int64_t n, double value)
 }
 
 // ---- max |u|, |v|, |w| over the padded arrays (discretization.c:391-401) ----
-// Seeded with DBL_MIN like the reference. Block maxima go to partials; the
-// last block folds them.
+// Seeded with DBL_MIN like the reference. Threads compare |x| as integer keys
+// (abs_key: bit patterns of non-negative doubles order like their values, NaN
+// ignored as the reference's `>` test ignores it), so the FP64 pipe stays
+// free; block maxima go to partials as doubles and the last block folds them.
 __global__ void __launch_bounds__(kBlock) k_max3(const double *__restrict__ u,
     const double *__restrict__ v, const double *__restrict__ w, int64_t n,
     double *__restrict__ partials, unsigned *ticket, double *__restrict__ out3)
 {
-  double mu = DBL_MIN, mv = DBL_MIN, mw = DBL_MIN;
+  const unsigned long long seed = (unsigned long long)__double_as_longlong(DBL_MIN);
+  unsigned long long ku = seed, kv = seed, kw = seed;
   const int64_t stride = (int64_t)gridDim.x * kBlock;
   // pairs of doubles (cudaMalloc bases are 256-byte aligned)
   const int64_t npair = n / 2;
@@ -58,15 +62,17 @@ __global__ void __launch_bounds__(kBlock) k_max3(const double *__restrict__ u,
   const double2 *w2 = reinterpret_cast<const double2 *>(w);
   for (int64_t q = blockIdx.x * (int64_t)kBlock + threadIdx.x; q < npair; q += stride) {
     double2 a = __ldg(u2 + q), b = __ldg(v2 + q), c = __ldg(w2 + q);
-    mu = fmax(mu, fmax(fabs(a.x), fabs(a.y)));
-    mv = fmax(mv, fmax(fabs(b.x), fabs(b.y)));
-    mw = fmax(mw, fmax(fabs(c.x), fabs(c.y)));
+    ku = max(ku, max(abs_key(a.x), abs_key(a.y)));
+    kv = max(kv, max(abs_key(b.x), abs_key(b.y)));
+    kw = max(kw, max(abs_key(c.x), abs_key(c.y)));
   }
   if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
-    mu = fmax(mu, fabs(u[n - 1]));
-    mv = fmax(mv, fabs(v[n - 1]));
-    mw = fmax(mw, fabs(w[n - 1]));
+    ku = max(ku, abs_key(u[n - 1]));
+    kv = max(kv, abs_key(v[n - 1]));
+    kw = max(kw, abs_key(w[n - 1]));
   }
+  double mu = __longlong_as_double((long long)ku), mv = __longlong_as_double((long long)kv),
+         mw = __longlong_as_double((long long)kw);
   __shared__ double sm[3][kBlock / 32];
   mu = block_reduce_max<kBlock>(mu, sm[0]);
   mv = block_reduce_max<kBlock>(mv, sm[1]);
@@ -162,13 +168,18 @@ __global__ void k_inflow(Dims g, double inflow, double *__restrict__ u)
 // z-convection of G, whose "minus" half uses V(i,j,k+1) (discretization.c:
 // 543-550, kept). The viscous term joins the face flux (nu*(q_a - q_b) with
 // nu = (1/Re)/h^2), so a cell needs three face fluxes per component instead of
-// six convective halves plus three second differences: about 85 FP64
-// instructions per cell instead of about 140 (GB300's FP64 pipe bounds this
-// kernel). A block owns a 32 x 8 tile of (i, j) columns and marches in k:
-// x-face fluxes pass to the right neighbour by warp shuffle, y-face fluxes to
-// the next row through shared memory, z-face fluxes stay in registers.
+// six convective halves plus three second differences.
+// A face flux c1*cp*(q_a + q_b) + (c2*|cp| + nu)*(q_a - q_b) is evaluated as
+// A*q_a + B*q_b with A = cp*(c1 +- c2) + nu, B = cp*(c1 -+ c2) - nu, the signs
+// picked by the sign bit of cp on the integer pipe: five FP64 instructions per
+// face (the add making cp included) instead of seven, about 73 per cell in
+// all. GB300 issues two FP64 lanes per SM and clock, so the FP64 instruction
+// count, not HBM, bounds this kernel. A block owns a 32 x 8 tile of (i, j)
+// columns and marches in k: x-face fluxes reach the right neighbour and
+// y-face fluxes the next row through shared memory, z-face fluxes stay in
+// registers.
 struct FaceCoef {
-  double c1, c2, nu;  // 0.25/h, gamma*0.25/h, (1/Re)/h^2
+  double P, M, nu;  // (1 + gamma)*0.25/h, (1 - gamma)*0.25/h, (1/Re)/h^2
 };
 
 struct FluxArgs {
@@ -183,8 +194,10 @@ struct FluxArgs {
 // side) and q_b (plus side), transported by the doubled velocity cp
 __device__ __forceinline__ double face_flux(const FaceCoef &a, double cp, double qa, double qb)
 {
-  const double s = qa + qb, d = qa - qb;
-  return fma(fma(a.c2, fabs(cp), a.nu), d, a.c1 * cp * s);
+  const bool neg = __double2hiint(cp) < 0;  // sign bit (an integer test, not DSETP)
+  const double A = fma(cp, neg ? a.M : a.P, a.nu);
+  const double B = fma(cp, neg ? a.P : a.M, -a.nu);
+  return fma(A, qa, B * qb);
 }
 
 struct XFace { double f, g, h; };
@@ -267,10 +280,13 @@ __global__ void __launch_bounds__(kFX *kFY) k_fgh_flux(FluxArgs A, const double 
       // F(imax), G(jmax), H(kmax) are wall faces carrying the velocity (discretization.c:609-651)
       const double sf = (xp.f - xm.f) + (yp.f - ym.f) + (zp.f - zm.f);
       f[c] = (i == g.imax) ? uc : fma(dt, A.gx - sf, uc);
+      // c1*(vc + vt)*(gp - gm) + c2*(vc - vt)*(|gp| + |gm|) as gp*Xp - gm*Xm,
+      // Xp and Xm weighted sums of vc and vt chosen by the signs of gp and gm
       const double vt = __ldg(v + c + sk);
-      const double s = vc + vt, d = vc - vt;
-      const double zconv =
-          fma(A.az.c2 * d, fabs(zp.gc) + fabs(zm.gc), A.az.c1 * s * (zp.gc - zm.gc));
+      const bool np = __double2hiint(zp.gc) < 0, nm = __double2hiint(zm.gc) < 0;
+      const double xpz = fma(np ? A.az.M : A.az.P, vc, (np ? A.az.P : A.az.M) * vt);
+      const double xmz = fma(nm ? A.az.P : A.az.M, vc, (nm ? A.az.M : A.az.P) * vt);
+      const double zconv = fma(zp.gc, xpz, -(zm.gc * xmz));
       const double sg = (xp.g - xm.g) + (yp.g - ym.g) + (zp.gv - zm.gv) + zconv;
       gg[c] = (j == g.jmax) ? vc : fma(dt, A.gy - sg, vc);
       const double sh = (xp.h - xm.h) + (yp.h - ym.h) + (zp.h - zm.h);
@@ -432,8 +448,9 @@ bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, do
   const double iRe = 1.0 / re;
   FaceCoef *fc[3] = { &A.ax, &A.ay, &A.az };
   for (int a = 0; a < 3; a++) {
-    fc[a]->c1 = inv[a] * 0.25;
-    fc[a]->c2 = gamma * inv[a] * 0.25;
+    const double c1 = inv[a] * 0.25, c2 = gamma * inv[a] * 0.25;
+    fc[a]->P = c1 + c2;
+    fc[a]->M = c1 - c2;
     fc[a]->nu = iRe * (inv[a] * inv[a]);
   }
   A.dt = dt;

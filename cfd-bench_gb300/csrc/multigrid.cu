@@ -25,6 +25,7 @@
 #include <cstring>
 #include <vector>
 
+#include "fp_bits.cuh"
 #include "nusif_internal.h"
 #include "reduce.cuh"
 #include "solver_internal.h"
@@ -133,6 +134,22 @@ __global__ void k_zero(T *__restrict__ x, int64_t n)
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x)
     x[q] = (T)0;
+}
+
+// the integer-pipe conversions of the mixed-precision kernels, element-wise
+// (nusifConvertF64ToF32 / nusifConvertF32ToF64)
+__global__ void k_to_f32(const double *__restrict__ x, float *__restrict__ y, int64_t n)
+{
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x)
+    y[q] = to_f32_rn(x[q]);
+}
+
+__global__ void k_to_f64(const float *__restrict__ x, double *__restrict__ y, int64_t n)
+{
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x)
+    y[q] = to_f64(x[q]);
 }
 
 template <typename T>
@@ -361,17 +378,27 @@ __global__ void __launch_bounds__(kNT) k_mx_residual(View<double> f, float *r32,
   const int64_t n = (int64_t)f.nx * f.ny * f.nz;
   const double sh = st->shift;
   double acc = 0.0;
-  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n;
-       q += (int64_t)gridDim.x * kNT) {
-    const int i = (int)(q % f.nx);
-    const int64_t rest = q / f.nx;
-    const int j = (int)(rest % f.ny);
-    const int k = (int)(rest / f.ny);
+  const int64_t q0 = blockIdx.x * (int64_t)kNT + threadIdx.x, stride = (int64_t)gridDim.x * kNT;
+  FlatWalk w(q0, stride, f.nx, f.ny);
+  for (int64_t q = q0; q < n; q += stride, w.advance(f.nx, f.ny)) {
+    const int i = w.i, j = w.j, k = w.k;
     const int64_t c = f.off + (int64_t)k * f.sz + (int64_t)j * f.sy + i;
-    const double r = (f.b[c] - sh) - lap_at(f, f.x, i, j, k, c, f.x[c]);
-    r32[q] = (float)r;
+    const double *x = f.x;
+    const double xc = x[c];
+    const double sx = (i > 0 ? x[c - 1] : xc) + (i < f.nx - 1 ? x[c + 1] : xc);
+    const double sy = (j > 0 ? x[c - f.sy] : xc) + (j < f.ny - 1 ? x[c + f.sy] : xc);
+    const double sz = (k > 0 ? x[c - f.sz] : xc) + (k < f.nz - 1 ? x[c + f.sz] : xc);
+    // r = (b - shift) - A x with the shift folded into the first FMA: eight
+    // FP64 instructions, the norm's FMA the ninth, the FP32 copy on the
+    // integer pipe
+    double t = fma(-f.diag, xc, sh);
+    t = fma(sx, f.ex, t);
+    t = fma(sy, f.ey, t);
+    t = fma(sz, f.ez, t);
+    const double r = f.b[c] - t;
+    r32[q] = to_f32_rn(r);
     if (e_zero) e_zero[q] = 0.0f;
-    acc += r * r;
+    acc = fma(r, r, acc);
   }
   __shared__ double sm[kNT / 32];
   acc = block_reduce_sum<kNT>(acc, sm);
@@ -951,13 +978,10 @@ __global__ void __launch_bounds__(kNT) k_mg_rhs_sum(View<double> f, MgState *st,
 {
   const int64_t n = (int64_t)f.nx * f.ny * f.nz;
   double acc = 0.0;
-  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n;
-       q += (int64_t)gridDim.x * kNT) {
-    const int i = (int)(q % f.nx);
-    const int64_t rest = q / f.nx;
-    const int64_t c = f.off + (rest / f.ny) * f.sz + (rest % f.ny) * f.sy + i;
-    acc += f.b[c];
-  }
+  const int64_t q0 = blockIdx.x * (int64_t)kNT + threadIdx.x, stride = (int64_t)gridDim.x * kNT;
+  FlatWalk w(q0, stride, f.nx, f.ny);
+  for (int64_t q = q0; q < n; q += stride, w.advance(f.nx, f.ny))
+    acc += f.b[f.off + (int64_t)w.k * f.sz + (int64_t)w.j * f.sy + w.i];
   __shared__ double sm[kNT / 32];
   acc = block_reduce_sum<kNT>(acc, sm);
   __shared__ bool last;
@@ -980,12 +1004,10 @@ __global__ void __launch_bounds__(kNT) k_mg_rhs_norm(View<double> f, MgState *st
   const int64_t n = (int64_t)f.nx * f.ny * f.nz;
   const double sh = st->shift;
   double acc = 0.0;
-  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n;
-       q += (int64_t)gridDim.x * kNT) {
-    const int i = (int)(q % f.nx);
-    const int64_t rest = q / f.nx;
-    const int64_t c = f.off + (rest / f.ny) * f.sz + (rest % f.ny) * f.sy + i;
-    const double b = f.b[c] - sh;
+  const int64_t q0 = blockIdx.x * (int64_t)kNT + threadIdx.x, stride = (int64_t)gridDim.x * kNT;
+  FlatWalk w(q0, stride, f.nx, f.ny);
+  for (int64_t q = q0; q < n; q += stride, w.advance(f.nx, f.ny)) {
+    const double b = f.b[f.off + (int64_t)w.k * f.sz + (int64_t)w.j * f.sy + w.i] - sh;
     acc += b * b;
   }
   __shared__ double sm[kNT / 32];
@@ -1418,11 +1440,13 @@ __global__ void k_mx_fold(View<float> e, double *p, int p_sj, int p_sk, const Mg
 {
   if (solve_finished(st)) return;
   const int64_t n = (int64_t)e.nx * e.ny * e.nz;
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
-       q += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(q % e.nx), j = (int)((q / e.nx) % e.ny), k = (int)(q / ((int64_t)e.nx * e.ny));
+  const int64_t q0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  FlatWalk w(q0, stride, e.nx, e.ny);
+  for (int64_t q = q0; q < n; q += stride, w.advance(e.nx, e.ny)) {
+    const int i = w.i, j = w.j, k = w.k;
     const int64_t pc = (int64_t)(k + 1) * p_sk + (int64_t)(j + 1) * p_sj + (i + 1);
-    const double np = p[pc] + (double)e.x[q];
+    const double np = p[pc] + to_f64(e.x[q]);  // widening on the integer pipe, one DADD
     p[pc] = np;
     if (i == 0) p[pc - 1] = np;
     if (i == e.nx - 1) p[pc + 1] = np;
@@ -2046,6 +2070,30 @@ int nusifSmoothRBF32(const float *x, const float *b, float *xout, int nx, int ny
   if (scratch) cudaFree(scratch);
   if (st) cudaFree(st);
   return ok ? NUSIF_OK : NUSIF_ERR_CUDA;
+}
+
+int nusifConvertF64ToF32(const double *x, float *y, long long n)
+{
+  if (!x || !y || n < 0) {
+    fail(NUSIF_ERR_ARG, "nusifConvertF64ToF32: needs device arrays and n >= 0");
+    return NUSIF_ERR_ARG;
+  }
+  if (n == 0) return NUSIF_OK;
+  k_to_f32<<<flat_blocks(n), kNT, 0, stream()>>>(x, y, n);
+  return launched("k_to_f32") && cuda_ok(cudaStreamSynchronize(stream()), "convert")
+             ? NUSIF_OK : NUSIF_ERR_CUDA;
+}
+
+int nusifConvertF32ToF64(const float *x, double *y, long long n)
+{
+  if (!x || !y || n < 0) {
+    fail(NUSIF_ERR_ARG, "nusifConvertF32ToF64: needs device arrays and n >= 0");
+    return NUSIF_ERR_ARG;
+  }
+  if (n == 0) return NUSIF_OK;
+  k_to_f64<<<flat_blocks(n), kNT, 0, stream()>>>(x, y, n);
+  return launched("k_to_f64") && cuda_ok(cudaStreamSynchronize(stream()), "convert")
+             ? NUSIF_OK : NUSIF_ERR_CUDA;
 }
 
 }  // extern "C"

@@ -4,6 +4,8 @@
 // any spin-wait.
 #pragma once
 
+#include <cstdint>
+
 #include <cuda_runtime.h>
 
 namespace nusif {
@@ -28,6 +30,35 @@ __device__ __forceinline__ float warp_sum_f(float v)
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+
+// (i, j, k) of the flat index q = i + nx*(j + ny*k) in a grid-stride loop:
+// the fixed stride is split into its (i, j, k) steps once, and each step of
+// the loop adds them with carries instead of dividing a 64-bit index.
+struct FlatWalk {
+  int i, j, k;
+  int di, dj, dk;
+  __device__ __forceinline__ FlatWalk(int64_t q0, int64_t stride, int nx, int ny)
+  {
+    i = (int)(q0 % nx);
+    const int64_t r = q0 / nx;
+    j = (int)(r % ny);
+    k = (int)(r / ny);
+    di = (int)(stride % nx);
+    const int64_t s = stride / nx;
+    dj = (int)(s % ny);
+    dk = (int)(s / ny);
+  }
+  __device__ __forceinline__ void advance(int nx, int ny)
+  {
+    i += di;
+    const int ci = i >= nx;
+    if (ci) i -= nx;
+    j += dj + ci;
+    const int cj = j >= ny;
+    if (cj) j -= ny;
+    k += dk + cj;
+  }
+};
 
 // linear thread index for 1-, 2- and 3-D blocks
 __device__ __forceinline__ int flat_tid()

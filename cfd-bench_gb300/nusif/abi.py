@@ -126,6 +126,8 @@ SIGNATURES = [
                                      C.POINTER(C.c_float)]),
     ("nusifSmoothRBF32", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                    C.c_int, C.c_double, C.c_double, C.c_double, C.c_int]),
+    ("nusifConvertF64ToF32", C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
+    ("nusifConvertF32ToF64", C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
     ("nusifSolverSetGuessNet", C.c_int, [C.POINTER(Solver), C.c_void_p]),
     ("nusifSolverRecordPair", C.c_int, [C.POINTER(Solver), C.c_void_p, C.c_void_p]),
     ("nusifSolverGuessStats", C.c_int, [C.POINTER(Solver), C.POINTER(C.c_int),

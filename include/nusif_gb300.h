@@ -228,6 +228,12 @@ NUSIF_API const char *nusifVersion(void);
  * No reference counterpart (the smoother of the corrected multigrid). */
 NUSIF_API int nusifSmoothRBF32(const float *x, const float *b, float *xout, int nx, int ny, int nz,
     double hx, double hy, double hz, int sweeps);
+/* The FP64 <-> FP32 conversions of the mixed-precision kernels (computed on
+ * the integer pipe: round to nearest even, and exact widening), element-wise
+ * on n device values. Results are those of the hardware conversions. No
+ * reference counterpart. */
+NUSIF_API int nusifConvertF64ToF32(const double *x, float *y, long long n);
+NUSIF_API int nusifConvertF32ToF64(const float *x, double *y, long long n);
 
 /* Learned pressure warm start (no reference counterpart). A 3-level 3D U-Net
  * (16/32/64 channels, 243,473 parameters; BF16 weights and activations, FP32

@@ -225,3 +225,54 @@ def test_one_kernel_coarse_tail_matches(nusif_lib, solver):
             assert ia.it == ib.it
         for f in "uvwp":
             np.testing.assert_array_equal(a.field(f), b.field(f))
+
+
+def _bits_f64(rng, n):
+    """Random binary64 patterns over every exponent (normal, subnormal, zero,
+    infinity, NaN), with round-to-nearest ties and near-ties for binary32."""
+    b = rng.integers(0, 2 ** 63, size=n, dtype=np.int64).astype(np.uint64)
+    b |= rng.integers(0, 2, size=n, dtype=np.uint64) << np.uint64(63)
+    exp = rng.integers(0, 2048, size=n, dtype=np.uint64)
+    near = rng.integers(0, 2, size=n).astype(bool)  # half of them near the binary32 range
+    exp[near] = rng.integers(860, 1160, size=int(near.sum()), dtype=np.uint64)
+    b = (b & ~(np.uint64(0x7ff) << np.uint64(52))) | (exp << np.uint64(52))
+    low = np.uint64(0x1fffffff)
+    ties = rng.integers(0, 4, size=n)
+    b[ties == 0] = (b[ties == 0] & ~low) | np.uint64(0x10000000)          # exact ties
+    b[ties == 1] = (b[ties == 1] & ~low) | np.uint64(0x10000001)          # just above
+    b[ties == 2] = (b[ties == 2] & ~low) | np.uint64(0x0fffffff)          # just below
+    edge = np.array([0, 1 << 63, 0x7ff0000000000000, 0xfff0000000000000, 0x7ff8000000000000,
+                     0x47efffffe0000000, 0x47efffffefffffff, 0x47effffff0000000,
+                     0x3810000000000000, 0x380fffffffffffff, 0x36a0000000000000,
+                     0x3690000000000000, 0x0000000000000001, 0x000fffffffffffff],
+                    dtype=np.uint64)
+    return np.concatenate([edge, b]).view(np.float64)
+
+
+def test_integer_pipe_conversions_match_hardware(nusif_lib):
+    """The mixed-precision kernels convert FP64 <-> FP32 with integer
+    operations; on random bit patterns of every class (ties, float subnormal
+    and overflow range, zeros, infinities, NaN) they return exactly what the
+    hardware conversion returns."""
+    import ctypes as C
+
+    import torch
+    rng = np.random.default_rng(77)
+    x = torch.from_numpy(_bits_f64(rng, 1 << 21)).cuda()
+    y = torch.empty(x.shape, dtype=torch.float32, device="cuda")
+    assert nusif_lib.nusifConvertF64ToF32(C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
+                                          x.numel()) == 0
+    want = x.float()
+    nan = torch.isnan(want)
+    assert torch.equal(torch.isnan(y), nan)
+    assert torch.equal(y[~nan].view(torch.int32), want[~nan].view(torch.int32))
+    # widening: every float class, from random 32-bit patterns
+    f = torch.from_numpy(rng.integers(0, 2 ** 32, size=1 << 21, dtype=np.uint64)
+                         .astype(np.uint32).view(np.float32)).cuda()
+    d = torch.empty(f.shape, dtype=torch.float64, device="cuda")
+    assert nusif_lib.nusifConvertF32ToF64(C.c_void_p(f.data_ptr()), C.c_void_p(d.data_ptr()),
+                                          f.numel()) == 0
+    want = f.double()
+    nan = torch.isnan(want)
+    assert torch.equal(torch.isnan(d), nan)
+    assert torch.equal(d[~nan].view(torch.int64), want[~nan].view(torch.int64))
