@@ -160,7 +160,10 @@ class ClockSampler:
 # configuration's cycle), and for the mixed-precision solver up to 4 FP32
 # V-cycles per FP64 residual (V(1,1), V(3,3), V(4,4) and 2 or 8 inner cycles
 # measured slower at 256^3 with the quadratic warm start)
-MG_SHAPE = {"mg": (2, 2, 4), "mg-mixed": (2, 2, 4)}
+# (pre-sweeps, post-sweeps, most FP32 V-cycles per FP64 residual); the FP32
+# correction of mg-mixed stops at 0.9 rtol (the library default mg_theta), so
+# three V(2,2) cycles usually end a 256^3 solve with the FP64 check passing
+MG_SHAPE = {"mg": (2, 2, 4), "mg-mixed": (2, 2, 3)}
 
 
 def bench_case(n: int, solver: str, itermax: int | None = None,
@@ -301,7 +304,8 @@ def run_gpu(args, rank, world, local):
                    "cells": ncell, "solver": solver, "tolerance": tol,
                    "learned_warm_start": False,
                    "initial_guess": (args.guess if solver in ("mg", "mg-mixed") else "previous"),
-                   "v_cycle": ("V(%d,%d), up to %d FP32 V-cycles per FP64 residual"
+                   "v_cycle": ("V(%d,%d), up to %d FP32 V-cycles per FP64 residual, "
+                               "FP32 correction to 0.9 rtol"
                                % MG_SHAPE["mg-mixed"] if solver == "mg-mixed" else
                                "V(%d,%d)" % MG_SHAPE["mg"][:2] if solver == "mg" else None),
                    "solve_launch": ("host-driven launches" if args.no_graph else

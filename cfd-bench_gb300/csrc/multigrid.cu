@@ -42,7 +42,8 @@ struct MgState {
   double res2;       // last FP64 ||b - Ap||^2
   double tol2;       // rtol^2 * nb2
   double rtol2;
-  double tol_inner;  // mg-mixed: (rtol/2)^2 * nb2, target of the FP32 correction
+  double theta2;     // mg-mixed: (target of the FP32 correction / rtol)^2
+  double tol_inner;  // mg-mixed: theta2 * rtol^2 * nb2, target of the FP32 correction
   double res2_inner; // mg-mixed: last ||r32 - A e||^2
   int cycles;        // V-cycles done
   int outer;         // mg-mixed: FP64 residual evaluations that found work to do
@@ -92,6 +93,7 @@ struct MgHierarchy {
   double rtol = 1e-6;
   int last_cycles = 0;  // queue size of the previous solve (cycles, or outer iterations)
   int inner = 4;        // mg-mixed: most FP32 V-cycles per FP64 residual
+  double theta = 0.9;   // mg-mixed: FP32 correction target as a fraction of rtol
   int guess = 0;        // 1: start from 2 p(n-1) - p(n-2)
   double *p_prev = nullptr;   // padded copy of the previous solve's result (guess >= 1)
   double *p_prev2 = nullptr;  // and of the one before (guess 2)
@@ -588,118 +590,132 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
     int kc, const MgState *st)
 {
   if (mg_done(st)) return;
-  __shared__ __align__(16) float xo[4][kRY][kWX];   // x_old planes, slot = plane & 3
-  __shared__ __align__(16) float bs[3][kBYr][kWX];  // b planes, slot = plane % 3
-  __shared__ float xr[3][kBYr][kQX];                // new odd values, slot = plane % 3
-  const float *__restrict__ xold = v.x;
-  const float *__restrict__ b = v.b;
+  constexpr int PX = kRY * kWX, PB = kBYr * kWX, PR = kBYr * kQX;  // floats per staged plane
+  __shared__ __align__(16) float xo[4 * PX];  // x_old planes, slot = plane & 3
+  __shared__ __align__(16) float bs[3 * PB];  // b planes, slot = plane mod 3
+  __shared__ float xr[3 * PR];                // new first-colour values, slot = plane mod 3
   const int nx = v.nx, ny = v.ny, nz = v.nz;
   const int i0 = blockIdx.x * kSX, j0 = blockIdx.y * kSY;
   const int k0 = blockIdx.z * kc, k1 = min(k0 + kc, nz);
   const int tid = threadIdx.x;
+  // staging: this thread's 16-byte chunk (row cr, chunk cc) of a staged plane
   constexpr int kChunks = kWX / 4;  // 18 per row
-  // this thread's chunk: row cr, chunk cc, and its offset inside a plane
   const int cr = tid / kChunks, cc = tid - cr * kChunks;
   const int gic = min(max(i0 - 4 + 4 * cc, 0), nx - 4);
-  const bool x_lane = cr < kRY, b_lane = cr < kBYr;
+  const bool x_lane = !ZERO && cr < kRY, b_lane = cr < kBYr;
   const int gjx = min(max(j0 - 2 + cr, 0), ny - 1), gjb = min(max(j0 - 1 + cr, 0), ny - 1);
-  const int64_t xoff = (int64_t)gjx * v.sy + gic, boff = (int64_t)gjb * v.sy + gic;
-  auto stage = [&](int kx, int kb) {
-    if (!ZERO && x_lane && kx <= k1 + 1) {
-      const int kk = min(max(kx, 0), nz - 1);  // mirror planes beyond the walls
-      cp_async16(&xo[kx & 3][cr][4 * cc], xold + (int64_t)kk * v.sz + xoff);
-    }
-    if (b_lane && kb >= 0 && kb < nz)
-      cp_async16(&bs[kb % 3][cr][4 * cc], b + (int64_t)kb * v.sz + boff);
-  };
+  const float *__restrict__ gxs = v.x + (int64_t)gjx * v.sy + gic;
+  const float *__restrict__ gbs = v.b + (int64_t)gjb * v.sy + gic;
+  const int so = cr * kWX + 4 * cc;  // the chunk's offset in a staged plane (x and b rows alike)
+  const int64_t sz = v.sz;
   // staged columns of the ghosts beyond the x walls, when inside this window
   const bool wl = i0 == 0;             // gi = -1 at column 3, wall column 4
   const int wr = nx - (i0 - 4);        // column of gi = nx
   const bool patch = !ZERO && (wl || wr < kWX);
   if (ZERO) {
-    for (int q = tid; q < 4 * kRY * kWX; q += 256) (&xo[0][0][0])[q] = 0.0f;
+    for (int q = tid; q < 4 * PX; q += 256) xo[q] = 0.0f;
   }
-  // this thread's first-colour items (at most two per plane): row, pair index
-  constexpr int kRow = kQX / 2;           // 33 per row
-  constexpr int kOdd = kRow * kBYr;       // 330 per plane
-  const int qa = tid, qb = tid + 256;
-  const int lja = qa / kRow, pia = qa - lja * kRow;
-  const int ljb = qb / kRow, pib = qb - ljb * kRow;
-  const bool has_b = qb < kOdd;
-  const int gja = j0 - 1 + lja, gjb2 = j0 - 1 + ljb;
-  const bool rowa = gja >= 0 && gja < ny, rowb = gjb2 >= 0 && gjb2 < ny;
-  // second-colour item: one cell per thread
+  // first-colour items (two at most per plane): offsets in a plane with the
+  // colour bit lsb = 0, the colour bit at even k, and in-domain flags per bit
+  constexpr int kRow = kQX / 2;      // 33 pairs per row
+  constexpr int kOdd = kRow * kBYr;  // 330 per plane
+  int ox[2], orr[2], par[2];
+  bool ok0[2], ok1[2];
+#pragma unroll
+  for (int s = 0; s < 2; s++) {
+    const int q = tid + 256 * s;
+    const int lj = q / kRow, pi = q - lj * kRow;
+    const int gj = j0 - 1 + lj, gi = i0 - 1 + 2 * pi;
+    const bool row = q < kOdd && gj >= 0 && gj < ny;
+    ox[s] = (lj + 1) * kWX + 2 * pi + 3;  // x_old column li + 3, row lj + 1 (b: row lj)
+    orr[s] = lj * kQX + 2 * pi;
+    par[s] = ((i0 + gj) & 1) ^ 1;
+    ok0[s] = row && gi >= 0 && gi < nx;
+    ok1[s] = row && gi + 1 >= 0 && gi + 1 < nx;
+  }
+  const bool has_b = tid + 256 < kOdd;
+  // second-colour item: the cell pair (2 ep, 2 ep + 1) of tile row tj
   const int tj = tid >> 5, ep = tid & 31;
   const int gje = j0 + tj;
   const bool even_ok = gje < ny && i0 + 2 * ep < nx;
+  const int epar = (i0 + gje + 1) & 1;         // its position in the pair at even planes
+  const int oxe = (tj + 2) * kWX + 2 * ep + 4;  // x_old of the pair's first cell
+  const int obe = (tj + 1) * kWX + 2 * ep + 4;  // b of the pair's first cell
+  const int ore = (tj + 1) * kQX + 2 * ep + 1;  // new first-colour values around it
+  float *__restrict__ gout = xnew + (int64_t)min(gje, ny - 1) * v.sy + i0 + 2 * ep;
   const float ex = v.ex, ey = v.ey, ez = v.ez, dg = v.diag, idg = v.inv_diag;
 
-  stage(k0 - 2, -1);
-  stage(k0 - 1, k0 - 1);
-  stage(k0, -1);
+  int m = (k0 + 2) % 3;  // slot of plane k0 - 1 in the mod-3 rings
+  if (x_lane) {
+#pragma unroll
+    for (int kx = k0 - 2; kx <= k0; kx++)
+      cp_async16(xo + (kx & 3) * PX + so, gxs + (int64_t)min(max(kx, 0), nz - 1) * sz);
+  }
+  if (b_lane && k0 >= 1) cp_async16(bs + m * PB + so, gbs + (int64_t)(k0 - 1) * sz);
   cp_async_commit();
   for (int k = k0 - 1; k <= k1; k++) {
-    stage(k + 2, k + 1);  // prefetch: completes during this plane's arithmetic
+    const int mp = m == 2 ? 0 : m + 1, mm = m == 0 ? 2 : m - 1;  // slots of k + 1, k - 1
+    // prefetch x_old(k + 2) and b(k + 1): completes during this plane's arithmetic
+    if (x_lane && k + 2 <= k1 + 1)
+      cp_async16(xo + ((k + 2) & 3) * PX + so, gxs + (int64_t)min(k + 2, nz - 1) * sz);
+    if (b_lane && k + 1 < nz) cp_async16(bs + mp * PB + so, gbs + (int64_t)(k + 1) * sz);
     cp_async_commit();
-    cp_async_wait<1>();   // all but the prefetch: x_old(k+1), b(k) are in
+    cp_async_wait<1>();  // all but the prefetch: x_old(k + 1), b(k) are in
     __syncthreads();
+    const float *xk = xo + (k & 3) * PX;
+    const float *xkm = xo + ((k + 3) & 3) * PX;
+    const float *xkp = xo + ((k + 1) & 3) * PX;
     if (patch) {  // ghost columns of plane k (read as x-neighbours below)
       if (tid < kRY) {
-        float *row = xo[k & 3][tid];
+        float *row = xo + (k & 3) * PX + tid * kWX;
         if (wl) row[3] = row[4];
         if (wr < kWX) row[wr] = row[wr - 1];
       }
       __syncthreads();
     }
     {
-      // k >= -1: (k + 3) % 3 is plane k's slot, never negative
-      float(*rq)[kQX] = xr[(k + 3) % 3];
-      const float(*xk)[kWX] = xo[k & 3];
-      const float(*xkm)[kWX] = xo[(k + 3) & 3];
-      const float(*xkp)[kWX] = xo[(k + 1) & 3];
-      const float(*bk)[kWX] = bs[(k + 3) % 3];
+      const float *bk = bs + m * PB;
+      float *rq = xr + m * PR;
       const bool kin = k >= 0 && k < nz;
-      auto red = [&](int lj, int pi, int gj, bool rowin) {
-        const int li = 2 * pi + (((i0 + gj + k) & 1) ^ 1);  // first-colour column
-        const int gi = i0 - 1 + li;
-        const int si = li + 3, sj = lj + 1;  // staged x_old column / row
-        const float xc = xk[sj][si];
-        const float sx = xk[sj][si - 1] + xk[sj][si + 1];
-        const float sy = xk[sj - 1][si] + xk[sj + 1][si];
-        const float sz = xkm[sj][si] + xkp[sj][si];
-        const float lap = sx * ex + sy * ey + sz * ez - dg * xc;
-        const float relaxed = xc - (bk[lj][si] - lap) * idg;
-        const bool in = kin && rowin && gi >= 0 && gi < nx;
-        rq[lj][li] = in ? relaxed : xc;
-      };
-      red(lja, pia, gja, rowa);
-      if (has_b) red(ljb, pib, gjb2, rowb);
+      const int kp = k & 1;
+#pragma unroll
+      for (int s = 0; s < 2; s++) {
+        if (s == 1 && !has_b) break;
+        const int lsb = par[s] ^ kp;
+        const int o = ox[s] + lsb;
+        const float xc = xk[o];
+        const float sx = xk[o - 1] + xk[o + 1];
+        const float sy = xk[o - kWX] + xk[o + kWX];
+        const float sz2 = xkm[o] + xkp[o];
+        const float lap = sx * ex + sy * ey + sz2 * ez - dg * xc;
+        const float relaxed = xc - (bk[o - kWX] - lap) * idg;
+        const bool in = kin && (lsb ? ok1[s] : ok0[s]);
+        rq[orr[s] + lsb] = in ? relaxed : xc;
+      }
     }
     __syncthreads();
-    // second-colour cells of plane k-1 on the tile: one cell pair per thread,
-    // both cells stored as one 8-byte vector
+    // second-colour cells of plane k - 1 on the tile, both cells of the pair
+    // stored as one 8-byte vector
     const int ke = k - 1;
     if (ke >= k0 && ke < k1 && even_ok) {
-      const float(*rm)[kQX] = xr[(ke + 2) % 3];
-      const float(*r0)[kQX] = xr[ke % 3];
-      const float(*rp)[kQX] = xr[(ke + 1) % 3];
-      const float(*xe)[kWX] = xo[ke & 3];
-      const float(*be)[kWX] = bs[ke % 3];
-      const int e = (i0 + gje + ke + 1) & 1;  // position of the second-colour cell in the pair
-      const int te = 2 * ep + e;
-      const int li = te + 1, lj = tj + 1;
-      const float xc = xe[lj + 1][te + 4];
-      const float sx = r0[lj][li - 1] + r0[lj][li + 1];
-      const float sy = r0[lj - 1][li] + r0[lj + 1][li];
-      const float sz = rm[lj][li] + rp[lj][li];
-      const float lap = sx * ex + sy * ey + sz * ez - dg * xc;
-      const float even = xc - (be[lj][te + 4] - lap) * idg;
-      const float odd = r0[lj][(te ^ 1) + 1];
+      const float *r0 = xr + mm * PR;  // plane ke
+      const float *rm = xr + mp * PR;  // plane ke - 1 (= k + 1 mod 3)
+      const float *rp = xr + m * PR;   // plane ke + 1
+      const float *be = bs + mm * PB;
+      const int e = epar ^ (ke & 1);
+      const int o = ore + e;
+      const float xc = xkm[oxe + e];  // x_old(ke) sits in plane k - 1's slot
+      const float sx = r0[o - 1] + r0[o + 1];
+      const float sy = r0[o - kQX] + r0[o + kQX];
+      const float sz2 = rm[o] + rp[o];
+      const float lap = sx * ex + sy * ey + sz2 * ez - dg * xc;
+      const float even = xc - (be[obe + e] - lap) * idg;
+      const float odd = r0[o + 1 - 2 * e];
       const float2 pair = e ? make_float2(odd, even) : make_float2(even, odd);
-      *reinterpret_cast<float2 *>(xnew + (int64_t)ke * v.sz + (int64_t)gje * v.sy + i0 + 2 * ep) =
-          pair;
+      *reinterpret_cast<float2 *>(gout + (int64_t)ke * sz) = pair;
     }
     __syncthreads();
+    m = mp;
   }
   cp_async_wait<0>();
 }
@@ -1023,7 +1039,7 @@ __global__ void __launch_bounds__(kNT) k_mg_rhs_norm(View<double> f, MgState *st
   if (threadIdx.x == 0) {
     st->nb2 = total;
     st->tol2 = st->rtol2 * total;
-    st->tol_inner = 0.25 * st->rtol2 * total;
+    st->tol_inner = st->theta2 * st->rtol2 * total;
     st->res2 = 0.0;
     st->res2_inner = 0.0;
     st->cycles = 0;
@@ -1476,7 +1492,7 @@ bool cycle_fp64(MgHierarchy *H, double *p, const double *rhs)
 
 // one outer iteration of mixed-precision refinement: FP64 residual (and stop
 // test), up to `inner` FP32 V-cycles on A e = r (stopped on the device once
-// ||r - A e|| <= rtol/2 ||b||), p += e in FP64
+// ||r - A e|| <= theta * rtol ||b||, theta the key mg_theta), p += e in FP64
 bool cycle_mixed(MgHierarchy *H, double *p, const double *rhs)
 {
   MgState *st = H->d_state;
@@ -1506,6 +1522,7 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
   H->coarse_sweeps = x.mg_coarse_sweeps;
   H->maxcycles = x.mg_maxcycles;
   H->inner = x.mg_inner < 1 ? 1 : x.mg_inner;
+  H->theta = x.mg_theta;
   H->guess = x.mg_guess == 1 || x.mg_guess == 2 ? x.mg_guess : 0;
   H->use_graph = x.mg_graph != 0;
   for (cudaStream_t &c : H->cap)
@@ -1522,8 +1539,9 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
       return false;
   }
   H->rtol = x.rtol;
-  if (H->pre < 0 || H->post < 0 || H->coarse_sweeps < 0 || H->maxcycles < 1 || !(H->rtol >= 0)) {
-    fail(NUSIF_ERR_ARG, "multigrid: invalid mg_pre/mg_post/mg_coarse/mg_cycles/rtol");
+  if (H->pre < 0 || H->post < 0 || H->coarse_sweeps < 0 || H->maxcycles < 1 || !(H->rtol >= 0) ||
+      !(H->theta > 0 && H->theta <= 1)) {
+    fail(NUSIF_ERR_ARG, "multigrid: invalid mg_pre/mg_post/mg_coarse/mg_cycles/rtol/mg_theta");
     return false;
   }
   H->nl = build_levels(&d->grid, x.mg_levels, H->lv);
@@ -1599,11 +1617,12 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
 
 namespace {
 
-__global__ void k_mg_state_init(MgState *st, double rtol2, int maxcycles)
+__global__ void k_mg_state_init(MgState *st, double rtol2, double theta2, int maxcycles)
 {
   MgState s;
   memset(&s, 0, sizeof(s));
   s.rtol2 = rtol2;
+  s.theta2 = theta2;
   s.maxcycles = maxcycles;
   *st = s;
 }
@@ -1654,7 +1673,8 @@ bool enqueue_warm_start(MgHierarchy *H, const View<double> &v0, double *p)
 
 bool enqueue_solve_head(MgHierarchy *H, const View<double> &v0)
 {
-  k_mg_state_init<<<1, 1, 0, stream()>>>(H->d_state, H->rtol * H->rtol, H->maxcycles);
+  k_mg_state_init<<<1, 1, 0, stream()>>>(H->d_state, H->rtol * H->rtol, H->theta * H->theta,
+                                         H->maxcycles);
   if (!launched("k_mg_state_init")) return false;
   const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
   const int blocks = flat_blocks(n0);
@@ -1895,6 +1915,7 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
   } else {
     memset(h, 0, sizeof(*h));
     h->rtol2 = H->rtol * H->rtol;
+    h->theta2 = H->theta * H->theta;
     h->maxcycles = H->maxcycles;
     if (!cuda_ok(cudaMemcpyAsync(H->d_state, h, sizeof(MgState), cudaMemcpyHostToDevice,
                      stream()),
