@@ -67,6 +67,9 @@ __global__ void k_step_dt(const double *max3, BatchDev *bd, double dtBound, doub
   }
   bd->sc.dt = dt;
   bd->sc.idt = 1.0 / dt;
+  bd->sc.rx = (1.0 / dx) * bd->sc.idt;
+  bd->sc.ry = (1.0 / dy) * bd->sc.idt;
+  bd->sc.rz = (1.0 / dz) * bd->sc.idt;
   bd->sc.fx = dt / dx;
   bd->sc.fy = dt / dy;
   bd->sc.fz = dt / dz;

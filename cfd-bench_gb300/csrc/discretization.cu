@@ -44,16 +44,17 @@ __global__ void k_fill(double *a, int64_t n, double value)
 }
 
 // ---- max |u|, |v|, |w| over the padded arrays (discretization.c:391-401) ----
-// Seeded with DBL_MIN like the reference. Threads compare |x| as integer keys
-// (abs_key: bit patterns of non-negative doubles order like their values, NaN
-// ignored as the reference's `>` test ignores it), so the FP64 pipe stays
-// free; block maxima go to partials as doubles and the last block folds them.
+// Seeded with DBL_MIN like the reference. Threads compare |x| as bit patterns
+// on the integer pipe (abs_max_key: non-negative doubles order like their
+// bits, NaN skipped as the reference's `>` test skips it), so the FP64 pipe
+// stays free; block maxima go to partials as doubles and the last block
+// folds them.
 __global__ void __launch_bounds__(kBlock) k_max3(const double *__restrict__ u,
     const double *__restrict__ v, const double *__restrict__ w, int64_t n,
     double *__restrict__ partials, unsigned *ticket, double *__restrict__ out3)
 {
-  const unsigned long long seed = (unsigned long long)__double_as_longlong(DBL_MIN);
-  unsigned long long ku = seed, kv = seed, kw = seed;
+  // running maxima as bit-pattern pairs (high, low), seeded with DBL_MIN
+  unsigned uh = 0x00100000u, ul = 0u, vh = 0x00100000u, vl = 0u, wh = 0x00100000u, wl = 0u;
   const int64_t stride = (int64_t)gridDim.x * kBlock;
   // pairs of doubles (cudaMalloc bases are 256-byte aligned)
   const int64_t npair = n / 2;
@@ -62,17 +63,20 @@ __global__ void __launch_bounds__(kBlock) k_max3(const double *__restrict__ u,
   const double2 *w2 = reinterpret_cast<const double2 *>(w);
   for (int64_t q = blockIdx.x * (int64_t)kBlock + threadIdx.x; q < npair; q += stride) {
     double2 a = __ldg(u2 + q), b = __ldg(v2 + q), c = __ldg(w2 + q);
-    ku = max(ku, max(abs_key(a.x), abs_key(a.y)));
-    kv = max(kv, max(abs_key(b.x), abs_key(b.y)));
-    kw = max(kw, max(abs_key(c.x), abs_key(c.y)));
+    abs_max_key(uh, ul, a.x);
+    abs_max_key(uh, ul, a.y);
+    abs_max_key(vh, vl, b.x);
+    abs_max_key(vh, vl, b.y);
+    abs_max_key(wh, wl, c.x);
+    abs_max_key(wh, wl, c.y);
   }
   if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
-    ku = max(ku, abs_key(u[n - 1]));
-    kv = max(kv, abs_key(v[n - 1]));
-    kw = max(kw, abs_key(w[n - 1]));
+    abs_max_key(uh, ul, u[n - 1]);
+    abs_max_key(vh, vl, v[n - 1]);
+    abs_max_key(wh, wl, w[n - 1]);
   }
-  double mu = __longlong_as_double((long long)ku), mv = __longlong_as_double((long long)kv),
-         mw = __longlong_as_double((long long)kw);
+  double mu = __hiloint2double((int)uh, (int)ul), mv = __hiloint2double((int)vh, (int)vl),
+         mw = __hiloint2double((int)wh, (int)wl);
   __shared__ double sm[3][kBlock / 32];
   mu = block_reduce_max<kBlock>(mu, sm[0]);
   mv = block_reduce_max<kBlock>(mv, sm[1]);
@@ -301,17 +305,19 @@ __global__ void __launch_bounds__(kFX *kFY) k_fgh_flux(FluxArgs A, const double 
 }
 
 // ---- RHS (discretization.c:334-362) ----
-__global__ void __launch_bounds__(kBlock) k_rhs(Dims g, double ix, double iy, double iz,
-    double idt_arg, const StepScalars *sp, const double *__restrict__ f,
+// ((F - F_w)/dx + (G - G_s)/dy + (H - H_b)/dz)/dt with 1/(h dt) folded into
+// one factor per axis: six FP64 instructions per cell instead of seven.
+__global__ void __launch_bounds__(kBlock) k_rhs(Dims g, double rx_arg, double ry_arg,
+    double rz_arg, const StepScalars *sp, const double *__restrict__ f,
     const double *__restrict__ gg, const double *__restrict__ h, double *__restrict__ rhs)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
   if (i > g.imax || j > g.jmax || k > g.kmax) return;
-  const double idt = sp ? sp->idt : idt_arg;
+  const double rx = sp ? sp->rx : rx_arg, ry = sp ? sp->ry : ry_arg, rz = sp ? sp->rz : rz_arg;
   const int64_t c = (int64_t)k * g.sk + (int64_t)j * g.sj + i;
-  rhs[c] = ((f[c] - f[c - 1]) * ix + (gg[c] - gg[c - g.sj]) * iy + (h[c] - h[c - g.sk]) * iz) * idt;
+  rhs[c] = (f[c] - f[c - 1]) * rx + (gg[c] - gg[c - g.sj]) * ry + (h[c] - h[c - g.sk]) * rz;
 }
 
 // ---- adaptUV (discretization.c:654-681) ----
@@ -472,8 +478,9 @@ bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, do
 bool launch_rhs(const Dims &g, double dt, double dx, double dy, double dz, const double *f,
     const double *gg, const double *h, double *rhs, const StepScalars *sp)
 {
+  const double idt = sp ? 0.0 : 1.0 / dt;
   k_rhs<<<cell_grid(g, kCellBlock), kCellBlock, 0, stream()>>>(
-      g, 1.0 / dx, 1.0 / dy, 1.0 / dz, sp ? 0.0 : 1.0 / dt, sp, f, gg, h, rhs);
+      g, (1.0 / dx) * idt, (1.0 / dy) * idt, (1.0 / dz) * idt, sp, f, gg, h, rhs);
   return launched("k_rhs");
 }
 

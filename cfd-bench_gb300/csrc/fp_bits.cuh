@@ -13,9 +13,9 @@
 //    gets exactly the hardware's result.
 //  - to_f64: exact widening; zeros and normal floats here, the rest by the
 //    hardware conversion.
-//  - abs_key: |x| as an unsigned integer whose order is the numeric order of
-//    |x| (non-negative doubles order like their bit patterns); NaN maps to 0,
-//    so a maximum over keys ignores NaN as fmax does.
+//  - abs_max_key: a running maximum of |x| kept as its bit pattern
+//    (non-negative doubles order like their bit patterns); NaN is skipped,
+//    as fmax and the reference's `>` test skip it.
 #pragma once
 
 #include <cstdint>
@@ -52,10 +52,17 @@ __device__ __forceinline__ double to_f64(float x)
   return (double)x;
 }
 
-__device__ __forceinline__ unsigned long long abs_key(double x)
+// running maximum of |x| as the pair (high word, low word) of its bit
+// pattern, compared lexicographically with 32-bit operations (a 64-bit
+// integer maximum would use the FP64 pipe's 64-bit datapath)
+__device__ __forceinline__ void abs_max_key(unsigned &mh, unsigned &ml, double x)
 {
-  const unsigned long long k = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
-  return k > 0x7ff0000000000000ull ? 0ull : k;
+  const unsigned h = (unsigned)__double2hiint(x) & 0x7fffffffu;
+  const unsigned l = (unsigned)__double2loint(x);
+  const bool nan = h > 0x7ff00000u || (h == 0x7ff00000u && l != 0u);
+  const bool gt = !nan && (h > mh || (h == mh && l > ml));
+  mh = gt ? h : mh;
+  ml = gt ? l : ml;
 }
 
 }  // namespace nusif

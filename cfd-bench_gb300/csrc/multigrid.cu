@@ -1991,6 +1991,12 @@ bool mg_time_kernel(SolverState *ss, const double *p, const double *rhs, int whi
         k_mx_residual<<<flat_blocks(n0), kNT, 0, stream()>>>(v0, H->b32[0], tst, H->red.partials,
             H->red.ticket, 0, nullptr);
         ok = launched("k_mx_residual");
+      } else if (which == 2 && H->mode == 1) {
+        // one whole FP32 V-cycle from zero on the current fine right-hand side
+        MgState *keep = H->d_state;
+        H->d_state = tst;
+        ok = vcycle<float>(H, 0, H->x32, H->b32, true, false);
+        H->d_state = keep;
       } else if (H->mode == 1) {
         ok = fused_sweeps(H, 0, 1, false, tst);  // one whole sweep
       } else {

@@ -75,6 +75,7 @@ void reduce_scratch_free(ReduceScratch &r);
 // as the host path: dt (computeTimestep), 1/dt (computeRHS), dt/h (adaptUV).
 struct StepScalars {
   double dt, idt, fx, fy, fz;
+  double rx, ry, rz;  // (1/dx)(1/dt), (1/dy)(1/dt), (1/dz)(1/dt): computeRHS factors
   double t;  // simulated time after the last completed step
   int nt;    // completed steps
   int pad;
