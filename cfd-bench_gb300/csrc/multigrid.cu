@@ -591,9 +591,13 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
 {
   if (mg_done(st)) return;
   constexpr int PX = kRY * kWX, PB = kBYr * kWX, PR = kBYr * kQX;  // floats per staged plane
-  __shared__ __align__(16) float xo[4 * PX];  // x_old planes, slot = plane & 3
-  __shared__ __align__(16) float bs[3 * PB];  // b planes, slot = plane mod 3
-  __shared__ float xr[3 * PR];                // new first-colour values, slot = plane mod 3
+  // Five x_old slots and four b and first-colour slots: the copies a thread
+  // issues for plane k + 3 never land in a slot that a slower warp may still
+  // read for the second colour of plane k - 1, so each plane needs two
+  // barriers, not three.
+  __shared__ __align__(16) float xo[5 * PX];  // x_old planes, slot = plane mod 5
+  __shared__ __align__(16) float bs[4 * PB];  // b planes, slot = plane & 3
+  __shared__ float xr[4 * PR];                // new first-colour values, slot = plane & 3
   const int nx = v.nx, ny = v.ny, nz = v.nz;
   const int i0 = blockIdx.x * kSX, j0 = blockIdx.y * kSY;
   const int k0 = blockIdx.z * kc, k1 = min(k0 + kc, nz);
@@ -613,7 +617,7 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
   const int wr = nx - (i0 - 4);        // column of gi = nx
   const bool patch = !ZERO && (wl || wr < kWX);
   if (ZERO) {
-    for (int q = tid; q < 4 * PX; q += 256) xo[q] = 0.0f;
+    for (int q = tid; q < 5 * PX; q += 256) xo[q] = 0.0f;
   }
   // first-colour items (two at most per plane): offsets in a plane with the
   // colour bit lsb = 0, the colour bit at even k, and in-domain flags per bit
@@ -645,37 +649,42 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
   float *__restrict__ gout = xnew + (int64_t)min(gje, ny - 1) * v.sy + i0 + 2 * ep;
   const float ex = v.ex, ey = v.ey, ez = v.ez, dg = v.diag, idg = v.inv_diag;
 
-  int m = (k0 + 2) % 3;  // slot of plane k0 - 1 in the mod-3 rings
+  int m5 = (k0 + 9) % 5;  // x_old slot of plane k0 - 1 (k0 - 1 >= -1)
   if (x_lane) {
+    int s5 = m5 == 0 ? 4 : m5 - 1;  // slot of plane k0 - 2
 #pragma unroll
-    for (int kx = k0 - 2; kx <= k0; kx++)
-      cp_async16(xo + (kx & 3) * PX + so, gxs + (int64_t)min(max(kx, 0), nz - 1) * sz);
+    for (int kx = k0 - 2; kx <= k0; kx++) {
+      cp_async16(xo + s5 * PX + so, gxs + (int64_t)min(max(kx, 0), nz - 1) * sz);
+      s5 = s5 == 4 ? 0 : s5 + 1;
+    }
   }
-  if (b_lane && k0 >= 1) cp_async16(bs + m * PB + so, gbs + (int64_t)(k0 - 1) * sz);
+  if (b_lane && k0 >= 1) cp_async16(bs + ((k0 - 1) & 3) * PB + so, gbs + (int64_t)(k0 - 1) * sz);
   cp_async_commit();
-  for (int k = k0 - 1; k <= k1; k++) {
-    const int mp = m == 2 ? 0 : m + 1, mm = m == 0 ? 2 : m - 1;  // slots of k + 1, k - 1
+  for (int k = k0 - 1; k <= k1; k++, m5 = m5 == 4 ? 0 : m5 + 1) {
+    // x_old slots of planes k - 1, k, k + 1, k + 2 (m5 is plane k's)
+    const int sm = m5 == 0 ? 4 : m5 - 1, sp = m5 == 4 ? 0 : m5 + 1;
+    const int sn = sp == 4 ? 0 : sp + 1;
     // prefetch x_old(k + 2) and b(k + 1): completes during this plane's arithmetic
     if (x_lane && k + 2 <= k1 + 1)
-      cp_async16(xo + ((k + 2) & 3) * PX + so, gxs + (int64_t)min(k + 2, nz - 1) * sz);
-    if (b_lane && k + 1 < nz) cp_async16(bs + mp * PB + so, gbs + (int64_t)(k + 1) * sz);
+      cp_async16(xo + sn * PX + so, gxs + (int64_t)min(k + 2, nz - 1) * sz);
+    if (b_lane && k + 1 < nz) cp_async16(bs + ((k + 1) & 3) * PB + so, gbs + (int64_t)(k + 1) * sz);
     cp_async_commit();
     cp_async_wait<1>();  // all but the prefetch: x_old(k + 1), b(k) are in
     __syncthreads();
-    const float *xk = xo + (k & 3) * PX;
-    const float *xkm = xo + ((k + 3) & 3) * PX;
-    const float *xkp = xo + ((k + 1) & 3) * PX;
+    const float *xk = xo + m5 * PX;
+    const float *xkm = xo + sm * PX;
+    const float *xkp = xo + sp * PX;
     if (patch) {  // ghost columns of plane k (read as x-neighbours below)
       if (tid < kRY) {
-        float *row = xo + (k & 3) * PX + tid * kWX;
+        float *row = xo + m5 * PX + tid * kWX;
         if (wl) row[3] = row[4];
         if (wr < kWX) row[wr] = row[wr - 1];
       }
       __syncthreads();
     }
     {
-      const float *bk = bs + m * PB;
-      float *rq = xr + m * PR;
+      const float *bk = bs + (k & 3) * PB;
+      float *rq = xr + (k & 3) * PR;
       const bool kin = k >= 0 && k < nz;
       const int kp = k & 1;
 #pragma unroll
@@ -698,10 +707,10 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
     // stored as one 8-byte vector
     const int ke = k - 1;
     if (ke >= k0 && ke < k1 && even_ok) {
-      const float *r0 = xr + mm * PR;  // plane ke
-      const float *rm = xr + mp * PR;  // plane ke - 1 (= k + 1 mod 3)
-      const float *rp = xr + m * PR;   // plane ke + 1
-      const float *be = bs + mm * PB;
+      const float *r0 = xr + (ke & 3) * PR;        // plane ke
+      const float *rm = xr + ((ke + 3) & 3) * PR;  // plane ke - 1
+      const float *rp = xr + (k & 3) * PR;         // plane ke + 1
+      const float *be = bs + (ke & 3) * PB;
       const int e = epar ^ (ke & 1);
       const int o = ore + e;
       const float xc = xkm[oxe + e];  // x_old(ke) sits in plane k - 1's slot
@@ -714,8 +723,8 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
       const float2 pair = e ? make_float2(odd, even) : make_float2(even, odd);
       *reinterpret_cast<float2 *>(gout + (int64_t)ke * sz) = pair;
     }
-    __syncthreads();
-    m = mp;
+    // no barrier here: the next plane's copies go to slots no warp reads now,
+    // and its first barrier orders everything else
   }
   cp_async_wait<0>();
 }
@@ -1983,20 +1992,43 @@ bool mg_time_kernel(SolverState *ss, const double *p, const double *rhs, int whi
   cudaEventCreate(&e1);
   View<double> v0 = padded_view(H->lv[0], pcopy, rhs);
   const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
+  // which >= 2 (mg-mixed): one FP32 V-cycle from level which - 2 down, from
+  // zero on that level's current right-hand side, captured once as a CUDA
+  // graph and replayed (as inside a solve)
+  cudaGraph_t vg = nullptr;
+  cudaGraphExec_t vge = nullptr;
+  if (ok && which >= 2) {
+    if (H->mode != 1 || which - 2 >= H->nl) {
+      fail(NUSIF_ERR_ARG, "nusifTimeKernel: which >= 2 times mg-mixed V-cycles from a level");
+      ok = false;
+    } else {
+      // copies above are ordered before the capture stream's work
+      ok = cuda_ok(cudaStreamSynchronize(stream()), "timing sync");
+      MgState *keep = H->d_state;
+      cudaStream_t lib = stream();
+      const unsigned long long c0 = launch_count();
+      H->d_state = tst;
+      ok = ok && cuda_ok(cudaStreamBeginCapture(H->cap[0], cudaStreamCaptureModeThreadLocal),
+                     "timing capture");
+      nusifSetStream(H->cap[0]);
+      const bool built = ok && vcycle<float>(H, which - 2, H->x32, H->b32, true, false);
+      nusifSetStream(lib);
+      set_launch_count(c0);  // the capture ran nothing
+      ok = ok && cuda_ok(cudaStreamEndCapture(H->cap[0], &vg), "timing capture end") && built &&
+           cuda_ok(cudaGraphInstantiate(&vge, vg, 0), "timing graph");
+      H->d_state = keep;
+    }
+  }
   if (ok) {
     // one untimed launch, then the timed ones
     for (int q = 0; q <= reps && ok; q++) {
       if (q == 1) cudaEventRecord(e0, stream());
-      if (which == 1 && H->mode == 1) {
+      if (which >= 2) {
+        ok = cuda_ok(cudaGraphLaunch(vge, stream()), "timing graph launch");
+      } else if (which == 1 && H->mode == 1) {
         k_mx_residual<<<flat_blocks(n0), kNT, 0, stream()>>>(v0, H->b32[0], tst, H->red.partials,
             H->red.ticket, 0, nullptr);
         ok = launched("k_mx_residual");
-      } else if (which == 2 && H->mode == 1) {
-        // one whole FP32 V-cycle from zero on the current fine right-hand side
-        MgState *keep = H->d_state;
-        H->d_state = tst;
-        ok = vcycle<float>(H, 0, H->x32, H->b32, true, false);
-        H->d_state = keep;
       } else if (H->mode == 1) {
         ok = fused_sweeps(H, 0, 1, false, tst);  // one whole sweep
       } else {
@@ -2014,6 +2046,8 @@ bool mg_time_kernel(SolverState *ss, const double *p, const double *rhs, int whi
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  if (vge) cudaGraphExecDestroy(vge);
+  if (vg) cudaGraphDestroy(vg);
   if (tst) cudaFree(tst);
   if (pcopy) cudaFree(pcopy);
   return ok;

@@ -215,8 +215,9 @@ NUSIF_API unsigned long long nusifLaunchCount(void);
  * launches of one fine-level kernel, timed with CUDA events on the library
  * stream; which = 0 the fine smoother (mg-mixed: one whole FP32 red-black
  * sweep; mg: one colour pass of the FP64 smoother), 1 the FP64 residual of
- * mg-mixed, 2 one whole FP32 V-cycle of mg-mixed (all levels, from zero, on
- * the fine right-hand side of the last solve).
+ * mg-mixed, 2 + l one FP32 V-cycle of mg-mixed from level l (0 = finest)
+ * down, from zero on that level's right-hand side of the last solve, replayed
+ * as a captured CUDA graph.
  * Works on scratch copies: p and rhs are only read. */
 NUSIF_API int nusifTimeKernel(Solver *s, const double *p, const double *rhs, int which, int reps,
     double *ms_out);
