@@ -19,10 +19,12 @@
 //            fine post-smoothing pass (iterative refinement).
 // Every kernel returns at once when the device-side done flag is up, so the
 // host queues whole cycles in chunks and reads the state once per chunk.
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <vector>
 
 #include "fp_bits.cuh"
@@ -104,6 +106,7 @@ struct MgHierarchy {
   cudaStream_t cap[3] = {};  // capture streams: graph, outer body, inner body
   bool use_graph = true;     // mg_graph: the host-driven solve runs as one graph
   int tail_l0 = 0;           // first level of the one-kernel coarse tail (0: none)
+  int kc[kMaxLevels] = {};   // planes per block of each level's one-kernel sweep (0: by rule)
   // kernels per part of the graph (counted at capture): head, one outer unit
   // without its inner loop, one inner V-cycle, tail
   int n_head = 0, n_outer = 0, n_inner = 0, n_tail = 0;
@@ -1323,6 +1326,80 @@ bool coarse_solve(const View<T> &v, int nsweeps, const MgState *st, const T *min
 // restriction folds the residual norm for the mixed-precision inner stop.
 // `count` whole red-black sweeps of an FP32 level with the one-kernel sweep;
 // each swaps the level's current and ping-pong buffers (x32[l] stays current)
+// Planes per block (chunk depth) of the one-kernel sweep. A block walks
+// kc + 2 planes (the first-colour planes just outside its chunk are
+// recomputed) and the grid runs in ceil(blocks / resident) waves; the rule
+// minimises waves * (kc + 2). The chunk depth changes only how the work is
+// split: every cell is computed the same way, so results do not depend on it.
+int sweep_chunk_rule(const MgLevelDesc &L)
+{
+  static int resident = 0;
+  if (resident == 0) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_sweep<false>, 256, 0);
+    resident = (per_sm > 0 ? per_sm : 1) * sm_count_mg();
+  }
+  const int gx = (L.n[0] + kSX - 1) / kSX, gy = (L.n[1] + kSY - 1) / kSY, nz = L.n[2];
+  int kc = nz;
+  int64_t best = -1;
+  for (int c = 1; c <= nz; c++) {
+    const int64_t blocks = (int64_t)gx * gy * ((nz + c - 1) / c);
+    const int64_t cost = ((blocks + resident - 1) / resident) * (int64_t)(c + 2);
+    if (best < 0 || cost < best) {
+      best = cost;
+      kc = c;
+    }
+  }
+  return kc;
+}
+
+// Autotuner: the chunk depth of the one-kernel sweep measured on a level's own
+// arrays (x, b read; xb written), once per level size (cached): the fastest
+// of a few depths over three timed sweeps each, the rule's depth among them.
+int sweep_chunk_tuned(const MgLevelDesc &L, float *x, float *xb, float *b)
+{
+  static std::map<std::array<int, 3>, int> cache;
+  const std::array<int, 3> key = { L.n[0], L.n[1], L.n[2] };
+  const auto hit = cache.find(key);
+  if (hit != cache.end()) return hit->second;
+  const int rule = sweep_chunk_rule(L);
+  static MgState *idle = nullptr;  // done = inner_done = 0
+  if (!idle && (cudaMalloc(&idle, sizeof(MgState)) != cudaSuccess ||
+                cudaMemset(idle, 0, sizeof(MgState)) != cudaSuccess)) {
+    idle = nullptr;
+    cudaGetLastError();
+    return rule;
+  }
+  const int gx = (L.n[0] + kSX - 1) / kSX, gy = (L.n[1] + kSY - 1) / kSY, nz = L.n[2];
+  const View<float> v = compact_view<float>(L, x, b);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int kc = rule;
+  float best = -1.0f;
+  const int cand[] = { rule, 1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64 };
+  for (const int c : cand) {
+    if (c > nz) continue;
+    const dim3 grid(gx, gy, (nz + c - 1) / c);
+    k_rbgs_sweep<false><<<grid, 256, 0, stream()>>>(v, xb, c, idle);  // warm-up
+    cudaEventRecord(e0, stream());
+    for (int r = 0; r < 3; r++) k_rbgs_sweep<false><<<grid, 256, 0, stream()>>>(v, xb, c, idle);
+    cudaEventRecord(e1, stream());
+    float ms = 0.0f;
+    if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
+      break;
+    if (best < 0 || ms < best) {
+      best = ms;
+      kc = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (cudaGetLastError() != cudaSuccess) return rule;
+  cache[key] = kc;
+  return kc;
+}
+
 bool fused_sweeps(MgHierarchy *H, int l, int count, bool zero_first, const MgState *st)
 {
   const MgLevelDesc &L = H->lv[l];
@@ -1331,8 +1408,7 @@ bool fused_sweeps(MgHierarchy *H, int l, int count, bool zero_first, const MgSta
     return sweeps<float>(v, count, zero_first, nullptr, st);
   }
   const int gx = (L.n[0] + kSX - 1) / kSX, gy = (L.n[1] + kSY - 1) / kSY;
-  int kc = 32;
-  while (kc > 4 && (int64_t)gx * gy * ((L.n[2] + kc - 1) / kc) < 8 * sm_count_mg()) kc >>= 1;
+  const int kc = H->kc[l] > 0 ? H->kc[l] : sweep_chunk_rule(L);
   const dim3 grid(gx, gy, (L.n[2] + kc - 1) / kc);
   for (int s = 0; s < count; s++) {
     const View<float> v = compact_view<float>(L, H->x32[l], H->b32[l]);
@@ -1576,6 +1652,10 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
       if (!cuda_ok(cudaMalloc(&H->b32[l], n * sizeof(float)), "cudaMalloc(mg b32)")) return false;
       cudaMemset(H->x32[l], 0, n * sizeof(float));
       cudaMemset(H->x32b[l], 0, n * sizeof(float));
+      cudaMemset(H->b32[l], 0, n * sizeof(float));
+      if (H->lv[l].n[0] % 4 == 0 && l < H->nl - 1)
+        H->kc[l] = x.mg_chunk > 0 ? x.mg_chunk
+                                  : sweep_chunk_tuned(H->lv[l], H->x32[l], H->x32b[l], H->b32[l]);
     }
   }
   // coarsest level: exact solve when mg_coarse is 0 and the level is small

@@ -37,6 +37,7 @@ struct Extras {
   int mg_guess = 0;          // initial guess: 0 previous p, 1 linear, 2 quadratic extrapolation in time
   int mg_graph = 1;          // 1: each solve is one CUDA graph launch (while-loops on the device)
   int mg_tail = 0;           // levels of at most this many cells run as one kernel (0: off)
+  int mg_chunk = 0;          // planes per block of the FP32 one-kernel sweep (0: autotuned)
   int mg_maxcycles = 100;
 };
 Extras *extras_for(const Parameter *p, bool create);

@@ -212,6 +212,23 @@ def test_graph_solve_matches_host_driven_solve(nusif_lib, solver, pre, post):
             np.testing.assert_array_equal(a.field(f), b.field(f))
 
 
+@pytest.mark.parametrize("chunk", [1, 3, 7, 64])
+def test_sweep_chunk_depth_does_not_change_results(nusif_lib, chunk):
+    """The FP32 one-kernel sweep's planes per block (autotuned by default,
+    forced here with mg_chunk) only splits the work: every cell is computed
+    the same way, so the fields are the same bit for bit."""
+    from nusif import Simulation
+    from nusif.params import cavity
+    base = cavity((64, 40, 48), re=800.0, te=1e9, solver="mg-mixed", rtol=1e-7,
+                  mg_guess="quadratic")
+    with Simulation(dict(base, mg_chunk=0)) as a, Simulation(dict(base, mg_chunk=chunk)) as b:
+        for _ in range(4):
+            ia, ib = a.step(), b.step()
+            assert ia.it == ib.it and ia.res == ib.res
+        for f in "uvwp":
+            np.testing.assert_array_equal(a.field(f), b.field(f))
+
+
 @pytest.mark.parametrize("solver", ["mg", "mg-mixed"])
 def test_one_kernel_coarse_tail_matches(nusif_lib, solver):
     """mg_tail runs the small levels of each V-cycle in one single-block
