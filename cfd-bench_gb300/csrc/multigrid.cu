@@ -19,6 +19,7 @@
 //            fine post-smoothing pass (iterative refinement).
 // Every kernel returns at once when the device-side done flag is up, so the
 // host queues whole cycles in chunks and reads the state once per chunk.
+#include <algorithm>
 #include <array>
 #include <cmath>
 #include <cstdio>
@@ -341,6 +342,118 @@ __global__ void __launch_bounds__(kNT) k_mg_restrict_x2(View<T> f, T *bc, int cn
         if (ACCUM) acc += (double)sq;
       }
       if (bc) bc[((int64_t)K * cny + J) * cnx + I] = sum * inv_count;
+    }
+  }
+  if (!ACCUM) return;
+  __shared__ double sm[kNT / 32];
+  acc = block_reduce_sum<kNT>(acc, sm);
+  __shared__ bool last;
+  const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (flat_tid() == 0) {
+    partials[bid] = acc;
+    last = ticket_is_last(ticket);
+  }
+  __syncthreads();
+  if (!last) return;
+  const double total = fold_partials<kNT>(partials, gridDim.x * gridDim.y * gridDim.z, sm);
+  if (flat_tid() == 0) {
+    const int c = st->cycles + 1;
+    st->cycles = c;
+    if (FOLD == FOLD_OUTER) {
+      st->res2 = total;
+      st->done = (total <= st->tol2) || (c >= st->maxcycles);
+    } else {
+      st->res2_inner = total;
+      st->inner_done = total <= st->tol_inner;
+    }
+    *ticket = 0;
+  }
+}
+
+// FP32 levels halved on every axis (rows of even length, no shift): one
+// thread per coarse column (I, J) walks a contiguous chunk of coarse planes.
+// A fine plane is held as 4 rows x 4 columns (rows 2J-1 .. 2J+2, columns
+// 2I-1 .. 2I+2; a neighbour beyond a wall is the cell itself, so the clamped
+// index gives it): each row comes as one 8-byte load and its outer columns
+// from the neighbouring lanes, and the planes shared by consecutive fine
+// planes stay in registers. Same arithmetic and summation order as
+// k_mg_restrict_x2<float>, with 12 vector loads per coarse cell instead of 64
+// scalar ones.
+template <int FOLD>
+__global__ void __launch_bounds__(kNT) k_mg_restrict_f32(View<float> f, float *bc, int cnx,
+    int cny, int cnz, int kcz, float inv_count, MgState *st, double *partials, unsigned *ticket)
+{
+  constexpr bool ACCUM = FOLD != FOLD_NONE;
+  if (mg_done(st)) return;
+  const int lane = threadIdx.x;  // blockDim.x == 32: a warp is one coarse row
+  const int I = blockIdx.x * 32 + lane, J = blockIdx.y * 8 + threadIdx.y;
+  const bool in = I < cnx && J < cny;
+  const int i0 = 2 * min(I, cnx - 1), j0 = 2 * min(J, cny - 1);  // loads stay in bounds
+  const bool has_l = i0 > 0, has_r = i0 + 2 < f.nx;
+  int64_t roff[4];
+#pragma unroll
+  for (int r = 0; r < 4; r++) roff[r] = (int64_t)min(max(j0 - 1 + r, 0), f.ny - 1) * f.sy + i0;
+  const float *__restrict__ x = f.x;
+  const float *__restrict__ b = f.b;
+  const float ex = f.ex, ey = f.ey, ez = f.ez, dg = f.diag;
+  auto load_plane = [&](float(&v)[4][4], int k) {
+    const int64_t ko = f.off + (int64_t)min(max(k, 0), f.nz - 1) * f.sz;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const float2 a = *reinterpret_cast<const float2 *>(x + ko + roff[r]);
+      float lv = __shfl_up_sync(0xffffffffu, a.y, 1);
+      float rv = __shfl_down_sync(0xffffffffu, a.x, 1);
+      if (lane == 0 && has_l) lv = x[ko + roff[r] - 1];
+      if (lane == 31 && has_r) rv = x[ko + roff[r] + 2];
+      v[r][0] = has_l ? lv : a.x;
+      v[r][1] = a.x;
+      v[r][2] = a.y;
+      v[r][3] = has_r ? rv : a.y;
+    }
+  };
+  auto resid = [&](const float(&vm)[4][4], const float(&vc)[4][4], const float(&vp)[4][4],
+                   int kf, float &sum, float &sq) {
+    const int64_t kb = f.off + (int64_t)kf * f.sz;
+#pragma unroll
+    for (int dj = 0; dj < 2; dj++) {
+      const float2 bb = *reinterpret_cast<const float2 *>(b + kb + roff[1 + dj]);
+#pragma unroll
+      for (int di = 0; di < 2; di++) {
+        const int rj = 1 + dj, ci = 1 + di;
+        const float xc = vc[rj][ci];
+        const float sx = vc[rj][ci - 1] + vc[rj][ci + 1];
+        const float sy = vc[rj - 1][ci] + vc[rj + 1][ci];
+        const float sz = vm[rj][ci] + vp[rj][ci];
+        const float lap = sx * ex + sy * ey + sz * ez - dg * xc;
+        const float r = (di ? bb.y : bb.x) - lap;
+        sum += r;
+        if (ACCUM) sq += r * r;
+      }
+    }
+  };
+  double acc = 0.0;
+  const int K0 = blockIdx.z * kcz, K1 = min(K0 + kcz, cnz);
+  if (K0 < K1) {
+    float p0[4][4], p1[4][4], p2[4][4], p3[4][4];
+    load_plane(p0, 2 * K0 - 1);
+    load_plane(p1, 2 * K0);
+    for (int K = K0; K < K1; K++) {
+      float sum = 0.0f, sq = 0.0f;
+      load_plane(p2, 2 * K + 1);
+      resid(p0, p1, p2, 2 * K, sum, sq);
+      load_plane(p3, 2 * K + 2);
+      resid(p1, p2, p3, 2 * K + 1, sum, sq);
+      if (in) {
+        bc[((int64_t)K * cny + J) * cnx + I] = sum * inv_count;
+        if (ACCUM) acc += to_f64(sq);
+      }
+#pragma unroll
+      for (int r = 0; r < 4; r++)
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          p0[r][c] = p2[r][c];
+          p1[r][c] = p3[r][c];
+        }
     }
   }
   if (!ACCUM) return;
@@ -1256,6 +1369,17 @@ bool restrict_to(const View<T> &f, T *bc, const MgLevelDesc &C, const double *sh
   // 3-D grid; planes strided so that the blocks fit the reduction scratch
   const int gx = (C.n[0] + 31) / 32, gy = (C.n[1] + 7) / 8;
   const int cap = FOLD != FOLD_NONE ? red.capacity : 8 * sm_count_mg();
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (!shift && C.r[0] == 2 && C.r[1] == 2 && C.r[2] == 2 && f.off % 2 == 0 && f.sy % 2 == 0 &&
+        f.sz % 2 == 0 && (int64_t)gx * gy <= cap) {
+      int gz = (int)std::min<int64_t>(C.n[2], cap / ((int64_t)gx * gy));
+      const int kcz = (C.n[2] + gz - 1) / gz;
+      gz = (C.n[2] + kcz - 1) / kcz;
+      k_mg_restrict_f32<FOLD><<<dim3(gx, gy, gz), dim3(32, 8), 0, stream()>>>(f, bc, C.n[0],
+          C.n[1], C.n[2], kcz, inv, st, red.partials, red.ticket);
+      return launched("k_mg_restrict_f32");
+    }
+  }
   if (C.r[0] == 2 && (int64_t)gx * gy <= cap) {
     int gz = C.n[2];
     while (gz > 1 && (int64_t)gx * gy * gz > cap) gz = (gz + 1) / 2;
