@@ -661,6 +661,90 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong_x4(View<T> f, const T *__res
   }
 }
 
+// x_f += trilinear interpolation of x_c on FP32 levels halved on every axis
+// with fine rows of a multiple of four cells (16-byte aligned): one thread per
+// four consecutive fine cells of a row walks a chunk of coarse planes K and
+// updates fine planes 2K and 2K+1. The x-interpolated values of the two
+// coarse rows it needs are kept for coarse planes K-1, K, K+1, so each coarse
+// plane is read once per thread, as one 8-byte load per row with the outer
+// columns from the neighbouring lanes. Same interpolation order as
+// k_mg_prolong_x4 (x, then y, then z).
+__global__ void __launch_bounds__(kNT) k_mg_prolong_f32(View<float> f, const float *__restrict__ xc,
+    int cnx, int cny, int cnz, int kcz, const MgState *st)
+{
+  if (mg_done(st)) return;
+  const int lane = threadIdx.x;  // blockDim.x == 32: a warp is one fine row
+  const int Qraw = blockIdx.x * 32 + lane, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (j >= f.ny) return;  // whole warps: a warp shares one j
+  const int nq = f.nx / 4;
+  const bool in = Qraw < nq;
+  const int Q = min(Qraw, nq - 1);  // loads stay in bounds
+  const int X0 = 2 * Q, X1 = X0 + 1;
+  const bool has_m = X0 > 0, has_p = X1 < cnx - 1;
+  const int Py = j >> 1;
+  const int ny_ = (j & 1) ? Py + 1 : Py - 1;
+  const int Qy = (ny_ < 0 || ny_ >= cny) ? Py : ny_;
+  const int64_t sy = cnx, sz = (int64_t)cnx * cny;
+  const float w = 0.25f;
+  // y-interpolated values of the four fine cells for one coarse plane
+  auto plane = [&](float(&y)[4], int K) {
+    const int Kc = min(max(K, 0), cnz - 1);
+    float o[2][4];
+#pragma unroll
+    for (int dy = 0; dy < 2; dy++) {
+      const int64_t base = (int64_t)Kc * sz + (int64_t)(dy ? Qy : Py) * sy;
+      const float2 a = *reinterpret_cast<const float2 *>(xc + base + X0);
+      float am = __shfl_up_sync(0xffffffffu, a.y, 1);
+      float ap = __shfl_down_sync(0xffffffffu, a.x, 1);
+      if (lane == 0 && has_m) am = xc[base + X0 - 1];
+      if (lane == 31 && has_p) ap = xc[base + X1 + 1];
+      if (!has_m) am = a.x;
+      if (!has_p) ap = a.y;
+      o[dy][0] = a.x + w * (am - a.x);
+      o[dy][1] = a.x + w * (a.y - a.x);
+      o[dy][2] = a.y + w * (a.x - a.y);
+      o[dy][3] = a.y + w * (ap - a.y);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) y[q] = o[0][q] + w * (o[1][q] - o[0][q]);
+  };
+  const int K0 = blockIdx.z * kcz, K1 = min(K0 + kcz, cnz);
+  if (K0 >= K1) return;
+  float ym[4], y0[4], yp[4];
+  plane(ym, K0 - 1);
+  plane(y0, K0);
+  float *__restrict__ row = f.x + f.off + (int64_t)j * f.sy + 4 * Q;
+  for (int K = K0; K < K1; K++) {
+    plane(yp, K + 1);
+    // fine plane 2K: coarse planes K and K - 1 (K itself at the low wall)
+    // fine plane 2K + 1: coarse planes K and K + 1 (K itself at the high wall)
+    const bool lo = K > 0, hi = K < cnz - 1;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      float add[4];
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        const float yq = h ? (hi ? yp[q] : y0[q]) : (lo ? ym[q] : y0[q]);
+        add[q] = y0[q] + w * (yq - y0[q]);
+      }
+      if (in) {
+        float4 *px = reinterpret_cast<float4 *>(row + (int64_t)(2 * K + h) * f.sz);
+        float4 v = *px;
+        v.x += add[0];
+        v.y += add[1];
+        v.z += add[2];
+        v.w += add[3];
+        *px = v;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      ym[q] = y0[q];
+      y0[q] = yp[q];
+    }
+  }
+}
+
 // One whole red-black Gauss-Seidel sweep in one kernel, exact: reads x_old,
 // writes x_new (ping-pong), so no block ever reads a value another block
 // writes. A block owns a 64 x 8 tile of (i, j) columns and a chunk of planes;
@@ -1395,6 +1479,19 @@ bool restrict_to(const View<T> &f, T *bc, const MgLevelDesc &C, const double *sh
 template <typename T>
 bool prolong_to(const View<T> &f, const T *xc, const MgLevelDesc &C, const MgState *st)
 {
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (C.r[0] == 2 && C.r[1] == 2 && C.r[2] == 2 && f.nx % 4 == 0 && f.off % 4 == 0 &&
+        f.sy % 4 == 0 && f.sz % 4 == 0) {
+      const int gx = (f.nx / 4 + 31) / 32, gy = (f.ny + 7) / 8;
+      int gz = C.n[2];
+      while (gz > 1 && (int64_t)gx * gy * gz > 8 * sm_count_mg()) gz = (gz + 1) / 2;
+      const int kcz = (C.n[2] + gz - 1) / gz;
+      gz = (C.n[2] + kcz - 1) / kcz;
+      k_mg_prolong_f32<<<dim3(gx, gy, gz), dim3(32, 8), 0, stream()>>>(f, xc, C.n[0], C.n[1],
+          C.n[2], kcz, st);
+      return launched("k_mg_prolong_f32");
+    }
+  }
   if (C.r[0] == 2 && f.nx % 4 == 0) {
     const dim3 blk(32, 8, 1);
     const int gx = (f.nx / 4 + 31) / 32, gy = (f.ny + 7) / 8;
