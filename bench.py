@@ -67,6 +67,8 @@ def parse_args():
     ap.add_argument("--learn-steps", type=int, default=300, help="steps per training run")
     ap.add_argument("--learn-iters", type=int, default=2000, help="Adam iterations (learned)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--phases", action="store_true",
+                    help="add a per-call split of the step and per-level FP32 V-cycle times")
     ap.add_argument("--no-roofline", action="store_true",
                     help="skip the per-kernel timing launches (clean launch lists for ncu)")
     ap.add_argument("--no-graph", action="store_true",
@@ -254,6 +256,8 @@ def run_gpu(args, rank, world, local):
     # ---- dominant kernels, timed live with CUDA events on the library stream ----
     roofs = [] if args.no_roofline else kernel_rooflines(sim, solver, stream, ncell)
 
+    phases = step_phases(sim, solver, stream) if args.phases else None
+
     # ---- e2e: same step through the C ABI with host buffers ----
     e2e = None
     if not args.no_e2e:
@@ -317,11 +321,57 @@ def run_gpu(args, rank, world, local):
         "compare_fp64_mg": compare,
         "roofline": roofs[0] if roofs else None,
         "roofline_kernels": roofs,
+        "phases": phases,
         "e2e": e2e,
         "gpu_launches": head["launches"],
         "clocks": head["clocks"],
         "cpu_baseline": cpu,
     }
+    return out
+
+
+def step_phases(sim, solver, stream, steps: int = 10) -> dict:
+    """Where a step's time goes: CUDA events between the reference calls of
+    `steps` more steps (the time each call keeps the library stream busy,
+    host-side waits of computeTimestep and solve included), and for
+    mg-mixed the fine FP64 residual and one FP32 V-cycle from each level down
+    (nusifTimeKernel, which replays the V-cycle as a captured graph)."""
+    import torch
+    names = ["computeTimestep", "setBoundaryConditions", "setSpecialBoundaryCondition",
+             "computeFG", "computeRHS", "solve", "adaptUV"]
+    calls = [sim.compute_timestep, sim.set_boundary_conditions,
+             sim.set_special_boundary_condition, sim.compute_fg, sim.compute_rhs, sim.solve,
+             sim.adapt_uv]
+    acc = [0.0] * len(names)
+    total = 0.0
+    for _ in range(steps):
+        if sim.nt % 100 == 0:
+            sim.normalize_pressure()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(names) + 1)]
+        ev[0].record(stream)
+        for q, call in enumerate(calls):
+            call()
+            ev[q + 1].record(stream)
+        sim.t += sim.d.dt
+        sim.nt += 1
+        torch.cuda.synchronize()
+        for q in range(len(names)):
+            acc[q] += ev[q].elapsed_time(ev[q + 1])
+        total += ev[0].elapsed_time(ev[-1])
+    out = {"ms_per_step": total / steps, "ms": {n: a / steps for n, a in zip(names, acc)}}
+    if solver == "mg-mixed":
+        ms = C.c_double()
+        lib = sim.lib
+        lib.nusifTimeKernel(C.byref(sim.s), sim.d.p, sim.d.rhs, 1, 20, C.byref(ms))
+        out["fp64_residual_ms"] = ms.value
+        levels = []
+        for lv in range(16):
+            if lib.nusifTimeKernel(C.byref(sim.s), sim.d.p, sim.d.rhs, 2 + lv, 20,
+                                   C.byref(ms)) != 0:
+                lib.nusifGetLastError(None, 0)  # past the coarsest level: clear it
+                break
+            levels.append(ms.value)
+        out["fp32_vcycle_from_level_ms"] = levels
     return out
 
 
