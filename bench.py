@@ -158,18 +158,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# V-cycle shape of each solver in the benchmark: V(2,2) (the reference
-# configuration's cycle), and for the mixed-precision solver up to 4 FP32
-# V-cycles per FP64 residual (V(1,1), V(3,3), V(4,4) and 2 or 8 inner cycles
-# measured slower at 256^3 with the quadratic warm start)
-# (pre-sweeps, post-sweeps, most FP32 V-cycles per FP64 residual); the FP32
-# correction of mg-mixed stops at 0.9 rtol (the library default mg_theta), so
-# three V(2,2) cycles usually end a 256^3 solve with the FP64 check passing
-MG_SHAPE = {"mg": (2, 2, 4), "mg-mixed": (2, 2, 3)}
+# (pre-sweeps, post-sweeps, most FP32 V-cycles per FP64 residual, smoother
+# relaxation omega) of each solver in the benchmark. FP64 multigrid: V(2,2)
+# red-black Gauss-Seidel, the reference configuration's cycle. Mixed
+# precision: V(1,1) with omega 1.3, at most 4 FP32 V-cycles per FP64
+# residual, the FP32 correction stopped at 0.9 rtol (the library default
+# mg_theta) - the fastest of the shapes measured at 256^3 with the quadratic
+# warm start.
+MG_SHAPE = {"mg": (2, 2, 4, 1.0), "mg-mixed": (1, 1, 4, 1.3)}
+# the FP64 arm with the same kind of tuning: V(1,2), omega 1.3 (fastest FP64
+# shape measured at 256^3 with the quadratic warm start)
+MG_SHAPE_FP64_TUNED = (1, 2, 4, 1.3)
 
 
 def bench_case(n: int, solver: str, itermax: int | None = None,
-               guess: str = "previous", shape: tuple[int, int, int] | None = None,
+               guess: str = "previous", shape: tuple | None = None,
                graph: bool = True) -> dict:
     from nusif.params import config2
     vals = config2(solver=solver)
@@ -177,8 +180,8 @@ def bench_case(n: int, solver: str, itermax: int | None = None,
     if itermax is not None:
         vals["itermax"] = itermax
     if solver in ("mg", "mg-mixed"):
-        pre, post, inner = shape or MG_SHAPE[solver]
-        vals.update(mg_guess=guess, mg_pre=pre, mg_post=post, mg_inner=inner,
+        pre, post, inner, omega = shape or MG_SHAPE[solver]
+        vals.update(mg_guess=guess, mg_pre=pre, mg_post=post, mg_inner=inner, mg_omega=omega,
                     mg_graph=1 if graph else 0)
     return vals
 
@@ -269,14 +272,15 @@ def run_gpu(args, rank, world, local):
     compare = None
     if solver == "mg-mixed" and not args.no_compare:
         compare = []
-        arms = [("previous", (2, 2, 4)), (args.guess, (2, 2, 4))]
+        arms = [("previous", MG_SHAPE["mg"]), (args.guess, MG_SHAPE["mg"]),
+                (args.guess, MG_SHAPE_FP64_TUNED)]
         for g, shape in dict.fromkeys(arms):
             sim64 = nusif.Simulation(bench_case(args.n, "mg", args.itermax, g, shape,
                                                 graph=not args.no_graph))
             ref64 = timed_steps(sim64, args, stream, local, world)
             sim64.close()
             compare.append({"solver": "mg (FP64 V-cycles, same rtol 1e-6)", "guess": g,
-                            "v_cycle": "V(%d,%d)" % shape[:2],
+                            "v_cycle": "V(%d,%d), omega %.2f" % (shape[0], shape[1], shape[3]),
                             "ms_per_step": ref64["ms_per_step"],
                             "v_cycles_per_step": ref64["iters"],
                             "residual_per_step": ref64["res"],
@@ -309,9 +313,11 @@ def run_gpu(args, rank, world, local):
                    "learned_warm_start": False,
                    "initial_guess": (args.guess if solver in ("mg", "mg-mixed") else "previous"),
                    "v_cycle": ("V(%d,%d), up to %d FP32 V-cycles per FP64 residual, "
-                               "FP32 correction to 0.9 rtol"
+                               "red-black smoother omega %.2f, FP32 correction to 0.9 rtol"
                                % MG_SHAPE["mg-mixed"] if solver == "mg-mixed" else
-                               "V(%d,%d)" % MG_SHAPE["mg"][:2] if solver == "mg" else None),
+                               "V(%d,%d), omega %.2f" % (MG_SHAPE["mg"][0], MG_SHAPE["mg"][1],
+                                                         MG_SHAPE["mg"][3])
+                               if solver == "mg" else None),
                    "solve_launch": ("host-driven launches" if args.no_graph else
                                     "one CUDA graph per solve (device while-loops)"),
                    "l2": "no flush: 8 FP64 fields of %.0f MB each, far larger than L2" % (padded * 8 / 1e6),

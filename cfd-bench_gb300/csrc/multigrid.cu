@@ -65,6 +65,7 @@ struct MgLevelDesc {
   int n[3];
   int r[3];  // coarsening ratio from the finer level
   double ih2[3];
+  double relax = 1.0;  // smoother: x -= relax * r / diag (Gauss-Seidel at 1)
 };
 
 // A level's array view: interior cell (i,j,k), 0-based, lives at
@@ -108,6 +109,8 @@ struct MgHierarchy {
   bool use_graph = true;     // mg_graph: the host-driven solve runs as one graph
   int tail_l0 = 0;           // first level of the one-kernel coarse tail (0: none)
   int kc[kMaxLevels] = {};   // planes per block of each level's one-kernel sweep (0: by rule)
+  // FP32 sweeps skipped inside a V-cycle copy x along (odd pre- or post-sweep counts)
+  int keep_on_skip = 0;
   // kernels per part of the graph (counted at capture): head, one outer unit
   // without its inner loop, one inner V-cycle, tail
   int n_head = 0, n_outer = 0, n_inner = 0, n_tail = 0;
@@ -787,9 +790,29 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // second-colour neighbour inside the domain must see there.
 template <bool ZERO>
 __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__restrict__ xnew,
-    int kc, const MgState *st)
+    int kc, const MgState *st, int keep)
 {
-  if (mg_done(st)) return;
+  if (mg_done(st)) {
+    // The host swaps the two buffers after every sweep it launches. A sweep
+    // skipped because the correction met its target inside this V-cycle must
+    // still leave x where the next kernels look (keep: set when a level's
+    // sweeps per V-cycle could be skipped in odd numbers): it copies its
+    // chunk, or writes the zero it would have started from.
+    if (keep && !solve_finished(st)) {
+      const int i0 = blockIdx.x * kSX, j0 = blockIdx.y * kSY, k0 = blockIdx.z * kc;
+      const int k1 = min(k0 + kc, v.nz);
+      constexpr int kRowChunks = kSX / 4, kPlane = kSY * kRowChunks;
+      for (int q = threadIdx.x; q < (k1 - k0) * kPlane; q += 256) {
+        const int k = k0 + q / kPlane, rem = q % kPlane;
+        const int j = j0 + rem / kRowChunks, i = i0 + 4 * (rem % kRowChunks);
+        if (j >= v.ny || i >= v.nx) continue;
+        const int64_t c = (int64_t)k * v.sz + (int64_t)j * v.sy + i;
+        *reinterpret_cast<float4 *>(xnew + c) =
+            ZERO ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(v.x + c);
+      }
+    }
+    return;
+  }
   constexpr int PX = kRY * kWX, PB = kBYr * kWX, PR = kBYr * kQX;  // floats per staged plane
   // Five x_old slots and four b and first-colour slots: the copies a thread
   // issues for plane k + 3 never land in a slot that a slower warp may still
@@ -1380,7 +1403,7 @@ View<T> compact_view(const MgLevelDesc &L, T *x, const T *b)
   v.ey = (T)L.ih2[1];
   v.ez = (T)L.ih2[2];
   v.diag = (T)d;
-  v.inv_diag = (T)(1.0 / d);
+  v.inv_diag = (T)(L.relax / d);
   return v;
 }
 
@@ -1602,9 +1625,10 @@ int sweep_chunk_tuned(const MgLevelDesc &L, float *x, float *xb, float *b)
   for (const int c : cand) {
     if (c > nz) continue;
     const dim3 grid(gx, gy, (nz + c - 1) / c);
-    k_rbgs_sweep<false><<<grid, 256, 0, stream()>>>(v, xb, c, idle);  // warm-up
+    k_rbgs_sweep<false><<<grid, 256, 0, stream()>>>(v, xb, c, idle, 0);  // warm-up
     cudaEventRecord(e0, stream());
-    for (int r = 0; r < 3; r++) k_rbgs_sweep<false><<<grid, 256, 0, stream()>>>(v, xb, c, idle);
+    for (int r = 0; r < 3; r++)
+      k_rbgs_sweep<false><<<grid, 256, 0, stream()>>>(v, xb, c, idle, 0);
     cudaEventRecord(e1, stream());
     float ms = 0.0f;
     if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
@@ -1634,9 +1658,9 @@ bool fused_sweeps(MgHierarchy *H, int l, int count, bool zero_first, const MgSta
   for (int s = 0; s < count; s++) {
     const View<float> v = compact_view<float>(L, H->x32[l], H->b32[l]);
     if (zero_first && s == 0)
-      k_rbgs_sweep<true><<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st);
+      k_rbgs_sweep<true><<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st, H->keep_on_skip);
     else
-      k_rbgs_sweep<false><<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st);
+      k_rbgs_sweep<false><<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st, H->keep_on_skip);
     if (!launched("k_rbgs_sweep")) return false;
     float *t = H->x32[l];
     H->x32[l] = H->x32b[l];
@@ -1678,7 +1702,7 @@ bool tail_vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero)
     t.ey = (T)L.ih2[1];
     t.ez = (T)L.ih2[2];
     t.diag = (T)d;
-    t.inv_diag = (T)(1.0 / d);
+    t.inv_diag = (T)(L.relax / d);
     t.x = xs[l + q];
     t.b = bs[l + q];
   }
@@ -1829,6 +1853,7 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
   H->maxcycles = x.mg_maxcycles;
   H->inner = x.mg_inner < 1 ? 1 : x.mg_inner;
   H->theta = x.mg_theta;
+  H->keep_on_skip = (H->pre % 2 != 0 || H->post % 2 != 0) ? 1 : 0;
   H->guess = x.mg_guess == 1 || x.mg_guess == 2 ? x.mg_guess : 0;
   H->use_graph = x.mg_graph != 0;
   for (cudaStream_t &c : H->cap)
@@ -1846,11 +1871,15 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
   }
   H->rtol = x.rtol;
   if (H->pre < 0 || H->post < 0 || H->coarse_sweeps < 0 || H->maxcycles < 1 || !(H->rtol >= 0) ||
-      !(H->theta > 0 && H->theta <= 1)) {
-    fail(NUSIF_ERR_ARG, "multigrid: invalid mg_pre/mg_post/mg_coarse/mg_cycles/rtol/mg_theta");
+      !(H->theta > 0 && H->theta <= 1) || !(x.mg_omega > 0 && x.mg_omega < 2)) {
+    fail(NUSIF_ERR_ARG,
+         "multigrid: invalid mg_pre/mg_post/mg_coarse/mg_cycles/rtol/mg_theta/mg_omega");
     return false;
   }
   H->nl = build_levels(&d->grid, x.mg_levels, H->lv);
+  // over-relaxed red-black smoothing (mg_omega; 1 is Gauss-Seidel): the FP64
+  // residual still decides convergence
+  for (int l = 0; l < H->nl; l++) H->lv[l].relax = x.mg_omega;
   // the coarse tail: from the first level below the finest with at most
   // mg_tail cells (0: off), when it leaves at least two levels to it
   H->tail_l0 = 0;

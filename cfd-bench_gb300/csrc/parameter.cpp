@@ -99,6 +99,7 @@ int apply_extra(Parameter *param, const char *tok, const char *val)
   if (starts_with(tok, "mg_cycles")) { x->mg_maxcycles = atoi(v); hit = 1; }
   if (starts_with(tok, "mg_inner")) { x->mg_inner = atoi(v); hit = 1; }
   if (starts_with(tok, "mg_theta")) { x->mg_theta = atof(v); hit = 1; }
+  if (starts_with(tok, "mg_omega")) { x->mg_omega = atof(v); hit = 1; }
   if (starts_with(tok, "mg_graph")) { x->mg_graph = atoi(v); hit = 1; }
   if (starts_with(tok, "mg_tail")) { x->mg_tail = atoi(v); hit = 1; }
   if (starts_with(tok, "mg_chunk")) { x->mg_chunk = atoi(v); hit = 1; }
