@@ -243,6 +243,9 @@ __device__ __forceinline__ ZFace z_face(const double *__restrict__ u, const doub
 
 constexpr int kFX = 32, kFY = 8;
 
+// GRAVITY false: gx = gy = gz = 0, where fma(dt, 0 - s, q) is exactly
+// fma(-dt, s, q): one FP64 instruction less per component, same bits.
+template <bool GRAVITY>
 __global__ void __launch_bounds__(kFX *kFY) k_fgh_flux(FluxArgs A, const double *__restrict__ u,
     const double *__restrict__ v, const double *__restrict__ w, double *__restrict__ f,
     double *__restrict__ gg, double *__restrict__ h)
@@ -283,7 +286,7 @@ __global__ void __launch_bounds__(kFX *kFY) k_fgh_flux(FluxArgs A, const double 
       const double uc = __ldg(u + c), vc = __ldg(v + c), wc = __ldg(w + c);
       // F(imax), G(jmax), H(kmax) are wall faces carrying the velocity (discretization.c:609-651)
       const double sf = (xp.f - xm.f) + (yp.f - ym.f) + (zp.f - zm.f);
-      f[c] = (i == g.imax) ? uc : fma(dt, A.gx - sf, uc);
+      f[c] = (i == g.imax) ? uc : GRAVITY ? fma(dt, A.gx - sf, uc) : fma(-dt, sf, uc);
       // c1*(vc + vt)*(gp - gm) + c2*(vc - vt)*(|gp| + |gm|) as gp*Xp - gm*Xm,
       // Xp and Xm weighted sums of vc and vt chosen by the signs of gp and gm
       const double vt = __ldg(v + c + sk);
@@ -292,9 +295,9 @@ __global__ void __launch_bounds__(kFX *kFY) k_fgh_flux(FluxArgs A, const double 
       const double xmz = fma(nm ? A.az.P : A.az.M, vc, (nm ? A.az.M : A.az.P) * vt);
       const double zconv = fma(zp.gc, xpz, -(zm.gc * xmz));
       const double sg = (xp.g - xm.g) + (yp.g - ym.g) + (zp.gv - zm.gv) + zconv;
-      gg[c] = (j == g.jmax) ? vc : fma(dt, A.gy - sg, vc);
+      gg[c] = (j == g.jmax) ? vc : GRAVITY ? fma(dt, A.gy - sg, vc) : fma(-dt, sg, vc);
       const double sh = (xp.h - xm.h) + (yp.h - ym.h) + (zp.h - zm.h);
-      h[c] = (k == g.kmax) ? wc : fma(dt, A.gz - sh, wc);
+      h[c] = (k == g.kmax) ? wc : GRAVITY ? fma(dt, A.gz - sh, wc) : fma(-dt, sh, wc);
       // low wall faces F(0), G(0), H(0) carry the velocity (discretization.c:601-643)
       if (i == 1) f[c - 1] = __ldg(u + c - 1);
       if (j == 1) gg[c - sj] = __ldg(v + c - sj);
@@ -471,7 +474,10 @@ bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, do
   if (kb_fixed > 0) kb = kb_fixed;
   A.kb = kb;
   dim3 grid(gx_blocks, gy_blocks, (g.kmax + kb - 1) / kb);
-  k_fgh_flux<<<grid, dim3(kFX, kFY), 0, stream()>>>(A, u, v, w, f, gg, h);
+  if (gx == 0.0 && gy == 0.0 && gz == 0.0)
+    k_fgh_flux<false><<<grid, dim3(kFX, kFY), 0, stream()>>>(A, u, v, w, f, gg, h);
+  else
+    k_fgh_flux<true><<<grid, dim3(kFX, kFY), 0, stream()>>>(A, u, v, w, f, gg, h);
   return launched("k_fgh_flux");
 }
 

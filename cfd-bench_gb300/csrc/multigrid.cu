@@ -55,7 +55,7 @@ struct MgState {
   int inner_done;    // mg-mixed: this outer iteration's correction is good enough
   int loops;         // units run by a graph while-loop (its independent stop)
   int inner_it;      // mg-mixed: FP32 V-cycles of the current correction (graph inner loop)
-  int pad;
+  int need_norm;     // the one-pass norm of the right-hand side was not trusted
 };
 
 // what the fold of a fine-level restriction decides
@@ -111,6 +111,7 @@ struct MgHierarchy {
   int kc[kMaxLevels] = {};   // planes per block of each level's one-kernel sweep (0: by rule)
   // FP32 sweeps skipped inside a V-cycle copy x along (odd pre- or post-sweep counts)
   int keep_on_skip = 0;
+  double *stats2 = nullptr;  // per-block sums of squares of the right-hand side
   // kernels per part of the graph (counted at capture): head, one outer unit
   // without its inner loop, one inner V-cycle, tail
   int n_head = 0, n_outer = 0, n_inner = 0, n_tail = 0;
@@ -1220,35 +1221,69 @@ __global__ void __launch_bounds__(1024) k_mg_tail(TailArgs<T> a)
   }
 }
 
-// mean of the right-hand side, then ||rhs - mean||^2; initialises the state
-__global__ void __launch_bounds__(kNT) k_mg_rhs_sum(View<double> f, MgState *st,
-    double *partials, unsigned *ticket)
+// the solve state for a right-hand side whose ||b - shift||^2 is nb2
+__device__ void open_solve(MgState *st, double nb2)
+{
+  st->nb2 = nb2;
+  st->tol2 = st->rtol2 * nb2;
+  st->tol_inner = st->theta2 * st->rtol2 * nb2;
+  st->res2 = 0.0;
+  st->res2_inner = 0.0;
+  st->cycles = 0;
+  st->outer = 0;
+  st->inner_done = 0;
+  st->loops = 0;
+  st->done = (nb2 == 0.0);
+}
+
+// One pass over the right-hand side: its sum and sum of squares, folded by the
+// last block into the mean (the shift) and ||b - shift||^2 = sum b^2 -
+// shift * sum b; initialises the solve state. The subtraction keeps its digits
+// while the mean is small against the spread (a compatible Neumann right-hand
+// side has mean ~0); when shift * sum b exceeds half of sum b^2 it raises
+// need_norm instead, and k_mg_rhs_norm computes the norm about the mean in a
+// second pass.
+__global__ void __launch_bounds__(kNT) k_mg_rhs_stats(View<double> f, MgState *st,
+    double *partials, double *partials2, unsigned *ticket)
 {
   const int64_t n = (int64_t)f.nx * f.ny * f.nz;
-  double acc = 0.0;
+  double acc = 0.0, acc2 = 0.0;
   const int64_t q0 = blockIdx.x * (int64_t)kNT + threadIdx.x, stride = (int64_t)gridDim.x * kNT;
   FlatWalk w(q0, stride, f.nx, f.ny);
-  for (int64_t q = q0; q < n; q += stride, w.advance(f.nx, f.ny))
-    acc += f.b[f.off + (int64_t)w.k * f.sz + (int64_t)w.j * f.sy + w.i];
+  for (int64_t q = q0; q < n; q += stride, w.advance(f.nx, f.ny)) {
+    const double b = f.b[f.off + (int64_t)w.k * f.sz + (int64_t)w.j * f.sy + w.i];
+    acc += b;
+    acc2 = fma(b, b, acc2);
+  }
   __shared__ double sm[kNT / 32];
   acc = block_reduce_sum<kNT>(acc, sm);
+  acc2 = block_reduce_sum<kNT>(acc2, sm);
   __shared__ bool last;
   if (threadIdx.x == 0) {
     partials[blockIdx.x] = acc;
+    partials2[blockIdx.x] = acc2;
     last = ticket_is_last(ticket);
   }
   __syncthreads();
   if (!last) return;
   const double total = fold_partials<kNT>(partials, gridDim.x, sm);
+  const double total2 = fold_partials<kNT>(partials2, gridDim.x, sm);
   if (threadIdx.x == 0) {
-    st->shift = total / (double)n;
+    const double shift = total / (double)n;
+    st->shift = shift;
+    const double mean_part = shift * total;  // n shift^2
+    st->need_norm = mean_part > 0.5 * total2;
+    if (!st->need_norm) open_solve(st, fmax(total2 - mean_part, 0.0));
     *ticket = 0;
   }
 }
 
+// ||b - shift||^2 in a second pass, when k_mg_rhs_stats did not trust its
+// one-pass value (returns at once otherwise)
 __global__ void __launch_bounds__(kNT) k_mg_rhs_norm(View<double> f, MgState *st,
     double *partials, unsigned *ticket)
 {
+  if (!*reinterpret_cast<const volatile int *>(&st->need_norm)) return;
   const int64_t n = (int64_t)f.nx * f.ny * f.nz;
   const double sh = st->shift;
   double acc = 0.0;
@@ -1269,16 +1304,8 @@ __global__ void __launch_bounds__(kNT) k_mg_rhs_norm(View<double> f, MgState *st
   if (!last) return;
   const double total = fold_partials<kNT>(partials, gridDim.x, sm);
   if (threadIdx.x == 0) {
-    st->nb2 = total;
-    st->tol2 = st->rtol2 * total;
-    st->tol_inner = st->theta2 * st->rtol2 * total;
-    st->res2 = 0.0;
-    st->res2_inner = 0.0;
-    st->cycles = 0;
-    st->outer = 0;
-    st->inner_done = 0;
-    st->loops = 0;
-    st->done = (total == 0.0);
+    open_solve(st, total);
+    st->need_norm = 0;
     *ticket = 0;
   }
 }
@@ -1937,6 +1964,9 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
   }
   const int64_t n0 = (int64_t)d->grid.imax * d->grid.jmax * d->grid.kmax;
   if (!reduce_scratch_alloc(H->red, flat_blocks(n0) + 16)) return false;
+  if (!cuda_ok(cudaMalloc(&H->stats2, sizeof(double) * (size_t)flat_blocks(n0)),
+          "cudaMalloc(rhs partials)"))
+    return false;
   if (!cuda_ok(cudaMalloc(&H->d_state, sizeof(MgState)), "cudaMalloc(mg state)")) return false;
   if (!cuda_ok(cudaMallocHost(&H->h_state, sizeof(MgState)), "cudaMallocHost(mg state)"))
     return false;
@@ -2017,8 +2047,9 @@ bool enqueue_solve_head(MgHierarchy *H, const View<double> &v0)
   if (!launched("k_mg_state_init")) return false;
   const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
   const int blocks = flat_blocks(n0);
-  k_mg_rhs_sum<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
-  if (!launched("k_mg_rhs_sum")) return false;
+  k_mg_rhs_stats<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->stats2,
+      H->red.ticket);
+  if (!launched("k_mg_rhs_stats")) return false;
   k_mg_rhs_norm<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
   return launched("k_mg_rhs_norm");
 }
@@ -2260,8 +2291,9 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
                      stream()),
             "mg state upload"))
       return NAN;
-    k_mg_rhs_sum<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
-    if (!launched("k_mg_rhs_sum")) return NAN;
+    k_mg_rhs_stats<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->stats2,
+        H->red.ticket);
+    if (!launched("k_mg_rhs_stats")) return NAN;
     k_mg_rhs_norm<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
     if (!launched("k_mg_rhs_norm")) return NAN;
     int chunk = H->last_cycles > 0 ? H->last_cycles : 4;
@@ -2395,6 +2427,7 @@ void mg_free(Solver *s, SolverState *ss)
     if (H->b32[l]) cudaFree(H->b32[l]);
   }
   if (H->graph) cudaGraphExecDestroy(H->graph);
+  if (H->stats2) cudaFree(H->stats2);
   for (cudaStream_t c : H->cap)
     if (c) cudaStreamDestroy(c);
   if (H->p_prev) cudaFree(H->p_prev);
