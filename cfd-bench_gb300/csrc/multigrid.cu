@@ -665,6 +665,64 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong_x4(View<T> f, const T *__res
   }
 }
 
+// One red-black sweep from x = 0 (the first pre-sweep of a V-cycle level),
+// FP32 rows of a multiple of four cells. From zero, a first-colour cell
+// ((i+j+k) even) relaxes to -b/diag (times the relaxation), and a
+// second-colour cell relaxes against those values: its other neighbours are
+// second-colour cells, still 0, as is a missing neighbour beyond a wall (the
+// cell itself). So the whole sweep is one stencil pass over b, one thread per
+// four consecutive cells of a row, writing x_new (the buffer the host swaps
+// in), with the arithmetic of k_rbgs_sweep<true>.
+__global__ void __launch_bounds__(kNT) k_rb_zero_sweep(View<float> v, float *__restrict__ xnew,
+    const MgState *st, int keep)
+{
+  const int Q = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = v.nx, ny = v.ny, nz = v.nz;
+  const int i0 = 4 * Q;
+  if (i0 >= nx || j >= ny) return;
+  if (mg_done(st)) {
+    // skipped inside a V-cycle: leave the zero it would have started from
+    if (keep && !solve_finished(st))
+      for (int k = blockIdx.z; k < nz; k += gridDim.z)
+        *reinterpret_cast<float4 *>(xnew + (int64_t)k * v.sz + (int64_t)j * v.sy + i0) =
+            make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const float ex = v.ex, ey = v.ey, ez = v.ez, dg = v.diag, idg = v.inv_diag;
+  const float *__restrict__ b = v.b;
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int k = blockIdx.z; k < nz; k += gridDim.z) {
+    const int64_t c = (int64_t)k * v.sz + (int64_t)j * v.sy + i0;
+    const float4 bc = *reinterpret_cast<const float4 *>(b + c);
+    const float4 bs = j > 0 ? *reinterpret_cast<const float4 *>(b + c - v.sy) : z4;
+    const float4 bn = j < ny - 1 ? *reinterpret_cast<const float4 *>(b + c + v.sy) : z4;
+    const float4 bd = k > 0 ? *reinterpret_cast<const float4 *>(b + c - v.sz) : z4;
+    const float4 bu = k < nz - 1 ? *reinterpret_cast<const float4 *>(b + c + v.sz) : z4;
+    const float brow[6] = { i0 > 0 ? b[c - 1] : 0.f, bc.x, bc.y, bc.z, bc.w,
+                            i0 + 4 < nx ? b[c + 4] : 0.f };
+    const float bsv[4] = { bs.x, bs.y, bs.z, bs.w }, bnv[4] = { bn.x, bn.y, bn.z, bn.w };
+    const float bdv[4] = { bd.x, bd.y, bd.z, bd.w }, buv[4] = { bu.x, bu.y, bu.z, bu.w };
+    // a first-colour cell's new value from its own b
+    auto first = [&](float bb) { return 0.0f - (bb - 0.0f) * idg; };
+    float out[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int i = i0 + q;
+      if (((i + j + k) & 1) == 0) {
+        out[q] = first(brow[q + 1]);
+      } else {
+        const float rw = i > 0 ? first(brow[q]) : 0.f, re = i < nx - 1 ? first(brow[q + 2]) : 0.f;
+        const float rs = j > 0 ? first(bsv[q]) : 0.f, rn = j < ny - 1 ? first(bnv[q]) : 0.f;
+        const float rd = k > 0 ? first(bdv[q]) : 0.f, ru = k < nz - 1 ? first(buv[q]) : 0.f;
+        const float sx = rw + re, sy = rs + rn, sz = rd + ru;
+        const float lap = sx * ex + sy * ey + sz * ez - dg * 0.0f;
+        out[q] = 0.0f - (brow[q + 1] - lap) * idg;
+      }
+    }
+    *reinterpret_cast<float4 *>(xnew + c) = make_float4(out[0], out[1], out[2], out[3]);
+  }
+}
+
 // x_f += trilinear interpolation of x_c on FP32 levels halved on every axis
 // with fine rows of a multiple of four cells (16-byte aligned): one thread per
 // four consecutive fine cells of a row walks a chunk of coarse planes K and
@@ -1684,11 +1742,17 @@ bool fused_sweeps(MgHierarchy *H, int l, int count, bool zero_first, const MgSta
   const dim3 grid(gx, gy, (L.n[2] + kc - 1) / kc);
   for (int s = 0; s < count; s++) {
     const View<float> v = compact_view<float>(L, H->x32[l], H->b32[l]);
-    if (zero_first && s == 0)
-      k_rbgs_sweep<true><<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st, H->keep_on_skip);
-    else
+    if (zero_first && s == 0) {
+      const int zx = (L.n[0] / 4 + 31) / 32, zy = (L.n[1] + 7) / 8;
+      int zz = L.n[2];
+      while (zz > 1 && (int64_t)zx * zy * zz > 8 * sm_count_mg()) zz = (zz + 1) / 2;
+      k_rb_zero_sweep<<<dim3(zx, zy, zz), dim3(32, 8), 0, stream()>>>(v, H->x32b[l], st,
+          H->keep_on_skip);
+      if (!launched("k_rb_zero_sweep")) return false;
+    } else {
       k_rbgs_sweep<false><<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st, H->keep_on_skip);
-    if (!launched("k_rbgs_sweep")) return false;
+      if (!launched("k_rbgs_sweep")) return false;
+    }
     float *t = H->x32[l];
     H->x32[l] = H->x32b[l];
     H->x32b[l] = t;
@@ -2455,10 +2519,11 @@ extern "C" {
 // One or more exact red-black Gauss-Seidel sweeps of the multigrid's FP32
 // smoother (the one-kernel sweep; ghost-free Neumann operator) on compact
 // device arrays x[nz][ny][nx] -> xout; first colour (i + j + k) even, 0-based.
+// x null: the sweeps start from zero (the first one by the zero-start kernel).
 int nusifSmoothRBF32(const float *x, const float *b, float *xout, int nx, int ny, int nz,
     double hx, double hy, double hz, int sweeps)
 {
-  if (!x || !b || !xout || nx < 4 || ny < 1 || nz < 1 || nx % 4 || sweeps < 1 || !(hx > 0) ||
+  if (!b || !xout || nx < 4 || ny < 1 || nz < 1 || nx % 4 || sweeps < 1 || !(hx > 0) ||
       !(hy > 0) || !(hz > 0)) {
     fail(NUSIF_ERR_ARG, "nusifSmoothRBF32: needs device arrays, nx a multiple of 4, sweeps >= 1");
     return NUSIF_ERR_ARG;
@@ -2479,13 +2544,14 @@ int nusifSmoothRBF32(const float *x, const float *b, float *xout, int nx, int ny
   bool ok = cuda_ok(cudaMalloc(&scratch, 2 * n * sizeof(float)), "cudaMalloc(smooth)") &&
             cuda_ok(cudaMalloc(&st, sizeof(MgState)), "cudaMalloc(smooth)") &&
             cuda_ok(cudaMemsetAsync(st, 0, sizeof(MgState), stream()), "smooth state") &&
-            cuda_ok(cudaMemcpyAsync(scratch, x, n * sizeof(float), cudaMemcpyDeviceToDevice,
-                        stream()),
-                "smooth copy");
+            (x ? cuda_ok(cudaMemcpyAsync(scratch, x, n * sizeof(float), cudaMemcpyDeviceToDevice,
+                             stream()),
+                     "smooth copy")
+               : cuda_ok(cudaMemsetAsync(scratch, 0, n * sizeof(float), stream()), "smooth zero"));
   H.x32[0] = scratch;
   H.x32b[0] = scratch + n;
   H.b32[0] = const_cast<float *>(b);
-  ok = ok && fused_sweeps(&H, 0, sweeps, false, st) &&
+  ok = ok && fused_sweeps(&H, 0, sweeps, x == nullptr, st) &&
        cuda_ok(cudaMemcpyAsync(xout, H.x32[0], n * sizeof(float), cudaMemcpyDeviceToDevice,
                    stream()),
            "smooth copy") &&

@@ -227,6 +227,8 @@ NUSIF_API const char *nusifVersion(void);
  * multigrid's FP32 smoother (one kernel per sweep) on compact device arrays
  * x, b [nz][ny][nx] (nx a multiple of 4) -> xout: ghost-free Neumann
  * operator with spacings hx, hy, hz; first colour (i + j + k) even, 0-based.
+ * x may be NULL: the sweeps start from x = 0 (as the first pre-sweep of every
+ * V-cycle level does).
  * No reference counterpart (the smoother of the corrected multigrid). */
 NUSIF_API int nusifSmoothRBF32(const float *x, const float *b, float *xout, int nx, int ny, int nz,
     double hx, double hy, double hz, int sweeps);

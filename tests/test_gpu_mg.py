@@ -272,6 +272,31 @@ def test_one_kernel_coarse_tail_matches(nusif_lib, solver):
             np.testing.assert_array_equal(a.field(f), b.field(f))
 
 
+@pytest.mark.parametrize("dims", [(64, 16, 8), (20, 12, 16), (36, 9, 70), (4, 3, 5), (128, 24, 40)])
+def test_fp32_zero_start_sweep_is_exact_red_black(nusif_lib, dims):
+    """The first pre-sweep of every V-cycle level starts from x = 0 and runs as
+    one stencil pass over b (k_rb_zero_sweep): it equals a two-pass red-black
+    sweep from zero, and the sweeps after it continue exactly."""
+    import ctypes as C
+
+    import torch
+    nx, ny, nz = dims
+    rng = np.random.default_rng(43)
+    b = rng.standard_normal((nz, ny, nx)).astype(np.float32)
+    h = (1.0 / nx, 0.8 / ny, 1.2 / nz)
+    want = np.zeros_like(b)
+    for s in (1, 2, 3):
+        want = _rb_sweep_f32(want, b, h)
+        bd = torch.from_numpy(b).cuda()
+        out = torch.empty_like(bd)
+        rc = nusif_lib.nusifSmoothRBF32(None, C.c_void_p(bd.data_ptr()),
+                                        C.c_void_p(out.data_ptr()), nx, ny, nz, *h, s)
+        assert rc == 0
+        got = out.cpu().numpy()
+        scale = np.abs(want).max()
+        assert np.abs(got - want).max() <= 2e-5 * scale, (s, np.abs(got - want).max() / scale)
+
+
 def _bits_f64(rng, n):
     """Random binary64 patterns over every exponent (normal, subnormal, zero,
     infinity, NaN), with round-to-nearest ties and near-ties for binary32."""
