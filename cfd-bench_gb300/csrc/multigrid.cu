@@ -672,7 +672,7 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong_x4(View<T> f, const T *__res
 // second-colour cells, still 0, as is a missing neighbour beyond a wall (the
 // cell itself). So the whole sweep is one stencil pass over b, one thread per
 // four consecutive cells of a row, writing x_new (the buffer the host swaps
-// in), with the arithmetic of k_rbgs_sweep<true>.
+// in), with the arithmetic of the general sweep (k_rbgs_sweep) on x = 0.
 __global__ void __launch_bounds__(kNT) k_rb_zero_sweep(View<float> v, float *__restrict__ xnew,
     const MgState *st, int keep)
 {
@@ -820,7 +820,7 @@ __global__ void __launch_bounds__(kNT) k_mg_prolong_f32(View<float> f, const flo
 // staged in shared memory by asynchronous copies issued one plane ahead
 // (cp.async, completed by cp.async.wait_group), so global latency overlaps
 // the arithmetic of the plane before. One sweep reads x and b once and
-// writes x once. ZERO: x_old is zero (not read).
+// writes x once. (A sweep from x = 0 is k_rb_zero_sweep.)
 constexpr int kSX = 64, kSY = 8;  // tile (cells)
 constexpr int kWX = kSX + 8;      // staged row: tile + 4 cells each side (16-byte chunks)
 constexpr int kRY = kSY + 4;      // staged x_old rows: tile + 2-row ring
@@ -847,7 +847,6 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // the wall column); a first-colour ring cell outside the domain stores that
 // mirrored old value instead of a relaxed one, which is exactly what its
 // second-colour neighbour inside the domain must see there.
-template <bool ZERO>
 __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__restrict__ xnew,
     int kc, const MgState *st, int keep)
 {
@@ -855,8 +854,7 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
     // The host swaps the two buffers after every sweep it launches. A sweep
     // skipped because the correction met its target inside this V-cycle must
     // still leave x where the next kernels look (keep: set when a level's
-    // sweeps per V-cycle could be skipped in odd numbers): it copies its
-    // chunk, or writes the zero it would have started from.
+    // sweeps per V-cycle could be skipped in odd numbers): it copies its chunk.
     if (keep && !solve_finished(st)) {
       const int i0 = blockIdx.x * kSX, j0 = blockIdx.y * kSY, k0 = blockIdx.z * kc;
       const int k1 = min(k0 + kc, v.nz);
@@ -866,8 +864,7 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
         const int j = j0 + rem / kRowChunks, i = i0 + 4 * (rem % kRowChunks);
         if (j >= v.ny || i >= v.nx) continue;
         const int64_t c = (int64_t)k * v.sz + (int64_t)j * v.sy + i;
-        *reinterpret_cast<float4 *>(xnew + c) =
-            ZERO ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<const float4 *>(v.x + c);
+        *reinterpret_cast<float4 *>(xnew + c) = *reinterpret_cast<const float4 *>(v.x + c);
       }
     }
     return;
@@ -888,7 +885,7 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
   constexpr int kChunks = kWX / 4;  // 18 per row
   const int cr = tid / kChunks, cc = tid - cr * kChunks;
   const int gic = min(max(i0 - 4 + 4 * cc, 0), nx - 4);
-  const bool x_lane = !ZERO && cr < kRY, b_lane = cr < kBYr;
+  const bool x_lane = cr < kRY, b_lane = cr < kBYr;
   const int gjx = min(max(j0 - 2 + cr, 0), ny - 1), gjb = min(max(j0 - 1 + cr, 0), ny - 1);
   const float *__restrict__ gxs = v.x + (int64_t)gjx * v.sy + gic;
   const float *__restrict__ gbs = v.b + (int64_t)gjb * v.sy + gic;
@@ -897,10 +894,7 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
   // staged columns of the ghosts beyond the x walls, when inside this window
   const bool wl = i0 == 0;             // gi = -1 at column 3, wall column 4
   const int wr = nx - (i0 - 4);        // column of gi = nx
-  const bool patch = !ZERO && (wl || wr < kWX);
-  if (ZERO) {
-    for (int q = tid; q < 5 * PX; q += 256) xo[q] = 0.0f;
-  }
+  const bool patch = wl || wr < kWX;
   // first-colour items (two at most per plane): offsets in a plane with the
   // colour bit lsb = 0, the colour bit at even k, and in-domain flags per bit
   constexpr int kRow = kQX / 2;      // 33 pairs per row
@@ -1665,7 +1659,7 @@ int sweep_chunk_rule(const MgLevelDesc &L)
   static int resident = 0;
   if (resident == 0) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_sweep<false>, 256, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_sweep, 256, 0);
     resident = (per_sm > 0 ? per_sm : 1) * sm_count_mg();
   }
   const int gx = (L.n[0] + kSX - 1) / kSX, gy = (L.n[1] + kSY - 1) / kSY, nz = L.n[2];
@@ -1710,10 +1704,10 @@ int sweep_chunk_tuned(const MgLevelDesc &L, float *x, float *xb, float *b)
   for (const int c : cand) {
     if (c > nz) continue;
     const dim3 grid(gx, gy, (nz + c - 1) / c);
-    k_rbgs_sweep<false><<<grid, 256, 0, stream()>>>(v, xb, c, idle, 0);  // warm-up
+    k_rbgs_sweep<<<grid, 256, 0, stream()>>>(v, xb, c, idle, 0);  // warm-up
     cudaEventRecord(e0, stream());
     for (int r = 0; r < 3; r++)
-      k_rbgs_sweep<false><<<grid, 256, 0, stream()>>>(v, xb, c, idle, 0);
+      k_rbgs_sweep<<<grid, 256, 0, stream()>>>(v, xb, c, idle, 0);
     cudaEventRecord(e1, stream());
     float ms = 0.0f;
     if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
@@ -1750,7 +1744,7 @@ bool fused_sweeps(MgHierarchy *H, int l, int count, bool zero_first, const MgSta
           H->keep_on_skip);
       if (!launched("k_rb_zero_sweep")) return false;
     } else {
-      k_rbgs_sweep<false><<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st, H->keep_on_skip);
+      k_rbgs_sweep<<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st, H->keep_on_skip);
       if (!launched("k_rbgs_sweep")) return false;
     }
     float *t = H->x32[l];
