@@ -6,19 +6,23 @@
 //  - levels: an axis is halved while its size is even and >= 16;
 //  - operator: 7-point Laplacian, homogeneous Neumann walls applied without
 //    ghost cells (a neighbour outside the domain is the cell itself);
-//  - smoother: red-black Gauss-Seidel, odd cells first, x -= r / diag;
+//  - smoother: red-black, first colour (i + j + k) even (0-based),
+//    x -= omega r / diag (omega = mg_omega; 1 is Gauss-Seidel);
 //  - restriction: average of the children of the residual; prolongation:
 //    trilinear (3/4, 1/4 per coarsened axis), added to x;
-//  - V(pre, post) cycles; coarsest level: fixed sweeps from zero, in shared
-//    memory by one block;
+//  - V(pre, post) cycles; coarsest level solved exactly by a dense inverse
+//    when it has at most kMaxDirect cells, else by fixed sweeps from zero;
 //  - right-hand side made mean-free; stop at ||b - Ap|| <= rtol ||b||.
 //  mg:       all FP64, p itself is the fine-level unknown; the residual norm
 //            is folded in the fine restriction after pre-smoothing.
-//  mg-mixed: FP64 residual of p (norm, mean shift) -> FP32 V-cycle for the
-//            correction from zero -> p += e in FP64, fused into the last
-//            fine post-smoothing pass (iterative refinement).
-// Every kernel returns at once when the device-side done flag is up, so the
-// host queues whole cycles in chunks and reads the state once per chunk.
+//  mg-mixed: FP64 residual of p (norm, mean shift) -> FP32 V-cycles for the
+//            correction until ||r - A e|| <= theta rtol ||b|| (theta =
+//            mg_theta, at most mg_inner cycles) -> p += e in FP64
+//            (iterative refinement; the FP64 residual decides the stop).
+// Every kernel returns at once when the device-side done flag is up. By
+// default each solve is one CUDA graph whose device while-loops run the
+// V-cycles; the host-driven path queues whole cycles in chunks and reads the
+// state once per chunk.
 #include <algorithm>
 #include <array>
 #include <cmath>
