@@ -1685,23 +1685,36 @@ int sweep_chunk_rule(const MgLevelDesc &L)
 // of a few depths over three timed sweeps each, the rule's depth among them.
 int sweep_chunk_tuned(const MgLevelDesc &L, float *x, float *xb, float *b)
 {
-  static std::map<std::array<int, 3>, int> cache;
-  const std::array<int, 3> key = { L.n[0], L.n[1], L.n[2] };
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static std::map<std::array<int, 4>, int> cache;  // (device, nx, ny, nz) -> planes per block
+  const std::array<int, 4> key = { dev, L.n[0], L.n[1], L.n[2] };
   const auto hit = cache.find(key);
   if (hit != cache.end()) return hit->second;
   const int rule = sweep_chunk_rule(L);
-  static MgState *idle = nullptr;  // done = inner_done = 0
-  if (!idle && (cudaMalloc(&idle, sizeof(MgState)) != cudaSuccess ||
-                cudaMemset(idle, 0, sizeof(MgState)) != cudaSuccess)) {
-    idle = nullptr;
-    cudaGetLastError();
-    return rule;
+  static std::map<int, MgState *> idle_state;  // per device: done = inner_done = 0
+  MgState *&idle = idle_state[dev];
+  if (!idle) {
+    MgState *fresh = nullptr;
+    if (cudaMalloc(&fresh, sizeof(MgState)) != cudaSuccess) {
+      cudaGetLastError();
+      return rule;
+    }
+    if (cudaMemset(fresh, 0, sizeof(MgState)) != cudaSuccess) {
+      cudaFree(fresh);
+      cudaGetLastError();
+      return rule;
+    }
+    idle = fresh;
   }
   const int gx = (L.n[0] + kSX - 1) / kSX, gy = (L.n[1] + kSY - 1) / kSY, nz = L.n[2];
   const View<float> v = compact_view<float>(L, x, b);
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    cudaGetLastError();
+    return rule;
+  }
   int kc = rule;
   float best = -1.0f;
   const int cand[] = { rule, 1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64 };
