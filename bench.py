@@ -390,6 +390,26 @@ def _traffic(kernel: str, ncell: int):
         return None
 
 
+# FP64 issue peak of a GB300: 2 FP64 lanes per SM and clock
+# (sm__sass_thread_inst_executed_op_dfma_pred_on.sum.peak_sustained = 304 for 152
+# SMs) at the maximum SM clock of MEASURED_PEAKS.json (2070 MHz)
+FP64_LANES_PER_CLOCK = 304
+
+
+def _fp64_pipe(inst_per_cell: float, ncell: int, ms: float) -> dict:
+    """Achieved FP64 instruction rate of an FP64-pipe-bound kernel (instructions
+    per cell counted from its source) against the GPU's FP64 issue peak."""
+    mhz = 2070.0
+    try:
+        mhz = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["sm_max_mhz"])
+    except Exception:
+        pass
+    peak = FP64_LANES_PER_CLOCK * mhz * 1e6
+    achieved = inst_per_cell * ncell / (ms * 1e-3)
+    return {"fp64_inst_per_cell": inst_per_cell, "fp64_inst_per_s": achieved,
+            "fp64_inst_peak_per_s": peak, "fp64_pipe_frac": achieved / peak}
+
+
 def _roof(name, kernel_key, ms, algo_bytes, ncell, peak, src, **extra):
     achieved = algo_bytes / (ms * 1e-3) / 1e9
     d = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -440,7 +460,8 @@ def kernel_rooflines(sim, solver, stream, ncell):
             abi.check(lib)
             out.append(_roof("k_mx_residual: FP64 residual of p into FP32 (refinement)",
                              "k_mx_residual", msr.value, 20.0 * ncell, ncell, peak, src,
-                             note="FP64-pipe bound"))
+                             note="FP64-pipe bound: 9 FP64 instructions per cell",
+                             fp64=_fp64_pipe(9.0, ncell, msr.value)))
         else:
             out.append(_roof("k_mg_smooth<double>: one colour pass of the fine FP64 smoother",
                              "k_mg_smooth_f64", msr.value, 12.0 * ncell, ncell, peak, src,
@@ -455,9 +476,12 @@ def kernel_rooflines(sim, solver, stream, ncell):
         sim.compute_fg()
     e1.record(stream)
     torch.cuda.synchronize()
-    out.append(_roof("k_fgh_flux: computeFG (FP64)", "k_fgh_flux",
-                     e0.elapsed_time(e1) / reps, 48.0 * ncell, ncell, peak, src,
-                     note="FP64-pipe bound: about 73 FP64 instructions per cell"))
+    ms_fg = e0.elapsed_time(e1) / reps
+    g0 = sim.d.gx == 0.0 and sim.d.gy == 0.0 and sim.d.gz == 0.0
+    fg_inst = 70.4 if g0 else 73.4  # per cell, counted from the kernel (halo share included)
+    out.append(_roof("k_fgh_flux: computeFG (FP64)", "k_fgh_flux", ms_fg, 48.0 * ncell, ncell,
+                     peak, src, note="FP64-pipe bound: about %.0f FP64 instructions per cell"
+                     % fg_inst, fp64=_fp64_pipe(fg_inst, ncell, ms_fg)))
     return out
 
 
