@@ -1,7 +1,8 @@
 // FP64 discretization kernels of the NuSiF time step and the reference
 // entry points that launch them (src/discretization.h:34-41).
 //
-// Layout in HBM: each field is one cudaMalloc'd FP64 array in the reference
+// Layout in HBM: each field is one cudaMalloc'd FP64 array (managed memory kept
+// in HBM with the key host_fields) in the reference
 // layout ((imax+2)(jmax+2)(kmax+2) doubles, i fastest, one ghost layer,
 // src/util.h:19-34). Threads map x -> i so every warp touches consecutive
 // doubles. All arithmetic is FP64 (the reference computes in double).
@@ -633,7 +634,23 @@ void initDiscretization(Discretization *s, Parameter *params)
   double **fields[8] = { &s->u, &s->v, &s->w, &s->p, &s->rhs, &s->f, &s->g, &s->h };
   for (int q = 0; q < 8; q++) {
     *fields[q] = nullptr;
-    if (!cuda_ok(cudaMalloc(fields[q], bytes), "cudaMalloc(field)")) return;
+    if (st->ext.host_fields) {
+      // host_fields: managed memory kept in HBM, so that host code (the
+      // reference's output stage) can read the fields through these pointers
+      if (!cuda_ok(cudaMallocManaged(fields[q], bytes, cudaMemAttachGlobal),
+              "cudaMallocManaged(field)"))
+        return;
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaMemLocation loc = {};
+      loc.type = cudaMemLocationTypeDevice;
+      loc.id = dev;
+      if (!cuda_ok(cudaMemAdvise(*fields[q], bytes, cudaMemAdviseSetPreferredLocation, loc),
+              "cudaMemAdvise(field)"))
+        return;
+    } else if (!cuda_ok(cudaMalloc(fields[q], bytes), "cudaMalloc(field)")) {
+      return;
+    }
   }
   if (!cuda_ok(cudaMalloc(&st->d_scalars, 8 * sizeof(double)), "cudaMalloc(scalars)")) return;
   if (!cuda_ok(cudaMallocHost(&st->h_scalars, 8 * sizeof(double)), "cudaMallocHost(scalars)"))
