@@ -166,6 +166,9 @@ class ClockSampler:
 # mg_theta) - the fastest of the shapes measured at 256^3 with the quadratic
 # warm start.
 MG_SHAPE = {"mg": (2, 2, 4, 1.0), "mg-mixed": (1, 1, 4, 1.3)}
+# learned warm start: once the network's guess lost twice in a row it is
+# evaluated only every LEARNED_PROBE-th step until a guess is taken again
+LEARNED_PROBE = 8
 # the FP64 arm with the same kind of tuning: V(1,2), omega 1.3 (fastest FP64
 # shape measured at 256^3 with the quadratic warm start)
 MG_SHAPE_FP64_TUNED = (1, 2, 4, 1.3)
@@ -775,7 +778,8 @@ def run_learned(args, local):
     evals = {}
     for use in (False, True):
         vals = bench_case(n, "mg-mixed", args.itermax, args.guess)
-        vals.update(re=2750.0, lid=1.25)
+        # the network is probed every 8th step once its guess lost twice in a row
+        vals.update(re=2750.0, lid=1.25, mg_probe=LEARNED_PROBE)
         sim = nusif.Simulation(vals)
         if use:
             sim.set_guess_net(net)
@@ -795,11 +799,15 @@ def run_learned(args, local):
                 u, rw, rg = sim.guess_stats()
                 taken += int(u)
                 ratios.append(rg / rw if rw > 0 else 1.0)
+        counts = sim.guess_counts() if use else (0, 0)
         sim.close()
         evals[use] = {"ms_per_step": ms / args.steps, "v_cycles_per_step": its}
         if use:
             evals[use].update({"guess_taken_steps": taken,
-                               "restricted_residual_ratio_median": float(np.median(ratios))})
+                               "restricted_residual_ratio_median": float(np.median(ratios)),
+                               "network_evaluations_incl_warmup": counts[0],
+                               "guesses_taken_incl_warmup": counts[1],
+                               "probe_every_after_two_rejections": LEARNED_PROBE})
     net.close()
     return {
         "metric": "learned warm start: ms/timestep at %d^3 to 1e-6, mixed-precision MG with vs "

@@ -47,6 +47,14 @@ struct GuessState {
   double *partial = nullptr;
   GuessStats *d_stats = nullptr, *h_stats = nullptr;
   int64_t nc = 0;
+  // key mg_probe P > 1: after two rejections in a row the network runs only
+  // every P-th step until a guess is taken again (the plain warm start is used
+  // in between, as after a rejection)
+  int probe_every = 1;
+  int rejections = 0;     // evaluated steps in a row whose guess lost
+  int skip_left = 0;      // steps to go without the network
+  bool evaluated = false; // the network ran for the current solve
+  long long n_eval = 0, n_taken = 0;
 };
 
 namespace {
@@ -348,6 +356,11 @@ bool features(GuessState *gs, const GGeom &g, const double *p, const double *rhs
 bool guess_before_solve(GuessState *gs, const Grid *grid, double *p, const double *rhs)
 {
   if (!gs || (!gs->net && !gs->recording)) return true;
+  gs->evaluated = false;
+  if (!gs->recording && gs->skip_left > 0) {  // backed off: the plain warm start only
+    gs->skip_left--;
+    return true;
+  }
   if (!ensure(gs, grid)) return false;
   const GGeom g = geom(grid);
   const int64_t padded = (int64_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
@@ -370,12 +383,28 @@ bool guess_before_solve(GuessState *gs, const Grid *grid, double *p, const doubl
   k_g_fold_select<<<1, 1, 0, stream()>>>(gs->partial, nb, gs->d_stats);
   if (!launched("k_g_fold_select")) return false;
   k_g_take<<<flat(padded), 256, 0, stream()>>>(p, gs->aux, padded, gs->d_stats);
-  return launched("k_g_take");
+  if (!launched("k_g_take")) return false;
+  // the outcome reaches the host with the solve's own synchronisation
+  gs->evaluated = true;
+  return cuda_ok(cudaMemcpyAsync(gs->h_stats, gs->d_stats, sizeof(GuessStats),
+                     cudaMemcpyDeviceToHost, stream()),
+      "guess outcome");
 }
 
 bool guess_after_solve(GuessState *gs, const Grid *grid, const double *p)
 {
-  if (!gs || !gs->recording) return true;
+  if (!gs) return true;
+  if (gs->evaluated) {  // the solve has synchronised: h_stats holds this step's outcome
+    gs->evaluated = false;
+    gs->n_eval++;
+    if (gs->h_stats->used) {
+      gs->n_taken++;
+      gs->rejections = 0;
+    } else if (++gs->rejections >= 2 && gs->probe_every > 1) {
+      gs->skip_left = gs->probe_every - 1;
+    }
+  }
+  if (!gs->recording) return true;
   gs->recording = false;
   const GGeom g = geom(grid);
   k_g_target<<<flat(gs->nc), 256, 0, stream()>>>(g, p, gs->aux, gs->d_stats, gs->rec_t);
@@ -402,7 +431,10 @@ GuessState *guess_state_for(Solver *s)
     fail(NUSIF_ERR_STATE, "learned warm start: needs a solver initialised with mg or mg-mixed");
     return nullptr;
   }
-  if (!ss->guess) ss->guess = new GuessState();
+  if (!ss->guess) {
+    ss->guess = new GuessState();
+    ss->guess->probe_every = ss->ext.mg_guess_probe > 1 ? ss->ext.mg_guess_probe : 1;
+  }
   return ss->guess;
 }
 
@@ -418,6 +450,17 @@ int nusifSolverSetGuessNet(Solver *s, NusifUNet *net)
   GuessState *gs = guess_state_for(s);
   if (!gs) return NUSIF_ERR_STATE;
   gs->net = net;
+  gs->rejections = gs->skip_left = 0;
+  gs->n_eval = gs->n_taken = 0;
+  return NUSIF_OK;
+}
+
+int nusifSolverGuessCounts(Solver *s, long long *evaluated, long long *taken)
+{
+  GuessState *gs = guess_state_for(s);
+  if (!gs) return NUSIF_ERR_STATE;
+  if (evaluated) *evaluated = gs->n_eval;
+  if (taken) *taken = gs->n_taken;
   return NUSIF_OK;
 }
 

@@ -40,6 +40,7 @@ struct Extras {
   int mg_tail = 0;           // levels of at most this many cells run as one kernel (0: off)
   int mg_chunk = 0;          // planes per block of the FP32 one-kernel sweep (0: autotuned)
   int host_fields = 0;       // 1: fields in managed memory (host-readable pointers)
+  int mg_guess_probe = 1;    // key mg_probe: learned guess every P-th step after 2 rejections
   int mg_maxcycles = 100;
 };
 Extras *extras_for(const Parameter *p, bool create);

@@ -104,6 +104,7 @@ int apply_extra(Parameter *param, const char *tok, const char *val)
   if (starts_with(tok, "mg_tail")) { x->mg_tail = atoi(v); hit = 1; }
   if (starts_with(tok, "mg_chunk")) { x->mg_chunk = atoi(v); hit = 1; }
   if (starts_with(tok, "host_fields")) { x->host_fields = atoi(v); hit = 1; }
+  if (starts_with(tok, "mg_probe")) { x->mg_guess_probe = atoi(v); hit = 1; }
   if (starts_with(tok, "mg_guess")) {
     if (strcmp(v, "previous") == 0) x->mg_guess = 0;
     else if (strcmp(v, "extrapolate") == 0) x->mg_guess = 1;

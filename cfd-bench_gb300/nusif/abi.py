@@ -132,6 +132,8 @@ SIGNATURES = [
     ("nusifSolverRecordPair", C.c_int, [C.POINTER(Solver), C.c_void_p, C.c_void_p]),
     ("nusifSolverGuessStats", C.c_int, [C.POINTER(Solver), C.POINTER(C.c_int),
                                         C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    ("nusifSolverGuessCounts", C.c_int, [C.POINTER(Solver), C.POINTER(C.c_longlong),
+                                         C.POINTER(C.c_longlong)]),
 ]
 
 _lib = None

@@ -124,6 +124,13 @@ class Simulation:
         abi.check(self.lib)
         return bool(used.value), rw.value, rg.value
 
+    def guess_counts(self) -> tuple[int, int]:
+        """(network evaluations, guesses taken) since set_guess_net."""
+        ev, tk = C.c_longlong(), C.c_longlong()
+        self.lib.nusifSolverGuessCounts(C.byref(self.s), C.byref(ev), C.byref(tk))
+        abi.check(self.lib)
+        return ev.value, tk.value
+
     def solve(self) -> float:
         res = self.lib.solve(C.byref(self.s), self.d.p, self.d.rhs)
         abi.check(self.lib)

@@ -281,6 +281,12 @@ NUSIF_API int nusifSolverRecordPair(Solver *s, float *x, float *t);
  * restricted residuals ||R(b - A p)|| / ||R b|| (b mean-free) of the plain
  * warm start and of the guess (the decision criterion) */
 NUSIF_API int nusifSolverGuessStats(Solver *s, int *used, double *rel_warm, double *rel_guess);
+/* Network evaluations and taken guesses since the last nusifSolverSetGuessNet.
+ * With the .par key mg_probe P > 1 the network runs, after two rejections in a
+ * row, only every P-th step until a guess is taken again (in between the
+ * plain warm start is used, as after a rejection; nusifSolverGuessStats keeps
+ * the last evaluated step's figures). */
+NUSIF_API int nusifSolverGuessCounts(Solver *s, long long *evaluated, long long *taken);
 
 #ifdef __cplusplus
 }

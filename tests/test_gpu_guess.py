@@ -119,3 +119,25 @@ def test_trained_guess_gains(nusif_lib, guess):
     assert taken >= 20, (taken, ratio)
     assert np.median(ratio) < 0.9, ratio
     assert cyc[True] <= cyc[False], cyc
+
+
+def test_probe_backs_off_after_rejections(nusif_lib):
+    """mg_probe 4: a network whose guess always loses runs in steps 1 and 2,
+    then - after two rejections in a row - only every 4th step (6 and 10 of
+    12); in between the plain warm start is used, so the run stays
+    bit-identical to one without a network."""
+    from nusif import Simulation, UNet
+    from nusif.params import cavity
+    vals = cavity(16, re=800.0, te=1e9, solver="mg-mixed", rtol=1e-7, mg_probe=4)
+    with UNet(seed=2) as net:
+        p = net.params()
+        p[-(27 * 16 + 1):] = 0.0  # output layer weights and bias: p1 = p0, never better
+        net.set_params(p)
+        with Simulation(vals) as a, Simulation(vals) as b:
+            b.set_guess_net(net)
+            for _ in range(12):
+                ia, ib = a.step(), b.step()
+                assert ia.it == ib.it
+            assert b.guess_counts() == (4, 0)
+            for f in "uvwp":
+                np.testing.assert_array_equal(a.field(f), b.field(f))
