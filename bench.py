@@ -78,6 +78,14 @@ def parse_args():
                     help="skip the FP64 multigrid comparison run")
     ap.add_argument("--itermax", type=int, default=None,
                     help="cap of the red-black iterations per step (short profiling runs)")
+    ap.add_argument("--rb-steps", type=int, default=2,
+                    help="time steps of the like-for-like red-black arm (the reference's solver "
+                         "on the GPU, itermax 10000: about 3.6 s per step at 256^3); 0 skips it")
+    ap.add_argument("--error-steps", type=int, default=None,
+                    help="steps of the field-error study of the headline solver against FP64 "
+                         "multigrid (default: warmup + steps)")
+    ap.add_argument("--ref-sweeps", type=int, default=100,
+                    help="red-black sweeps timed per step by the reference arm")
     return ap.parse_args()
 
 
@@ -287,11 +295,22 @@ def run_gpu(args, rank, world, local):
                             "ms_per_step": ref64["ms_per_step"],
                             "v_cycles_per_step": ref64["iters"],
                             "residual_per_step": ref64["res"],
-                            "speedup_of_value": ref64["ms_per_step"] / head["ms_per_step"]})
+                            "speedup_of_value": ref64["ms_per_step"] / head["ms_per_step"],
+                            "mlups": mlups(ref64["iters"], ncell, ref64["ms_per_step"])})
+
+    errors = None
+    if solver != "mg" and solver.startswith("mg") and not args.no_compare and rank == 0:
+        n_err = args.error_steps if args.error_steps is not None else args.warmup + args.steps
+        if n_err > 0:
+            errors = field_error_study(args, stream, solver, n_err)
+
+    rb = None
+    if solver != "rb" and args.rb_steps > 0 and not args.no_compare:
+        rb = rb_arm(args, stream, local, world)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(vals, solver, head["iters"])
+        cpu = cpu_baseline(vals, solver, head["iters"], args.ref_sweeps)
 
     if rank != 0:
         return None
@@ -327,8 +346,11 @@ def run_gpu(args, rank, world, local):
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "solver_iterations_per_step": head["iters"],
         "residual_per_step": head["res"],
+        "mlups": mlups(head["iters"], ncell, head["ms_per_step"]),
         "compare_fp64_mg": compare,
-        "roofline": roofs[0] if roofs else None,
+        "error_vs_fp64_mg": errors,
+        "compare_rb": rb,
+        "roofline": dominant(roofs),
         "roofline_kernels": roofs,
         "phases": phases,
         "e2e": e2e,
@@ -337,6 +359,91 @@ def run_gpu(args, rank, world, local):
         "cpu_baseline": cpu,
     }
     return out
+
+
+def mlups(iters: list[int], ncell: int, ms_per_step: float) -> dict:
+    """The reference's solver throughput, MLUPS = iterations x imax*jmax*kmax x
+    1e-6 / solver seconds (src/profiler.c:61-74), with the whole step's time
+    as the denominator (so a lower bound of the solver-only figure); for the
+    multigrid solvers an iteration is one V-cycle or refinement unit. Also the
+    time-step rate, cells x steps / seconds."""
+    it = sum(iters) / max(len(iters), 1)
+    sec = ms_per_step * 1e-3
+    return {"solver_mlups": it * ncell * 1e-6 / sec if sec > 0 else None,
+            "iterations_per_step": it,
+            "timestep_mlups": ncell * 1e-6 / sec if sec > 0 else None,
+            "definition": "iterations x cells x 1e-6 / step seconds (src/profiler.c:61-74, "
+                          "whole step as the solver time)"}
+
+
+def field_error_study(args, stream, solver: str, steps: int) -> dict:
+    """The headline solver and FP64 multigrid (V(2,2), same rtol and warm
+    start) stepped side by side from rest: after every step the L2 and Linf
+    differences of u, v, w (relative to the FP64 velocity field as a whole)
+    and of the mean-free p (relative to the FP64 mean-free p)."""
+    import torch
+
+    import nusif
+    sims = {"test": nusif.Simulation(bench_case(args.n, solver, args.itermax, args.guess)),
+            "fp64": nusif.Simulation(bench_case(args.n, "mg", args.itermax, args.guess))}
+    shape = sims["fp64"].padded_shape
+
+    def view(sim, f):
+        return torch.as_tensor(DeviceArray(getattr(sim.d, f), shape),
+                               device="cuda")[1:-1, 1:-1, 1:-1]
+
+    err = {f: {"l2": [], "linf": []} for f in "uvwp"}
+    for _ in range(steps):
+        for sim in sims.values():
+            sim.step()
+        torch.cuda.synchronize()
+        vel = {f: view(sims["fp64"], f) for f in "uvw"}
+        vel_l2 = float(torch.sqrt(sum(torch.linalg.vector_norm(vel[f]) ** 2 for f in "uvw")))
+        vel_max = float(max(vel[f].abs().max() for f in "uvw"))
+        for f in "uvwp":
+            a, b = view(sims["test"], f), view(sims["fp64"], f)
+            if f == "p":
+                a, b = a - a.mean(), b - b.mean()
+                l2_ref, max_ref = float(torch.linalg.vector_norm(b)), float(b.abs().max())
+            else:
+                l2_ref, max_ref = vel_l2, vel_max
+            d = a - b
+            err[f]["l2"].append(float(torch.linalg.vector_norm(d)) / max(l2_ref, 1e-300))
+            err[f]["linf"].append(float(d.abs().max()) / max(max_ref, 1e-300))
+    for sim in sims.values():
+        sim.close()
+    return {"against": "FP64 multigrid V(2,2), same rtol 1e-6 and warm start, stepped alongside",
+            "steps": steps,
+            "max": {f: {k: max(v) for k, v in err[f].items()} for f in "uvwp"},
+            "final": {f: {k: v[-1] for k, v in err[f].items()} for f in "uvwp"},
+            "per_step_l2": {f: err[f]["l2"] for f in "uvwp"}}
+
+
+def rb_arm(args, stream, local, world) -> dict:
+    """The drop-in with the reference's own solver: red-black SOR (omega 1.7,
+    eps 1e-6, itermax 10000) on the GPU, the like-for-like counterpart of the
+    reference arm; args.rb_steps time steps from rest after one untimed step."""
+    import torch
+
+    import nusif
+    vals = bench_case(args.n, "rb", args.itermax)
+    sim = nusif.Simulation(vals)
+    sim.step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    infos = [sim.step() for _ in range(args.rb_steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.rb_steps
+    ncell = vals["imax"] * vals["jmax"] * vals["kmax"]
+    sim.close()
+    its = [i.it for i in infos]
+    return {"solver": "rb (the reference's red-black SOR, omega 1.7, eps 1e-6, itermax %d)"
+                      % vals["itermax"],
+            "steps_timed": args.rb_steps, "ms_per_step": ms, "iterations_per_step": its,
+            "ms_per_sweep": ms / (sum(its) / len(its)) if sum(its) else None,
+            "mlups": mlups(its, ncell, ms)}
 
 
 def step_phases(sim, solver, stream, steps: int = 10) -> dict:
@@ -384,13 +491,27 @@ def step_phases(sim, solver, stream, steps: int = 10) -> dict:
     return out
 
 
+def _profile_entry(kernel: str) -> dict:
+    try:
+        return json.loads(TRAFFIC.read_text()).get(kernel) or {}
+    except Exception:
+        return {}
+
+
 def _traffic(kernel: str, ncell: int):
     """DRAM bytes per launch of a kernel from the committed ncu summary, scaled by cells."""
-    try:
-        entry = json.loads(TRAFFIC.read_text()).get(kernel)
-        return entry["bytes_per_cell_per_launch"] * ncell if entry else None
-    except Exception:
+    entry = _profile_entry(kernel)
+    b = entry.get("bytes_per_cell_per_launch")
+    return b * ncell if b is not None else None
+
+
+def dominant(roofs: list[dict]):
+    """The entry of the kernel with the largest share of the step's device time
+    (the share measured in the committed ncu launch list of the same step);
+    ties or missing shares keep the first entry."""
+    if not roofs:
         return None
+    return max(roofs, key=lambda r: r.get("share_of_step") or 0.0)
 
 
 # FP64 issue peak of a GB300: 2 FP64 lanes per SM and clock
@@ -415,10 +536,13 @@ def _fp64_pipe(inst_per_cell: float, ncell: int, ms: float) -> dict:
 
 def _roof(name, kernel_key, ms, algo_bytes, ncell, peak, src, **extra):
     achieved = algo_bytes / (ms * 1e-3) / 1e9
+    prof = _profile_entry(kernel_key)
     d = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
          "frac": achieved / peak, "traffic": _traffic(kernel_key, ncell), "kernel": name,
          "launch_ms": ms, "algorithmic_bytes_per_launch": algo_bytes,
-         "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else src}
+         "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else src,
+         "share_of_step": prof.get("share_of_step"),
+         "ncu_fp64_pipe_frac": prof.get("fp64_pipe_frac")}
     d.update(extra)
     return d
 
@@ -516,64 +640,113 @@ def run_e2e(sim, args, stream, padded):
 
 # ---------------------------------------------------------------- CPU side
 
-def cpu_step_estimate(vals, iters_per_step, fast=True):
-    """One time step of the reference algorithm on one host core, estimated
-    from a bounded sample: the non-solver operators once, plus a fixed number
-    of red-black iterations scaled to the per-step iteration count."""
-    import numpy as np
-    import oracle
-    kind = "port"
-    run = oracle.OracleRun(dict(vals, itermax=1), "rb", fast=fast)
-    lib = run.lib
-    st = run.st
-    g = st.g
-    n = int(np.prod(run.shape))
-    t0 = time.perf_counter()
-    # non-solver part of src/main.c:61-72,72: CFL, BCs, F/G/H, RHS, adaptUV
-    dt = lib.or_timestep(st.dtBound, g.dx, g.dy, g.dz, lib.or_max_abs(st.u, n),
-                         lib.or_max_abs(st.v, n), lib.or_max_abs(st.w, n), st.c.tau)
-    lib.or_set_bc(C.byref(g), st.c.bc, st.u, st.v, st.w)
-    lib.or_special_bc(C.byref(g), st.c.problem, C.c_double(st.c.lid), C.c_double(st.c.inflow), st.u)
-    d = C.c_double
-    lib.or_compute_fgh(C.byref(g), d(st.c.re), d(st.c.gamma), d(st.c.gx), d(st.c.gy), d(st.c.gz),
-                       d(dt), st.u, st.v, st.w, st.f, st.gf, st.h)
-    lib.or_compute_rhs(C.byref(g), d(dt), st.f, st.gf, st.h, st.rhs)
-    lib.or_adapt_uv(C.byref(g), d(dt), st.f, st.gf, st.h, st.p, st.u, st.v, st.w)
-    t_ns = time.perf_counter() - t0
-    sample_it = 8
-    res = C.c_double()
-    t0 = time.perf_counter()
-    lib.or_solve_rb(C.byref(g), 0.0, st.c.omega, sample_it, st.p, st.rhs, C.byref(res))
-    t_it = (time.perf_counter() - t0) / sample_it
-    run.close()
-    per_step = t_ns + iters_per_step * t_it
-    return per_step * 1e3, t_ns, t_it, kind, sample_it
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
 
 
-def cpu_baseline(vals, solver, gpu_iters):
-    import oracle
+class CpuStepSampler:
+    """The reference algorithm's time step on one host core, through the
+    oracle's C restatement built with the reference's flags (-O3 -ffast-math):
+    the non-solver operators once (src/main.c:61-70,79: CFL, boundary
+    conditions, F/G/H, RHS, adaptUV) and a bounded number of red-black SOR
+    iterations (src/solver-rb.c:54-160), timed separately. The state stays
+    allocated between samples; the iterations run on the state's own p and
+    rhs with eps 0, so none stops early."""
+
+    def __init__(self, vals, fast=True):
+        import numpy as np
+        import oracle
+        self.run = oracle.OracleRun(dict(vals, itermax=1), "rb", fast=fast)
+        self.n = int(np.prod(self.run.shape))
+
+    def sample(self, sweeps: int) -> tuple[float, float]:
+        """(seconds of the non-solver operators, seconds of `sweeps` iterations)."""
+        lib, st = self.run.lib, self.run.st
+        g, n, d = st.g, self.n, C.c_double
+        t0 = time.perf_counter()
+        dt = lib.or_timestep(st.dtBound, g.dx, g.dy, g.dz, lib.or_max_abs(st.u, n),
+                             lib.or_max_abs(st.v, n), lib.or_max_abs(st.w, n), st.c.tau)
+        lib.or_set_bc(C.byref(g), st.c.bc, st.u, st.v, st.w)
+        lib.or_special_bc(C.byref(g), st.c.problem, d(st.c.lid), d(st.c.inflow), st.u)
+        lib.or_compute_fgh(C.byref(g), d(st.c.re), d(st.c.gamma), d(st.c.gx), d(st.c.gy),
+                           d(st.c.gz), d(dt), st.u, st.v, st.w, st.f, st.gf, st.h)
+        lib.or_compute_rhs(C.byref(g), d(dt), st.f, st.gf, st.h, st.rhs)
+        lib.or_adapt_uv(C.byref(g), d(dt), st.f, st.gf, st.h, st.p, st.u, st.v, st.w)
+        t_ns = time.perf_counter() - t0
+        res = C.c_double()
+        t0 = time.perf_counter()
+        if sweeps > 0:
+            lib.or_solve_rb(C.byref(g), 0.0, st.c.omega, sweeps, st.p, st.rhs, C.byref(res))
+        return t_ns, time.perf_counter() - t0
+
+    def close(self):
+        self.run.close()
+
+
+def cpu_baseline(vals, solver, gpu_iters, sweeps: int = 100):
     it = float(sum(gpu_iters)) / max(len(gpu_iters), 1) if solver == "rb" else float(vals["itermax"])
-    ms, t_ns, t_it, kind, sample_it = cpu_step_estimate(vals, it)
-    return {"value": ms, "unit": UNIT, "cores": 1, "kind": kind,
-            "sample": (f"one pass of the non-solver operators ({t_ns:.2f} s) plus {sample_it} "
+    smp = CpuStepSampler(vals)
+    try:
+        t_ns, t_sw = smp.sample(sweeps)
+    finally:
+        smp.close()
+    t_it = t_sw / max(sweeps, 1)
+    ms = (t_ns + it * t_it) * 1e3
+    return {"value": ms, "unit": UNIT, "cores": 1, "kind": "port", "cpu_model": cpu_model(),
+            "extrapolated": True, "sweeps_timed": sweeps, "sweeps_per_step_assumed": it,
+            "timed_s": t_ns + t_sw,
+            "sample": (f"one pass of the non-solver operators ({t_ns:.2f} s) plus {sweeps} "
                        f"red-black SOR iterations ({t_it * 1e3:.1f} ms each) at "
                        f"{vals['imax']}^3 on one host core, scaled to {it:.0f} iterations per "
                        f"step (the reference's red-black solve for this case)")}
 
 
 def run_reference(args, rank, world):
+    """The reference's CPU code path for the benchmark step: each step times
+    the non-solver operators once and args.ref_sweeps red-black iterations
+    on one core, and `value` extrapolates the step to the reference's
+    itermax = 10000 iterations (every step of this case reaches itermax in
+    the reference: tests/golden/config2_rb.npz)."""
     if rank != 0:
         return None
     solver = pick_solver(args.solver)
     vals = bench_case(args.n, solver, args.itermax)
     it = float(vals["itermax"])
-    samples = []
-    for s in range(args.warmup + args.steps):
-        ms, t_ns, t_it, kind, sample_it = cpu_step_estimate(vals, it)
-        if s >= args.warmup:
-            samples.append(ms)
-    ms = sum(samples) / len(samples)
+    sweeps = args.ref_sweeps
+    smp = CpuStepSampler(vals)
+    ns, sw, wall = [], [], 0.0
+    try:
+        for s in range(args.warmup + args.steps):
+            # warm-up steps run the operators and one sweep only (they warm caches and pages)
+            t_ns, t_sw = smp.sample(sweeps if s >= args.warmup else 1)
+            if s >= args.warmup:
+                ns.append(t_ns)
+                sw.append(t_sw)
+                wall += t_ns + t_sw
+    finally:
+        smp.close()
+    t_ns = sum(ns) / len(ns)
+    t_it = sum(sw) / (len(sw) * max(sweeps, 1))
+    ms = (t_ns + it * t_it) * 1e3
     n = vals["imax"]
+    sample = (f"per step: the non-solver operators once ({t_ns:.2f} s) plus {sweeps} red-black "
+              f"iterations ({t_it * 1e3:.1f} ms each), extrapolated to {it:.0f} iterations "
+              f"(the reference's algorithm, oracle C restatement compiled with -O3 -ffast-math, "
+              f"sequential, one core)")
     return {
         "impl": "reference",
         "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": world,
@@ -583,11 +756,13 @@ def run_reference(args, rank, world):
         "config": {"workload": f"lid-driven cavity {n}x{n}x{n}, Re 1000, tau 0.5, "
                                f"reference red-black SOR solve (omega 1.7, eps 1e-6, itermax 10000)",
                    "cells": n ** 3, "solver": "rb (reference)"},
-        "cpu_baseline": {"value": ms, "unit": UNIT, "cores": 1, "kind": kind,
-                         "sample": (f"per step: the non-solver operators once plus {sample_it} "
-                                    f"red-black iterations, scaled to {it:.0f} iterations "
-                                    f"(the reference's own C code path compiled with "
-                                    f"-O3 -ffast-math, sequential)")},
+        "extrapolated": True, "sweeps_timed_per_step": sweeps,
+        "sweeps_per_step_assumed": it, "timed_region_s": wall,
+        "ms_per_sweep": t_it * 1e3, "non_solver_ms": t_ns * 1e3,
+        "mlups": {"solver_mlups": n ** 3 * 1e-6 / t_it,
+                  "definition": "iterations x cells x 1e-6 / solver seconds (src/profiler.c:61-74)"},
+        "cpu_baseline": {"value": ms, "unit": UNIT, "cores": 1, "kind": "port",
+                         "cpu_model": cpu_model(), "sample": sample},
         "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 

@@ -1,24 +1,30 @@
 // Red-black SOR solve that allocates no memory.
 //
-// Some callers cannot call cudaMalloc: code that runs inside a CUDA graph
-// being captured (allocation breaks or is forbidden during capture), solver
-// hosts that hand out only pre-sized device buffers and forbid growth, or
-// embedded runtimes that pre-allocate everything at start-up. They still pass
-// their own pressure and right-hand-side arrays; the per-block partial sums,
-// the ticket counter and the convergence state that solve() keeps in
-// cudaMalloc'd scratch live here instead in one file-scope __device__ array
-// of fixed size. Every GPU that loads the library holds that array until the
+// Some callers cannot call cudaMalloc: solver hosts that hand out only
+// pre-sized device buffers and forbid growth after start-up, embedded or
+// plug-in runtimes that reserve all device memory when they initialise, and
+// services that must not fail a request on an out-of-memory error. They still
+// pass their own pressure and right-hand-side arrays; the per-block partial
+// sums, the ticket counter and the convergence state that solve() keeps in
+// cudaMalloc'd scratch live here instead in one file-scope __device__ array of
+// fixed size. Every GPU that loads the library holds that array until the
 // process exits.
 //
 // The array's name in host code is only a host-side stand-in, not a device
 // address, so it is never passed to a kernel. The first call on each device
 // (with that device current) looks up the real address with
-// cudaGetSymbolAddress and remembers it; make that first call before any
-// stream capture, because the lookup itself is not a stream operation.
+// cudaGetSymbolAddress and keeps it; make that first call before any stream
+// capture, because the lookup is not a stream operation. The kept address is
+// only valid for the device context it was looked up in: do not call
+// cudaDeviceReset on a device between calls of this function.
+//
+// Like solve(), the function reads the convergence state back to the host
+// and synchronises the library's stream after every chunk of iterations.
 //
 // All calls share the one array and it keeps the last call's contents: each
 // call first resets the counter and the convergence state it reads. Calls
 // that overlap on the GPU (two streams, two host threads) race on the array.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 
@@ -38,7 +44,9 @@ static_assert(sizeof(SolveState) <= kStateBytes, "solve state does not fit its s
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticBytes];
 
 constexpr int kMaxDevices = 64;
-static unsigned char *g_scratch_addr[kMaxDevices];  // device address, per device ordinal
+// device address per device ordinal; atomic because host threads may call
+// concurrently on different devices (the address is the same for every thread)
+static std::atomic<unsigned char *> g_scratch_addr[kMaxDevices];
 
 __global__ void k_static_init(SolveState *st, unsigned *ticket, double epssq, int itermax,
     double ncell)
@@ -62,13 +70,15 @@ unsigned char *static_scratch()
     fail(NUSIF_ERR_ARG, "nusifSolveRBStatic: device ordinal %d beyond %d", dev, kMaxDevices);
     return nullptr;
   }
-  if (g_scratch_addr[dev] == nullptr) {
+  unsigned char *addr = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (addr == nullptr) {
     void *ptr = nullptr;
     if (!cuda_ok(cudaGetSymbolAddress(&ptr, g_static_scratch), "cudaGetSymbolAddress(scratch)"))
       return nullptr;
-    g_scratch_addr[dev] = static_cast<unsigned char *>(ptr);
+    addr = static_cast<unsigned char *>(ptr);
+    g_scratch_addr[dev].store(addr, std::memory_order_release);
   }
-  return g_scratch_addr[dev];
+  return addr;
 }
 
 }  // namespace

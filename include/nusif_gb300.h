@@ -5,7 +5,10 @@
  * and solver-{rb,mg}.o of HPC-Dwarfs/CFD-Bench ("NuSiF", src/). The entry
  * points below have the reference names, signatures, argument meaning and
  * error behaviour; the structs have the reference member order and types, so
- * an unchanged src/main.c links against the library.
+ * an unchanged src/main.c links against the library: link main.o and the
+ * reference's remaining objects (comm.o, allocate.o, timing.o, progress.o,
+ * profiler.o, vtkWriter-seq.o) with -L<lib dir> -lnusif_gb300 -lcudart -lstdc++
+ * in place of parameter.o, discretization.o and solver-*.o.
  *
  * Differences a caller must know:
  *  - The field pointers in Discretization (p, rhs, f, g, h, u, v, w) are
@@ -169,14 +172,16 @@ NUSIF_API void nusifFreeSolver(Solver *s);
 /* Red-black SOR solve that allocates no memory. No counterpart in the
  * reference. Same result as solve() with the rb solver on the same p, rhs
  * (device arrays in the padded layout) and parameters, for callers that cannot
- * call cudaMalloc (a CUDA graph under capture, hosts that forbid device
- * allocation after start-up). Its scratch is a fixed 256.5 KiB __device__
- * array of the library: grids needing more than 32768 per-block partial sums
- * (larger than about 512^3 cells) are rejected with NUSIF_ERR_ARG. The first
- * call on a device looks up that array's address and should come before any
- * stream capture.
- * Calls share the array: calls that overlap on the GPU race. Returns a
- * NUSIF_* code; *res_out and *it_out get solve()'s residual and iterations. */
+ * call cudaMalloc (hosts that hand out only pre-sized device buffers, runtimes
+ * that reserve all device memory at start-up). Its scratch is a fixed
+ * 256.5 KiB __device__ array of the library: grids needing more than 32768
+ * per-block partial sums (larger than about 512^3 cells) are rejected with
+ * NUSIF_ERR_ARG. The first call on a device looks up that array's address and
+ * should come before any stream capture; do not reset the device between
+ * calls. Like solve(), it synchronises the library's stream after every chunk
+ * of iterations. Calls share the array: calls that overlap on the GPU race.
+ * Returns a NUSIF_* code; *res_out and *it_out get solve()'s residual and
+ * iterations. */
 NUSIF_API int nusifSolveRBStatic(double *p, const double *rhs, int imax, int jmax, int kmax,
     double dx, double dy, double dz, double omega, double eps, int itermax, double *res_out,
     int *it_out);

@@ -21,6 +21,20 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 REF_DIR = HERE / "_ref"
+
+
+def reference_source_root() -> Path | None:
+    """The reference tree oracle/build_ref.sh compiled from (NUSIF_REFERENCE
+    overrides it), or None where the reference has not been built here."""
+    env = os.environ.get("NUSIF_REFERENCE")
+    if env:
+        return Path(env)
+    rec = REF_DIR / "source_root.txt"
+    if rec.exists():
+        root = Path(rec.read_text().strip())
+        if (root / "src").is_dir():
+            return root
+    return None
 LIB_STRICT = HERE / "liboracle.so"
 LIB_FAST = HERE / "liboracle_fast.so"
 SRC = HERE / "nusif_oracle.c"

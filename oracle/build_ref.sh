@@ -2,12 +2,15 @@
 # Builds the reference NuSiF sources, where they lie, into oracle/_ref/ --
 # test infrastructure only (the checker and the CPU baseline), never the product.
 #
-#   oracle/build_ref.sh [REFERENCE_ROOT]      (default: /root/reference)
+#   oracle/build_ref.sh [REFERENCE_ROOT]
+#       (default: $NUSIF_REFERENCE, else /root/reference; with NUSIF_REF_OPTIONAL=1
+#        a missing source tree exits 0 without building)
 #
 # Outputs (git-ignored; nothing is written into the reference tree):
 #   _ref/libnusif_ref_rb.so   reference objects + oracle/ref_driver.c, SOLVER=rb
 #   _ref/libnusif_ref_mg.so   the same with SOLVER=mg
 #   _ref/NusifSolver-rb, _ref/NusifSolver-mg   the reference program itself
+#   _ref/source_root.txt      the reference root the sources were read from
 #
 # Flags follow the reference's sequential GCC build (config.mk, mk/include_GCC.mk:
 # -O3 -ffast-math -std=c99 -D_GNU_SOURCE -DARRAY_ALIGNMENT=64 -DVERBOSE), minus
@@ -15,11 +18,13 @@
 # The libraries are built twice: "strict" (-O2, no fast-math, no FMA contraction)
 # pins the oracle bit-for-bit; "fast" keeps the reference's own flags for timing.
 set -euo pipefail
-REF="${1:-/root/reference}"
+REF="${1:-${NUSIF_REFERENCE:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 SRC="$REF/src"
 if [ ! -f "$SRC/solver-rb.c" ]; then
+  # NUSIF_REF_OPTIONAL=1: a machine without the sources (the GPU machine) is not an error
+  if [ "${NUSIF_REF_OPTIONAL:-0}" = "1" ]; then exit 0; fi
   echo "build_ref: reference sources not found under $SRC" >&2
   exit 2
 fi
@@ -51,4 +56,7 @@ for solver in rb mg; do
   "$CC" $COMMON $FAST -o "$OUT/NusifSolver-$solver" \
     $(for f in $LIBSRC main.c vtkWriter-seq.c solver-$solver.c; do echo "$SRC/$f"; done) -lm
 done
+# where the sources were found, for the tests that compile reference files
+# themselves (layout probe, link test)
+(cd "$REF" && pwd) > "$OUT/source_root.txt"
 echo "build_ref: wrote $(ls "$OUT" | tr '\n' ' ')"

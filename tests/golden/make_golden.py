@@ -123,6 +123,45 @@ def config1_run() -> None:
     print(f"config1_rb: {len(its)} steps, {sum(its)} iterations")
 
 
+# sampled cells of a 258^3 padded field: every 9th index on each axis, ghosts
+# included (0, 9, ..., 252), so both red-black colours and the walls appear
+CONFIG2_STRIDE = 9
+
+
+def config2_run(solver: str, steps: int) -> None:
+    """The 256^3 benchmark cavity (Re 1000, tau 0.5, gamma 0.9) stepped by the
+    reference: red-black SOR with omega 1.7, eps 1e-6, itermax 10000 (about 15
+    minutes of one core per step), or the reference's multigrid build with 6
+    levels and 2 + 2 sweeps. Stored per step: iterations, residual, dt, t; after
+    every step the u, v, w, p samples on a stride-9 lattice of the padded array
+    and whole-interior sums and sums of squares."""
+    vals = cavity(256, re=1000.0, tau=0.5, te=1e9, omg=1.7, eps=1e-6, itermax=10000,
+                  gamma=0.9, levels=6, presmooth=2, postsmooth=2)
+    name = "config2_rb" if solver == "rb" else "config2_mgref"
+    with tempfile.TemporaryDirectory() as d:
+        par = write_par(Path(d) / "config2.par", vals)
+        ref = oracle.RefDriver(par, solver, fast=True)
+        rec = {"it": [], "res": [], "dt": [], "t": []}
+        out = {}
+        sl = (slice(0, None, CONFIG2_STRIDE),) * 3
+        for s in range(1, steps + 1):
+            it, res, dt, t = ref.step()
+            for key, v in zip(("it", "res", "dt", "t"), (it, res, dt, t)):
+                rec[key].append(v)
+            for f in "uvwp":
+                a = ref.field(f)
+                out[f"{f}_sample_{s}"] = a[sl].copy()
+                inner = a[1:-1, 1:-1, 1:-1]
+                out[f"{f}_sum_{s}"] = np.array(inner.sum())
+                out[f"{f}_sumsq_{s}"] = np.array((inner * inner).sum())
+            print(f"{name}: step {s} it={it} res={res!r}", flush=True)
+    np.savez_compressed(OUT / f"{name}.npz", values=np.array(repr(vals)),
+                        solver=np.array(solver), stride=np.array(CONFIG2_STRIDE),
+                        it=np.array(rec["it"], dtype=np.int64), res=np.array(rec["res"]),
+                        dt=np.array(rec["dt"]), t=np.array(rec["t"]), **out)
+    print(f"{name}: {steps} steps written")
+
+
 def program_outputs() -> None:
     """The reference program (src/main.c) end to end on a 10^3 cavity: its
     residual.dat and dcavity.vtk, as written by the reference's own writers."""
@@ -144,9 +183,15 @@ def program_outputs() -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--skip-config1", action="store_true")
+    ap.add_argument("--config2", action="store_true",
+                    help="only the 256^3 benchmark runs (about 30 minutes of one core)")
     args = ap.parse_args()
     if not oracle.ref_available("rb", fast=True):
         sys.exit("reference not built: run oracle/build_ref.sh first")
+    if args.config2:
+        config2_run("mg-ref", 3)
+        config2_run("rb", 2)
+        return
     kat_ops()
     run_case("cavity8_rb", cavity(8, te=1e9, omg=1.7, eps=1e-3, itermax=500), "rb", 12,
              [1, 6, 12])

@@ -12,7 +12,10 @@ import pytest
 from conftest import ROOT
 
 HEADER = ROOT / "include" / "nusif_gb300.h"
-REF_SRC = Path("/root/reference/src")
+import oracle  # noqa: E402  (test infrastructure: where the reference was built from)
+
+_REF_ROOT = oracle.reference_source_root()
+REF_SRC = (_REF_ROOT / "src") if _REF_ROOT else Path("/nonexistent")
 
 
 def declared_functions() -> list[str]:

@@ -16,7 +16,10 @@ import pytest
 
 from conftest import ROOT
 
-REF = Path(os.environ.get("NUSIF_REFERENCE", "/root/reference")) / "src"
+import oracle  # noqa: E402  (test infrastructure: where the reference was built from)
+
+_REF_ROOT = oracle.reference_source_root()
+REF = (_REF_ROOT / "src") if _REF_ROOT else Path("/nonexistent")
 KEPT = ["main.c", "comm.c", "progress.c", "timing.c", "allocate.c", "profiler.c",
         "vtkWriter-seq.c"]
 LIB = ROOT / "cfd-bench_gb300" / "lib"
