@@ -116,7 +116,7 @@ bool enqueue_step(BatchInst *b, bool normalize, int queue, cudaStream_t body)
   if (!launch_special(g, problem_code(d->problem), st->ext.lid, st->ext.inflow, d->u))
     return false;
   if (!launch_fgh(g, d->re, d->gamma, d->gx, d->gy, d->gz, 0.0, d->grid.dx, d->grid.dy,
-          d->grid.dz, d->u, d->v, d->w, d->f, d->g, d->h, sp, b->fg_kb))
+          d->grid.dz, d->u, d->v, d->w, d->f, d->g, d->h, sp, b->fg_kb, st->ext.fg_fp64 != 0))
     return false;
   if (!launch_rhs(g, 0.0, d->grid.dx, d->grid.dy, d->grid.dz, d->f, d->g, d->h, d->rhs, sp))
     return false;
@@ -174,11 +174,11 @@ void autotune(BatchInst *b, cudaStream_t s)
   for (int c : cand) {
     if (c > st->dims.kmax) continue;
     launch_fgh(st->dims, d->re, d->gamma, d->gx, d->gy, d->gz, d->dt, d->grid.dx, d->grid.dy,
-        d->grid.dz, d->u, d->v, d->w, d->f, d->g, d->h, nullptr, c);
+        d->grid.dz, d->u, d->v, d->w, d->f, d->g, d->h, nullptr, c, st->ext.fg_fp64 != 0);
     cudaEventRecord(e0, s);
     for (int r = 0; r < 3; r++)
       launch_fgh(st->dims, d->re, d->gamma, d->gx, d->gy, d->gz, d->dt, d->grid.dx, d->grid.dy,
-          d->grid.dz, d->u, d->v, d->w, d->f, d->g, d->h, nullptr, c);
+          d->grid.dz, d->u, d->v, d->w, d->f, d->g, d->h, nullptr, c, st->ext.fg_fp64 != 0);
     cudaEventRecord(e1, s);
     cudaEventSynchronize(e1);
     float ms = 0.0f;

@@ -12,6 +12,7 @@
 #include <cstring>
 
 #include "nusif_internal.h"
+#include "fgh_df.cuh"
 #include "fp_bits.cuh"
 #include "reduce.cuh"
 
@@ -308,6 +309,164 @@ __global__ void __launch_bounds__(kFX *kFY) k_fgh_flux(FluxArgs A, const double 
   }
 }
 
+// ---- F, G, H in double-float arithmetic (fgh_df.cuh) ----
+// The same flux form, tile (32 x 8 columns marching in k) and flux sharing
+// as k_fgh_flux, with the face fluxes carried in pairs of FP32 numbers on the
+// FP32 pipe (about 2^-47 of the operands, measured within 2e-14 of the FP64
+// oracle on random fields at 64^3..256^3) instead of ~70 FP64 instructions
+// per cell. u, v, w are split into pairs once per block: a ring of three
+// planes in shared memory holds the pairs of the (34 x 10) region around the
+// tile (one halo column and row on each side); plane k+2 is loaded into
+// registers while plane k's fluxes are computed and split into the ring
+// slot plane k-1 used, so one barrier per plane suffices. The result
+// q + dt (g - s) is formed in FP64 (two FP64 adds per component) from the
+// exact velocity q and the pair dt (g - s).
+constexpr int kDX = 32, kDY = 8;
+constexpr int kRW = kDX + 2, kRH = kDY + 2;  // region columns i0-1 .. i0+32, rows j0-1 .. j0+8
+constexpr int kRC = kRW * kRH;               // cells per field and plane
+constexpr int kRItems = 3 * kRC;             // u, v, w
+constexpr int kRPer = (kRItems + kDX * kDY - 1) / (kDX * kDY);
+constexpr size_t kDfRingBytes = 3 * (size_t)kRItems * sizeof(df::f2);
+constexpr size_t kDfXsBytes = 2 * (size_t)kDY * (kDX + 1) * sizeof(df::Face);
+constexpr size_t kDfYsBytes = 2 * (size_t)kDY * kDX * sizeof(df::Face);
+constexpr size_t kDfSmemBytes = kDfRingBytes + kDfXsBytes + kDfYsBytes;
+
+struct FluxArgsDF {
+  Dims g;
+  df::AxisCoef ax, ay, az;
+  df::f2 gx, gy, gz;
+  double dt;
+  const StepScalars *sp;  // when set, dt comes from device memory (captured steps)
+  int kb;                 // k planes per block
+};
+
+template <bool GRAVITY>
+__global__ void __launch_bounds__(kDX *kDY, 2) k_fgh_df(FluxArgsDF A, const double *__restrict__ u,
+    const double *__restrict__ v, const double *__restrict__ w, double *__restrict__ f,
+    double *__restrict__ gg, double *__restrict__ h)
+{
+  using namespace df;
+  extern __shared__ __align__(16) unsigned char df_smem[];
+  f2 *ring = reinterpret_cast<f2 *>(df_smem);  // [slot][field][row][col]
+  Face(*xs)[kDY][kDX + 1] = reinterpret_cast<Face(*)[kDY][kDX + 1]>(df_smem + kDfRingBytes);
+  Face(*ys)[kDY][kDX] =
+      reinterpret_cast<Face(*)[kDY][kDX]>(df_smem + kDfRingBytes + kDfXsBytes);
+
+  const Dims &g = A.g;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kDX + tx;
+  const int i0 = blockIdx.x * kDX + 1, j0 = blockIdx.y * kDY + 1;
+  const bool active = i0 + tx <= g.imax && j0 + ty <= g.jmax;
+  const int i = min(i0 + tx, g.imax), j = min(j0 + ty, g.jmax);
+  const int k0 = blockIdx.z * A.kb + 1;
+  const int k1 = min(k0 + A.kb - 1, g.kmax);
+  const int sj = g.sj, sk = g.sk;
+
+  // the region cells this thread loads for every plane: field pointer + column offset
+  const double *src[kRPer];
+  int soff[kRPer];
+#pragma unroll
+  for (int r = 0; r < kRPer; r++) {
+    const int q = min(tid + r * kDX * kDY, kRItems - 1);  // surplus threads repeat the last item
+    const int fld = q / kRC, cell = q - fld * kRC;
+    const int row = cell / kRW, col = cell - row * kRW;
+    // region row/col -> padded j/i, clamped to the array (clamped cells feed inactive cells only)
+    const int jj = min(j0 - 1 + row, g.jmax + 1), ii = min(i0 - 1 + col, g.imax + 1);
+    src[r] = (fld == 0 ? u : fld == 1 ? v : w) + (int64_t)jj * sj + ii;
+    soff[r] = q;
+  }
+  auto load_plane = [&](int kk, double (&val)[kRPer]) {
+    const int64_t o = (int64_t)min(kk, g.kmax + 1) * sk;
+#pragma unroll
+    for (int r = 0; r < kRPer; r++) val[r] = __ldg(src[r] + o);
+  };
+  auto store_plane = [&](int slot, const double (&val)[kRPer]) {
+#pragma unroll
+    for (int r = 0; r < kRPer; r++) ring[slot * kRItems + soff[r]] = split(val[r]);
+  };
+  // the quad (cell, +x, +y, +z neighbours) of field fld at region (row, col), planes s0 / s1
+  auto quad = [&](int s0, int s1, int fld, int row, int col) {
+    const f2 *p0 = ring + s0 * kRItems + fld * kRC + row * kRW + col;
+    const f2 *p1 = ring + s1 * kRItems + fld * kRC + row * kRW + col;
+    return Quad{ p0[0], p0[1], p0[kRW], p1[0] };
+  };
+
+  const double dt = A.sp ? A.sp->dt : A.dt;
+  const f2 mdt = split(-dt);
+
+  // planes k0-1, k0, k0+1 into slots 0, 1, 2
+  {
+    double val[kRPer];
+    load_plane(k0 - 1, val);
+    store_plane(0, val);
+    load_plane(k0, val);
+    store_plane(1, val);
+    load_plane(k0 + 1, val);
+    store_plane(2, val);
+  }
+  __syncthreads();
+  ZFaceG zgm;
+  Face zm;
+  {
+    const Quad U = quad(0, 1, 0, ty + 1, tx + 1), V = quad(0, 1, 1, ty + 1, tx + 1),
+               W = quad(0, 1, 2, ty + 1, tx + 1);
+    zm = z_face(A.az, U, V, W, zgm);
+  }
+  __syncthreads();  // slot 0 (plane k0-1) is refilled in the first iteration
+
+  int s0 = 1, s1 = 2, s2 = 0;  // slots of planes k, k+1, k+2
+  int buf = 0;
+  for (int k = k0; k <= k1; k++) {
+    double val[kRPer];
+    load_plane(k + 2, val);
+    const Quad U = quad(s0, s1, 0, ty + 1, tx + 1), V = quad(s0, s1, 1, ty + 1, tx + 1),
+               W = quad(s0, s1, 2, ty + 1, tx + 1);
+    const Face xp = x_face(A.ax, U, V, W);
+    const Face yp = y_face(A.ay, U, V, W);
+    ZFaceG zgp;
+    const Face zp = z_face(A.az, U, V, W, zgp);
+    xs[buf][ty][tx + 1] = xp;
+    ys[buf][ty][tx] = yp;
+    if (ty == 1 && tx < kDY) {  // the left halo x-face of row tx (column i0-1)
+      const Quad Uh = quad(s0, s1, 0, tx + 1, 0), Vh = quad(s0, s1, 1, tx + 1, 0),
+                 Wh = quad(s0, s1, 2, tx + 1, 0);
+      xs[buf][tx][0] = x_face(A.ax, Uh, Vh, Wh);
+    }
+    Face ymh;
+    if (ty == 0) {  // the y-face below the tile's first row (row j0-1)
+      const Quad Uh = quad(s0, s1, 0, 0, tx + 1), Vh = quad(s0, s1, 1, 0, tx + 1),
+                 Wh = quad(s0, s1, 2, 0, tx + 1);
+      ymh = y_face(A.ay, Uh, Vh, Wh);
+    }
+    store_plane(s2, val);
+    __syncthreads();
+    const Face xm = xs[buf][ty][tx];
+    const Face ym = ty > 0 ? ys[buf][ty - 1][tx] : ymh;
+    if (active) {
+      const int64_t c = (int64_t)k * sk + (int64_t)j * sj + i;
+      const double uc = __ldg(u + c), vc = __ldg(v + c), wc = __ldg(w + c);
+      // F(imax), G(jmax), H(kmax) are wall faces carrying the velocity (discretization.c:609-651)
+      const f2 sf = add(add(sub(xp.f, xm.f), sub(yp.f, ym.f)), sub(zp.f, zm.f));
+      f[c] = (i == g.imax) ? uc : update(uc, sf, A.gx, mdt, GRAVITY);
+      const f2 zc = g_zconv(A.az, zgp.gc, zgm.gc, V.c, V.z);
+      const f2 sg = add(add(add(sub(xp.g, xm.g), sub(yp.g, ym.g)), sub(zgp.gv, zgm.gv)), zc);
+      gg[c] = (j == g.jmax) ? vc : update(vc, sg, A.gy, mdt, GRAVITY);
+      const f2 sh = add(add(sub(xp.h, xm.h), sub(yp.h, ym.h)), sub(zp.h, zm.h));
+      h[c] = (k == g.kmax) ? wc : update(wc, sh, A.gz, mdt, GRAVITY);
+      // low wall faces F(0), G(0), H(0) carry the velocity (discretization.c:601-643)
+      if (i == 1) f[c - 1] = __ldg(u + c - 1);
+      if (j == 1) gg[c - sj] = __ldg(v + c - sj);
+      if (k == 1) h[c - sk] = __ldg(w + c - sk);
+    }
+    zm = zp;
+    zgm = zgp;
+    buf ^= 1;
+    const int t = s0;
+    s0 = s1;
+    s1 = s2;
+    s2 = t;
+  }
+}
+
 // ---- RHS (discretization.c:334-362) ----
 // ((F - F_w)/dx + (G - G_s)/dy + (H - H_b)/dz)/dt with 1/(h dt) folded into
 // one factor per axis: six FP64 instructions per cell instead of seven.
@@ -450,7 +609,8 @@ bool launch_special(const Dims &g, int problem, double lid, double inflow, doubl
 
 bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, double gz,
     double dt, double dx, double dy, double dz, const double *u, const double *v,
-    const double *w, double *f, double *gg, double *h, const StepScalars *sp, int kb_fixed)
+    const double *w, double *f, double *gg, double *h, const StepScalars *sp, int kb_fixed,
+    bool fp64)
 {
   FluxArgs A;
   A.g = g;
@@ -475,11 +635,44 @@ bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, do
   if (kb_fixed > 0) kb = kb_fixed;
   A.kb = kb;
   dim3 grid(gx_blocks, gy_blocks, (g.kmax + kb - 1) / kb);
-  if (gx == 0.0 && gy == 0.0 && gz == 0.0)
-    k_fgh_flux<false><<<grid, dim3(kFX, kFY), 0, stream()>>>(A, u, v, w, f, gg, h);
+  const bool gravity = !(gx == 0.0 && gy == 0.0 && gz == 0.0);
+  if (fp64) {
+    if (!gravity)
+      k_fgh_flux<false><<<grid, dim3(kFX, kFY), 0, stream()>>>(A, u, v, w, f, gg, h);
+    else
+      k_fgh_flux<true><<<grid, dim3(kFX, kFY), 0, stream()>>>(A, u, v, w, f, gg, h);
+    return launched("k_fgh_flux");
+  }
+  static_assert(kDX == kFX && kDY == kFY, "both computeFG kernels share one tiling");
+  FluxArgsDF D;
+  D.g = g;
+  df::AxisCoef *dc[3] = { &D.ax, &D.ay, &D.az };
+  for (int a = 0; a < 3; a++) *dc[a] = df::axis_coef(fc[a]->P, fc[a]->M, fc[a]->nu);
+  D.gx = df::from_double_rn(gx);
+  D.gy = df::from_double_rn(gy);
+  D.gz = df::from_double_rn(gz);
+  D.dt = dt;
+  D.sp = sp;
+  D.kb = kb;
+  // the kernel's shared memory (49.4 KB) is above the 48 KB default: opt in once per device
+  static bool attr_set[64] = {};
+  int dev = 0;
+  if (!cuda_ok(cudaGetDevice(&dev), "cudaGetDevice")) return false;
+  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    if (!cuda_ok(cudaFuncSetAttribute(k_fgh_df<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                     (int)kDfSmemBytes),
+            "k_fgh_df<false> shared memory") ||
+        !cuda_ok(cudaFuncSetAttribute(k_fgh_df<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                     (int)kDfSmemBytes),
+            "k_fgh_df<true> shared memory"))
+      return false;
+    attr_set[dev] = true;
+  }
+  if (!gravity)
+    k_fgh_df<false><<<grid, dim3(kDX, kDY), kDfSmemBytes, stream()>>>(D, u, v, w, f, gg, h);
   else
-    k_fgh_flux<true><<<grid, dim3(kFX, kFY), 0, stream()>>>(A, u, v, w, f, gg, h);
-  return launched("k_fgh_flux");
+    k_fgh_df<true><<<grid, dim3(kDX, kDY), kDfSmemBytes, stream()>>>(D, u, v, w, f, gg, h);
+  return launched("k_fgh_df");
 }
 
 bool launch_rhs(const Dims &g, double dt, double dx, double dy, double dz, const double *f,
@@ -711,7 +904,7 @@ void computeFG(Discretization *s)
   DiscState *st = need_state(s, "computeFG");
   if (!st) return;
   launch_fgh(st->dims, s->re, s->gamma, s->gx, s->gy, s->gz, s->dt, s->grid.dx, s->grid.dy,
-      s->grid.dz, s->u, s->v, s->w, s->f, s->g, s->h);
+      s->grid.dz, s->u, s->v, s->w, s->f, s->g, s->h, nullptr, 0, st->ext.fg_fp64 != 0);
 }
 
 void computeRHS(Discretization *s)

@@ -42,6 +42,7 @@ struct Extras {
   int host_fields = 0;       // 1: fields in managed memory (host-readable pointers)
   int mg_guess_probe = 1;    // key mg_probe: learned guess every P-th step after 2 rejections
   int mg_maxcycles = 100;
+  int fg_fp64 = 0;           // key fg_arith: computeFG in FP64 instructions (fp64) or FP32 pairs (df32)
 };
 Extras *extras_for(const Parameter *p, bool create);
 
@@ -104,7 +105,7 @@ bool launch_bc(const Dims &g, const int bc[6], int problem, double lid, double i
 bool launch_fgh(const Dims &g, double re, double gamma, double gx, double gy, double gz,
     double dt, double dx, double dy, double dz, const double *u, const double *v,
     const double *w, double *f, double *gg, double *h, const StepScalars *sp = nullptr,
-    int kb_fixed = 0);
+    int kb_fixed = 0, bool fp64 = false);
 bool launch_rhs(const Dims &g, double dt, double dx, double dy, double dz, const double *f,
     const double *gg, const double *h, double *rhs, const StepScalars *sp = nullptr);
 bool launch_interior_sum(const Dims &g, const double *p, ReduceScratch &red, double *d_out);

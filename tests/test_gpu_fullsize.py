@@ -24,10 +24,11 @@ def _vals(solver="rb", **over):
     return v
 
 
-def test_operators_at_256_match_oracle(nusif_lib, oracle_mod):
+@pytest.mark.parametrize("arith", ["df32", "fp64"])
+def test_operators_at_256_match_oracle(nusif_lib, oracle_mod, arith):
     from nusif import Simulation
     o = oracle_mod
-    v = _vals()
+    v = _vals(fg_arith=arith)
     rng = np.random.default_rng(2561)
     with Simulation(v) as sim:
         shape = sim.padded_shape

@@ -6,7 +6,9 @@ Tolerances: the GPU evaluates the reference's FP64 expressions with fused
 multiply-adds and reordered sums, so results may differ in the last bits.
 Boundary copies are exact; arithmetic operators must agree to 1e-13 of the
 field's magnitude; the red-black solve must give the same iteration count and
-fields to 1e-11.
+fields to 1e-11. computeFG runs in both of its arithmetic forms (fg_arith
+df32: face fluxes in pairs of FP32 numbers, the default; fp64: FP64
+instructions), both held to the same 1e-13.
 """
 from __future__ import annotations
 
@@ -81,12 +83,13 @@ def _case(dims, bc, name="dcavity", **over):
     return cavity(dims, **base)
 
 
+@pytest.mark.parametrize("arith", ["df32", "fp64"])
 @pytest.mark.parametrize("dims", SIZES)
 @pytest.mark.parametrize("bci", range(len(BCS)))
-def test_operators_match_oracle_random(nusif_lib, oracle_mod, dims, bci):
+def test_operators_match_oracle_random(nusif_lib, oracle_mod, dims, bci, arith):
     o = oracle_mod
     name = "canal" if bci == 2 else "dcavity"
-    v = _case(dims, BCS[bci], name=name, lid=1.25, inflow=0.75)
+    v = _case(dims, BCS[bci], name=name, lid=1.25, inflow=0.75, fg_arith=arith)
     rng = np.random.default_rng(abs(hash((dims, bci))) % (2 ** 32))
     with _sim(v) as sim:
         shape = sim.padded_shape
