@@ -20,7 +20,7 @@ OBJ = PKG / "_build"
 LIB = PKG / "lib" / "libnusif_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["runtime.cpp", "parameter.cpp", "discretization.cu", "solver.cu", "multigrid.cu",
-           "solver_static.cu", "output.cu", "batch.cu", "unet.cu", "guess.cu"]
+           "solver_static.cu", "output.cu", "batch.cu", "unet.cu", "unet_tc.cu", "guess.cu"]
 
 
 def nvcc() -> str:

@@ -14,6 +14,10 @@
 // times its ReLU mask is rounded to BF16 before the tensor-core kernels use it.
 //
 // Kernels:
+//  - k_conv_tc (unet_tc.cu): the forward and input-gradient convolutions on
+//    the 5th-generation tensor cores (tcgen05.mma, TMEM accumulators, TMA
+//    staging) whenever the volume's rows tile into 128-cell blocks; the
+//    decoder's upsampled concat source is then materialised by k_upsample.
 //  - k_conv_mma: implicit-GEMM conv on the tensor cores (mma.sync m16n8k16
 //    BF16 -> FP32): M = cells (16 per warp), N = output channels, K = 27 taps x
 //    input channels in chunks of 16. Its loader reads up to two sources, the
@@ -34,6 +38,7 @@
 
 #include "nusif_internal.h"
 #include "unet_internal.h"
+#include "unet_tc.h"
 
 namespace nusif {
 namespace {
@@ -463,11 +468,49 @@ __global__ void __launch_bounds__(256) k_wgrad_plain(const void *g_, const bf16 
 
 // ------------------------------------------------------------------ elementwise
 
-__global__ void k_f32_to_bf16(const float *__restrict__ a, int64_t n, bf16 *__restrict__ b)
+// the 2-channel FP32 input as BF16, once as [cells][2] (the first layer's
+// weight gradient) and once zero-padded to [cells][16] (the tensor-core
+// first layer: K must be a multiple of 16)
+__global__ void k_input_bf16(const float *__restrict__ x, int64_t n, bf16 *__restrict__ x2,
+    bf16 *__restrict__ x16)
 {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const float2 a = reinterpret_cast<const float2 *>(x)[c];
+    const uint32_t v = pack_bf16(a.x, a.y);
+    reinterpret_cast<uint32_t *>(x2)[c] = v;
+    uint4 *o = reinterpret_cast<uint4 *>(x16 + c * 16);
+    o[0] = make_uint4(v, 0u, 0u, 0u);
+    o[1] = make_uint4(0u, 0u, 0u, 0u);
+  }
+}
+
+// W[27][co][ci] (FP32) -> BF16 [27][16][16], zero outside co x ci (the first
+// and last layers on the tensor cores)
+__global__ void k_pad_weights16(const float *__restrict__ w, int co, int ci, bf16 *__restrict__ wp)
+{
+  const int n = 27 * 16 * 16;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int tap = i / 256, o = (i / 16) % 16, k = i % 16;
+    wp[i] = __float2bfloat16_rn(o < co && k < ci ? w[(tap * co + o) * ci + k] : 0.0f);
+  }
+}
+
+// nearest upsampling of a [half cells][C] BF16 volume to full resolution, 8
+// channels (16 bytes) per thread
+__global__ void k_upsample(const bf16 *__restrict__ c, Vol fv, int C, bf16 *__restrict__ f)
+{
+  const int g8 = C / 8;
+  const int64_t n = fv.cells() * g8;
+  const int hZ = fv.Z / 2, hY = fv.Y / 2, hX = fv.X / 2;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    b[i] = __float2bfloat16_rn(a[i]);
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int grp = (int)(i % g8);
+    int b, z, y, x;
+    decompose(fv, i / g8, b, z, y, x);
+    const int64_t cc = (((int64_t)b * hZ + (z >> 1)) * hY + (y >> 1)) * hX + (x >> 1);
+    reinterpret_cast<uint4 *>(f)[i] = reinterpret_cast<const uint4 *>(c)[cc * g8 + grp];
+  }
 }
 
 // G = bf16(dY * (Y > 0))
@@ -630,6 +673,11 @@ struct UNetState {
   float *out = nullptr, *dout = nullptr, *F1 = nullptr, *F2 = nullptr, *Fe0b = nullptr,
         *Fe1b = nullptr, *partial = nullptr;
   int64_t partial_cap = 0;
+  bf16 *up1 = nullptr, *up0 = nullptr;  // materialised up(e2a) [n1][64], up(d1b) [n0][32]
+  bf16 *x16 = nullptr;                  // input zero-padded to 16 channels
+  bf16 *w_first16 = nullptr, *w_last16 = nullptr;  // e0a and out weights padded to [27][16][16]
+  int *err = nullptr;                   // device: a tensor-core kernel's wait timed out
+  int use_tc = 1;                       // tcgen05 kernels where the volume allows
   double *loss_partial = nullptr;
   float *loss = nullptr;  // device scalar
   std::vector<void *> ws;
@@ -672,7 +720,9 @@ bool ensure_workspace(UNetState *u, const Vol &v)
             dalloc(u, &u->d1b, 32 * n1) && dalloc(u, &u->d0a, 16 * n0) && dalloc(u, &u->d0b, 16 * n0) &&
             dalloc(u, &u->G, 16 * n0) && dalloc(u, &u->out, n0) && dalloc(u, &u->dout, n0) &&
             dalloc(u, &u->F1, 48 * n0) && dalloc(u, &u->F2, 16 * n0) && dalloc(u, &u->Fe0b, 16 * n0) &&
-            dalloc(u, &u->Fe1b, 32 * n1) && dalloc(u, &u->loss_partial, 1024);
+            dalloc(u, &u->Fe1b, 32 * n1) && dalloc(u, &u->loss_partial, 1024) &&
+            dalloc(u, &u->up1, 64 * n1) && dalloc(u, &u->up0, 32 * n0) &&
+            dalloc(u, &u->x16, 16 * n0);
   if (!ok) return false;
   u->cap0 = n0;
   return true;
@@ -716,10 +766,26 @@ bool conv_mma(const ConvSrc &s0, const ConvSrc &s1, const Vol &v, const bf16 *w,
   return launched("k_conv_mma");
 }
 
+bool tc_ok(const UNetState *u, const Vol &v, int n, int c0, int c1)
+{
+  return u->use_tc && tc_conv_supported(v.X, v.Y, v.Z, v.B, n, c0, c1);
+}
+
 // forward conv of a tensor-core layer (BF16 out, bias, ReLU)
 bool fwd(UNetState *u, int l, const ConvSrc &s0, const ConvSrc &s1, const Vol &v, bf16 *out)
 {
   const float *bias = u->master + u->b_off[l];
+  if (tc_ok(u, v, kDesc[l].cout, s0.c, s1.c)) {
+    const bf16 *a0 = s0.p;
+    if (s0.up) {  // the decoder's upsampled source, materialised at full resolution
+      bf16 *dst = s0.c == 64 ? u->up1 : u->up0;
+      k_upsample<<<blocks_for(v.cells() * (s0.c / 8)), 256, 0, stream()>>>(s0.p, v, s0.c, dst);
+      if (!launched("k_upsample")) return false;
+      a0 = dst;
+    }
+    return tc_conv(a0, s0.c, s1.p, s1.c, v.B, v.Z, v.Y, v.X, u->wb[l], kDesc[l].cout, bias, 1, true,
+        out, u->err);
+  }
   switch (kDesc[l].cout) {
   case 16: return conv_mma<16, true>(s0, s1, v, u->wb[l], bias, 1, out);
   case 32: return conv_mma<32, true>(s0, s1, v, u->wb[l], bias, 1, out);
@@ -734,6 +800,9 @@ bool dgrad(UNetState *u, int l, const Vol &v, float *dx)
 {
   const ConvSrc g = { u->G, kDesc[l].cout, 0 };
   const ConvSrc none = { nullptr, 0, 0 };
+  if (tc_ok(u, v, kDesc[l].cin, kDesc[l].cout, 0))
+    return tc_conv(u->G, kDesc[l].cout, nullptr, 0, v.B, v.Z, v.Y, v.X, u->wt[l], kDesc[l].cin,
+        nullptr, 0, false, dx, u->err);
   switch (kDesc[l].cin) {
   case 16: return conv_mma<16, false>(g, none, v, u->wt[l], nullptr, 0, dx);
   case 32: return conv_mma<32, false>(g, none, v, u->wt[l], nullptr, 0, dx);
@@ -821,7 +890,10 @@ bool refresh_bf16(UNetState *u)
         kDesc[l].cin, u->wb[l], u->wt[l]);
     if (!launched("k_layer_bf16")) return false;
   }
-  return true;
+  k_pad_weights16<<<27, 256, 0, stream()>>>(u->master + u->w_off[L_E0A], 16, 2, u->w_first16);
+  if (!launched("k_pad_weights16")) return false;
+  k_pad_weights16<<<27, 256, 0, stream()>>>(u->master + u->w_off[L_OUT], 1, 16, u->w_last16);
+  return launched("k_pad_weights16");
 }
 
 }  // namespace
@@ -832,9 +904,15 @@ bool unet_forward(UNetState *u)
   const Vol v0 = u->vol, v1 = half(v0), v2 = half(v1);
   const int64_t n0 = v0.cells();
   const ConvSrc none = { nullptr, 0, 0 };
-  k_conv_first<<<(unsigned)((n0 + 255) / 256), 256, 0, stream()>>>(u->x, v0, u->wb[L_E0A],
-      u->master + u->b_off[L_E0A], u->e0a);
-  if (!launched("k_conv_first")) return false;
+  if (tc_ok(u, v0, 16, 16, 0)) {
+    if (!tc_conv(u->x16, 16, nullptr, 0, v0.B, v0.Z, v0.Y, v0.X, u->w_first16, 16,
+            u->master + u->b_off[L_E0A], 1, true, u->e0a, u->err))
+      return false;
+  } else {
+    k_conv_first<<<(unsigned)((n0 + 255) / 256), 256, 0, stream()>>>(u->x, v0, u->wb[L_E0A],
+        u->master + u->b_off[L_E0A], u->e0a);
+    if (!launched("k_conv_first")) return false;
+  }
   if (!fwd(u, L_E0B, { u->e0a, 16, 0 }, none, v0, u->e0b)) return false;
   k_pool<<<blocks_for(v1.cells() * 16), 256, 0, stream()>>>(u->e0b, v0, 16, u->p0);
   if (!launched("k_pool")) return false;
@@ -847,6 +925,9 @@ bool unet_forward(UNetState *u)
   if (!fwd(u, L_D1B, { u->d1a, 32, 0 }, none, v1, u->d1b)) return false;
   if (!fwd(u, L_D0A, { u->d1b, 32, 1 }, { u->e0b, 16, 0 }, v0, u->d0a)) return false;
   if (!fwd(u, L_D0B, { u->d0a, 16, 0 }, none, v0, u->d0b)) return false;
+  if (tc_ok(u, v0, 16, 16, 0))
+    return tc_conv(u->d0b, 16, nullptr, 0, v0.B, v0.Z, v0.Y, v0.X, u->w_last16, 16,
+        u->master + u->b_off[L_OUT], 0, false, u->out, u->err, 1);
   k_conv_last<<<(unsigned)((n0 + 255) / 256), 256, 0, stream()>>>(u->d0b, v0, u->wb[L_OUT],
       u->master + u->b_off[L_OUT], u->out);
   return launched("k_conv_last");
@@ -952,9 +1033,8 @@ bool unet_backward(UNetState *u, const float *target)
 bool unet_set_input(UNetState *u, const float *x, const Vol &v)
 {
   if (!ensure_workspace(u, v)) return false;
-  const int64_t n = 2 * v.cells();
-  k_f32_to_bf16<<<blocks_for(n), 256, 0, stream()>>>(x, n, u->x);
-  return launched("k_f32_to_bf16");
+  k_input_bf16<<<blocks_for(v.cells()), 256, 0, stream()>>>(x, v.cells(), u->x, u->x16);
+  return launched("k_input_bf16");
 }
 
 }  // namespace nusif
@@ -989,6 +1069,22 @@ NusifUNet *checked(NusifUNet *n)
 {
   if (!n) fail(NUSIF_ERR_ARG, "unet: null network");
   return n;
+}
+
+// the tensor-core kernels' error flag (a bounded wait that ran out); synchronises
+bool tc_clean(UNetState *u)
+{
+  int e = 0;
+  if (!cuda_ok(cudaMemcpyAsync(&e, u->err, sizeof(int), cudaMemcpyDeviceToHost, stream()),
+          "unet error flag") ||
+      !cuda_ok(cudaStreamSynchronize(stream()), "unet error flag"))
+    return false;
+  if (e) {
+    cudaMemsetAsync(u->err, 0, sizeof(int), stream());
+    fail(NUSIF_ERR_CUDA, "unet: a tensor-core convolution timed out waiting for its operands");
+    return false;
+  }
+  return true;
 }
 
 }  // namespace
@@ -1031,7 +1127,11 @@ NusifUNet *nusifUNetCreate(unsigned long long seed)
             cuda_ok(cudaMalloc(&u->grad, o * sizeof(float)), "cudaMalloc(unet)") &&
             cuda_ok(cudaMalloc(&u->m, o * sizeof(float)), "cudaMalloc(unet)") &&
             cuda_ok(cudaMalloc(&u->v, o * sizeof(float)), "cudaMalloc(unet)") &&
-            cuda_ok(cudaMalloc(&u->loss, sizeof(float)), "cudaMalloc(unet)");
+            cuda_ok(cudaMalloc(&u->loss, sizeof(float)), "cudaMalloc(unet)") &&
+            cuda_ok(cudaMalloc(&u->err, sizeof(int)), "cudaMalloc(unet)") &&
+            cuda_ok(cudaMemset(u->err, 0, sizeof(int)), "unet init");
+  ok = ok && cuda_ok(cudaMalloc(&u->w_first16, 27 * 256 * sizeof(bf16)), "cudaMalloc(unet)") &&
+       cuda_ok(cudaMalloc(&u->w_last16, 27 * 256 * sizeof(bf16)), "cudaMalloc(unet)");
   for (int l = 0; ok && l < kLayers; l++) {
     const size_t nw = 27 * kDesc[l].cout * kDesc[l].cin;
     ok = cuda_ok(cudaMalloc(&u->wb[l], nw * sizeof(bf16)), "cudaMalloc(unet)") &&
@@ -1059,6 +1159,9 @@ void nusifUNetFree(NusifUNet *n)
   if (u->partial) cudaFree(u->partial);
   for (float *p : { u->master, u->grad, u->m, u->v, u->loss })
     if (p) cudaFree(p);
+  if (u->err) cudaFree(u->err);
+  if (u->w_first16) cudaFree(u->w_first16);
+  if (u->w_last16) cudaFree(u->w_last16);
   for (int l = 0; l < kLayers; l++) {
     if (u->wb[l]) cudaFree(u->wb[l]);
     if (u->wt[l]) cudaFree(u->wt[l]);
@@ -1124,6 +1227,16 @@ int nusifUNetForward(NusifUNet *n, const float *x, int B, int Z, int Y, int X, f
                    stream()),
           "unet output"))
     return NUSIF_ERR_CUDA;
+  return tc_clean(u) ? NUSIF_OK : NUSIF_ERR_CUDA;
+}
+
+int nusifUNetSetTensorCore(NusifUNet *n, int mode)
+{
+  if (!checked(n) || (mode != 0 && mode != 1)) {
+    fail(NUSIF_ERR_ARG, "nusifUNetSetTensorCore: mode 0 (mma.sync) or 1 (tcgen05)");
+    return NUSIF_ERR_ARG;
+  }
+  n->s.use_tc = mode;
   return NUSIF_OK;
 }
 
@@ -1148,6 +1261,7 @@ int nusifUNetTrainStep(NusifUNet *n, const float *x, const float *target, int B,
             "unet loss") ||
         !cuda_ok(cudaStreamSynchronize(stream()), "unet loss"))
       return NUSIF_ERR_CUDA;
+    if (!tc_clean(u)) return NUSIF_ERR_CUDA;
   }
   return NUSIF_OK;
 }

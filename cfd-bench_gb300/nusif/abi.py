@@ -121,6 +121,7 @@ SIGNATURES = [
     ("nusifUNetGetGrads", C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong]),
     ("nusifUNetForward", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                    C.c_void_p]),
+    ("nusifUNetSetTensorCore", C.c_int, [C.c_void_p, C.c_int]),
     ("nusifUNetTrainStep", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                      C.c_int, C.c_int, C.c_float, C.c_int,
                                      C.POINTER(C.c_float)]),

@@ -50,6 +50,11 @@ class UNet:
         abi.check(self.lib)
         return out
 
+    def set_tensor_core(self, tcgen05: bool) -> None:
+        """Convolutions on the tcgen05 kernels (where the volume allows) or on mma.sync."""
+        self.lib.nusifUNetSetTensorCore(self.handle, 1 if tcgen05 else 0)
+        abi.check(self.lib)
+
     def forward(self, x):
         """x: [B][Z][Y][X][2] -> [B][Z][Y][X]."""
         import torch

@@ -264,6 +264,11 @@ NUSIF_API int nusifUNetGetGrads(const NusifUNet *net, float *host, long long cou
 /* out (device, [B][Z][Y][X]) = net(x) */
 NUSIF_API int nusifUNetForward(NusifUNet *net, const float *x, int B, int Z, int Y, int X,
     float *out);
+/* Convolution kernels: 1 (default) the tcgen05 tensor-core kernels wherever the
+ * volume's x-rows tile into 128-cell blocks (x a divisor of 128 or a multiple
+ * of it), else and with 0 the mma.sync kernels. Results agree to BF16
+ * rounding of the activations. */
+NUSIF_API int nusifUNetSetTensorCore(NusifUNet *net, int mode);
 /* forward, mean-squared-error loss against `target` (device), backward; with
  * update != 0 one Adam step (lr, beta 0.9 / 0.999, eps 1e-8). loss_host may be
  * NULL (no synchronisation). */

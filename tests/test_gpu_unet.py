@@ -1,5 +1,7 @@
 """The U-Net's GPU kernels (tensor-core convolutions, backward pass, Adam)
-against the numpy oracle with the same BF16 rounding points.
+against the numpy oracle with the same BF16 rounding points, and the
+tcgen05 convolutions against the mma.sync ones on volumes where every level
+runs on tcgen05 (x-rows tiling into 128-cell blocks).
 
 Tolerances: outputs and gradients are compared as relative L2 norms per
 layer. The GPU sums in FP32 in another order than the oracle, so a stored
@@ -118,3 +120,38 @@ def test_training_reduces_loss(nusif_lib):
             net.train_step(xd, td, lr=1e-3, update=True, want_loss=False)
         last = net.train_step(xd, td, lr=1e-3, update=True)
     assert last < first / 5, (first, last)
+
+
+@pytest.mark.parametrize("shape", [(1, 16, 16, 32), (2, 16, 32, 16)])
+def test_tcgen05_forward_matches_oracle(nusif_lib, shape):
+    """Levels 0 and 1 of these volumes run on tcgen05 (level 2 where it tiles)."""
+    from nusif import UNet
+    flat, x, _ = _case(6, shape)
+    ref = U.UNet(flat).forward(x)
+    with UNet() as net:
+        net.set_params(flat)
+        out = net.forward(_dev(x)).cpu().numpy()
+    assert _rel(out, ref) < 2e-2
+
+
+@pytest.mark.parametrize("shape", [(1, 64, 64, 64), (2, 32, 32, 64)])
+def test_tcgen05_matches_mma_sync(nusif_lib, shape):
+    """Every level on tcgen05 against every level on mma.sync: the forward
+    output and all gradients (both paths share the BF16 rounding points and
+    differ only in FP32 summation order)."""
+    from nusif import UNet
+    flat, x, t = _case(7, shape)
+    res = {}
+    for tc in (True, False):
+        with UNet() as net:
+            net.set_params(flat)
+            net.set_tensor_core(tc)
+            out = net.forward(_dev(x)).cpu().numpy()
+            loss = net.train_step(_dev(x), _dev(t), update=False)
+            res[tc] = (out, loss, net.grads())
+    assert _rel(res[True][0], res[False][0]) < 1e-2
+    assert res[True][1] == pytest.approx(res[False][1], rel=1e-2)
+    offs = np.cumsum([0] + [27 * ci * co + co for _, ci, co, _ in U.LAYERS])
+    for li, (name, ci, co, _) in enumerate(U.LAYERS):
+        a, b = res[True][2][offs[li]:offs[li + 1]], res[False][2][offs[li]:offs[li + 1]]
+        assert _rel(a, b) < 3e-2, name
