@@ -41,6 +41,10 @@ UNIT = "ms/timestep"
 PEAKS = ROOT / "MEASURED_PEAKS.json"
 TRAFFIC = ROOT / "profiles" / "traffic.json"
 FALLBACK_HBM_GBS = 6800.0
+# the warm-start network the headline arm uses, trained by
+#   python bench.py --workload learned --save-net <this file>
+# (64 cavities at 128^3, Re ~ U[100, 5000], lid ~ U[0.5, 2], seeded)
+NET_PATH = ROOT / "cfd-bench_gb300" / "nusif" / "weights" / "unet_cavity128.npz"
 
 
 def parse_args():
@@ -66,6 +70,7 @@ def parse_args():
     ap.add_argument("--learn-n", type=int, default=128, help="training cavity edge (learned)")
     ap.add_argument("--learn-steps", type=int, default=300, help="steps per training run")
     ap.add_argument("--learn-iters", type=int, default=2000, help="Adam iterations (learned)")
+    ap.add_argument("--learn-batch", type=int, default=8, help="pairs per Adam step (learned)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--phases", action="store_true",
                     help="add a per-call split of the step and per-level FP32 V-cycle times")
@@ -86,6 +91,13 @@ def parse_args():
                          "multigrid (default: warmup + steps)")
     ap.add_argument("--ref-sweeps", type=int, default=100,
                     help="red-black sweeps timed per step by the reference arm")
+    ap.add_argument("--net", default=str(NET_PATH),
+                    help="trained warm-start network (learn.save_params file) of the headline "
+                         "arm: learned guess + mixed-precision multigrid")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="headline without the learned warm start (mixed-precision MG alone)")
+    ap.add_argument("--save-net", default=None,
+                    help="--workload learned: write the trained network here")
     return ap.parse_args()
 
 
@@ -197,6 +209,23 @@ def bench_case(n: int, solver: str, itermax: int | None = None,
     return vals
 
 
+def load_headline_net(args, solver: str):
+    """The trained warm-start network of the headline arm (mixed-precision MG
+    only), or None (--no-learned, another solver, or no weights file)."""
+    if args.no_learned or solver != "mg-mixed" or not Path(args.net).exists():
+        return None
+    from nusif.learn import load_net
+    return load_net(args.net)
+
+
+def learned_meta(path) -> dict:
+    try:
+        from nusif.learn import saved_meta
+        return saved_meta(path)
+    except Exception:
+        return {}
+
+
 def pick_solver(requested: str) -> str:
     return "mg-mixed" if requested == "auto" else requested
 
@@ -261,11 +290,22 @@ def run_gpu(args, rank, world, local):
 
     solver = pick_solver(args.solver)
     vals = bench_case(args.n, solver, args.itermax, args.guess, graph=not args.no_graph)
+    net = load_headline_net(args, solver)
+    if net is not None:
+        vals.update(mg_probe=LEARNED_PROBE)
     sim = nusif.Simulation(vals)
+    if net is not None:
+        sim.set_guess_net(net)
     i, j, k = sim.dims
     ncell = i * j * k
     padded = (i + 2) * (j + 2) * (k + 2)
     head = timed_steps(sim, args, stream, local, world)
+    learned = None
+    if net is not None:
+        ev, taken = sim.guess_counts()
+        learned = {"network": str(Path(args.net).name), "probe_every_after_two_rejections":
+                   LEARNED_PROBE, "evaluations_incl_warmup": ev, "guesses_taken_incl_warmup": taken,
+                   "trained": learned_meta(args.net)}
 
     # ---- dominant kernels, timed live with CUDA events on the library stream ----
     roofs = [] if args.no_roofline else kernel_rooflines(sim, solver, stream, ncell)
@@ -277,6 +317,16 @@ def run_gpu(args, rank, world, local):
     if not args.no_e2e:
         e2e = run_e2e(sim, args, stream, padded)
     sim.close()
+
+    # ---- the same solver without the network ----
+    if net is not None:
+        sim0 = nusif.Simulation(bench_case(args.n, solver, args.itermax, args.guess,
+                                           graph=not args.no_graph))
+        alone = timed_steps(sim0, args, stream, local, world)
+        sim0.close()
+        learned.update({"ms_per_step_without_network": alone["ms_per_step"],
+                        "v_cycles_per_step_without_network": alone["iters"],
+                        "speedup_from_network": alone["ms_per_step"] / head["ms_per_step"]})
 
     # ---- the comparison the metric names: plain FP64 multigrid, same case ----
     # (previous-p guess: plain FP64 multigrid; and with this run's guess)
@@ -302,7 +352,7 @@ def run_gpu(args, rank, world, local):
     if solver != "mg" and solver.startswith("mg") and not args.no_compare and rank == 0:
         n_err = args.error_steps if args.error_steps is not None else args.warmup + args.steps
         if n_err > 0:
-            errors = field_error_study(args, stream, solver, n_err)
+            errors = field_error_study(args, stream, solver, n_err, net)
 
     rb = None
     if solver != "rb" and args.rb_steps > 0 and not args.no_compare:
@@ -312,6 +362,8 @@ def run_gpu(args, rank, world, local):
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(vals, solver, head["iters"], args.ref_sweeps)
 
+    if net is not None:
+        net.close()
     if rank != 0:
         return None
     tol = ("relative residual 1e-6 (mean-free rhs)" if solver.startswith("mg")
@@ -330,9 +382,10 @@ def run_gpu(args, rank, world, local):
         "dtype": "f64" if solver in ("rb", "mg", "mg-ref") else "f64+f32",
         "data": "synthetic: lid-driven cavity from rest, no dataset",
         "config": {"workload": f"lid-driven cavity {i}x{j}x{k}, Re 1000, tau 0.5, "
-                               f"pressure solve {solver}",
+                               f"pressure solve {solver}"
+                               + (" with the learned warm start" if net is not None else ""),
                    "cells": ncell, "solver": solver, "tolerance": tol,
-                   "learned_warm_start": False,
+                   "learned_warm_start": net is not None,
                    "initial_guess": (args.guess if solver in ("mg", "mg-mixed") else "previous"),
                    "v_cycle": ("V(%d,%d), up to %d FP32 V-cycles per FP64 residual, "
                                "red-black smoother omega %.2f, FP32 correction to 0.9 rtol"
@@ -347,6 +400,7 @@ def run_gpu(args, rank, world, local):
         "solver_iterations_per_step": head["iters"],
         "residual_per_step": head["res"],
         "mlups": mlups(head["iters"], ncell, head["ms_per_step"]),
+        "learned": learned,
         "compare_fp64_mg": compare,
         "error_vs_fp64_mg": errors,
         "compare_rb": rb,
@@ -376,7 +430,7 @@ def mlups(iters: list[int], ncell: int, ms_per_step: float) -> dict:
                           "whole step as the solver time)"}
 
 
-def field_error_study(args, stream, solver: str, steps: int) -> dict:
+def field_error_study(args, stream, solver: str, steps: int, net=None) -> dict:
     """The headline solver and FP64 multigrid (V(2,2), same rtol and warm
     start) stepped side by side from rest: after every step the L2 and Linf
     differences of u, v, w (relative to the FP64 velocity field as a whole)
@@ -384,8 +438,13 @@ def field_error_study(args, stream, solver: str, steps: int) -> dict:
     import torch
 
     import nusif
-    sims = {"test": nusif.Simulation(bench_case(args.n, solver, args.itermax, args.guess)),
+    tv = bench_case(args.n, solver, args.itermax, args.guess)
+    if net is not None:
+        tv.update(mg_probe=LEARNED_PROBE)
+    sims = {"test": nusif.Simulation(tv),
             "fp64": nusif.Simulation(bench_case(args.n, "mg", args.itermax, args.guess))}
+    if net is not None:
+        sims["test"].set_guess_net(net)
     shape = sims["fp64"].padded_shape
 
     def view(sim, f):
@@ -945,10 +1004,20 @@ def run_learned(args, local):
     net = nusif.UNet(seed=LEARN_SEED)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    log = train(net, data, iters=args.learn_iters, batch=8, lr=1e-3,
+    log = train(net, data, iters=args.learn_iters, batch=args.learn_batch, lr=1e-3,
                 log_every=max(args.learn_iters // 8, 1))
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
+    if args.save_net:
+        from nusif.learn import save_params
+        save_params(net, args.save_net, {
+            "cases": f"{args.learn_runs} lid-driven cavities at {args.learn_n}^3, Re ~ U[100,5000], "
+                     f"lid ~ U[0.5,2.0], seed {LEARN_SEED}",
+            "pairs": int(data.x.shape[0]), "snapshots": f"every 5 steps from step 10 to "
+                                                         f"{args.learn_steps}",
+            "warm_start_base": args.guess, "adam_iters": args.learn_iters, "batch": args.learn_batch,
+            "lr": "1e-3 cosine to 1e-4", "final_loss": log[-1][1] if log else None,
+            "train_s": train_s})
     n = args.n
     evals = {}
     for use in (False, True):
@@ -995,7 +1064,8 @@ def run_learned(args, local):
                                f"snapshots every 5 steps from step 10 to {args.learn_steps}; "
                                f"evaluate at {n}^3, Re 2750, lid 1.25",
                    "warm_start_base": args.guess, "pairs": int(data.x.shape[0]),
-                   "train_iters": args.learn_iters, "batch": 8, "lr": "1e-3 cosine to 1e-4"},
+                   "train_iters": args.learn_iters, "batch": args.learn_batch,
+                   "lr": "1e-3 cosine to 1e-4"},
         "pair_generation_s": data.seconds, "train_s": train_s,
         "train_ms_per_iter": train_s * 1e3 / max(args.learn_iters, 1),
         "loss": log,

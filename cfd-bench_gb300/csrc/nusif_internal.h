@@ -116,10 +116,4 @@ bool launch_adapt_uv(const Dims &g, double dt, double dx, double dy, double dz,
 bool launch_special(const Dims &g, int problem, double lid, double inflow, double *u);
 int problem_code(const char *name);
 
-// ---- host <-> device field copies (output.cu) ----
-// device address of a page-locked host array (nullptr for pageable memory)
-const void *mapped_device_ptr(const void *host);
-// n doubles from src to dst (16-byte aligned, either side may be mapped host memory), by SMs
-bool copy_doubles_sm(double *dst, const double *src, int64_t n);
-
 }  // namespace nusif

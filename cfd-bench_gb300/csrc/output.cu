@@ -17,33 +17,6 @@
 namespace nusif {
 namespace {
 
-// Field copies between device memory and pinned host memory, moved by the SMs
-// over the CPU-GPU link (host memory mapped into the device's address space):
-// every thread keeps four 16-byte loads in flight, the grid covers every SM
-// several times. Used when the host array is page-locked and 16-byte aligned
-// like the field; anything else goes through cudaMemcpyAsync.
-constexpr int kCopyBlock = 256, kCopyUnroll = 4;
-
-__global__ void __launch_bounds__(kCopyBlock) k_copy16(const int4 *__restrict__ src,
-    int4 *__restrict__ dst, int64_t n16)
-{
-  const int64_t stride = (int64_t)gridDim.x * kCopyBlock;
-  int64_t q = blockIdx.x * (int64_t)kCopyBlock + threadIdx.x;
-  for (; q + (kCopyUnroll - 1) * stride < n16; q += kCopyUnroll * stride) {
-    int4 t[kCopyUnroll];
-#pragma unroll
-    for (int r = 0; r < kCopyUnroll; r++) t[r] = src[q + r * stride];
-#pragma unroll
-    for (int r = 0; r < kCopyUnroll; r++) dst[q + r * stride] = t[r];
-  }
-  for (; q < n16; q += stride) dst[q] = src[q];
-}
-
-__global__ void k_copy_tail(const double *__restrict__ src, double *__restrict__ dst)
-{
-  dst[0] = src[0];
-}
-
 __global__ void k_collect(Dims g, const double *__restrict__ u, const double *__restrict__ v,
     const double *__restrict__ w, const double *__restrict__ p, double *__restrict__ out)
 {
@@ -81,38 +54,6 @@ bool host_is_little_endian()
 }
 
 }  // namespace
-
-const void *mapped_device_ptr(const void *host)
-{
-  cudaPointerAttributes a;
-  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
-    cudaGetLastError();  // not a CUDA-known pointer: clear and report "not mapped"
-    return nullptr;
-  }
-  if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return nullptr;
-  return a.devicePointer;
-}
-
-bool copy_doubles_sm(double *dst, const double *src, int64_t n)
-{
-  if (n <= 0) return true;
-  const int64_t n16 = n / 2;
-  int dev = 0, sms = 152;
-  if (cudaGetDevice(&dev) == cudaSuccess)
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int64_t want = (n16 + kCopyBlock * kCopyUnroll - 1) / (kCopyBlock * kCopyUnroll);
-  const int blocks = (int)(want < 8LL * sms ? (want > 0 ? want : 1) : 8LL * sms);
-  if (n16 > 0) {
-    k_copy16<<<blocks, kCopyBlock, 0, stream()>>>(reinterpret_cast<const int4 *>(src),
-        reinterpret_cast<int4 *>(dst), n16);
-    if (!launched("k_copy16")) return false;
-  }
-  if (n & 1) {
-    k_copy_tail<<<1, 1, 0, stream()>>>(src + n - 1, dst + n - 1);
-    if (!launched("k_copy_tail")) return false;
-  }
-  return true;
-}
 
 }  // namespace nusif
 

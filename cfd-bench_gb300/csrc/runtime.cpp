@@ -158,17 +158,9 @@ int nusifDownloadField(const Discretization *d, int which, double *host)
     return NUSIF_ERR_ARG;
   }
   size_t bytes = sizeof(double) * (size_t)st->dims.padded;
-  // page-locked, 16-byte aligned host arrays: copied by the SMs (faster than a copy engine
-  // on the CPU-GPU link); anything else by cudaMemcpyAsync
-  const void *mapped = ((uintptr_t)host & 15u) == 0 ? mapped_device_ptr(host) : nullptr;
-  if (mapped) {
-    if (!copy_doubles_sm(static_cast<double *>(const_cast<void *>(mapped)), src,
-            st->dims.padded))
-      return NUSIF_ERR_CUDA;
-  } else if (!cuda_ok(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, g_stream),
-                 "download field")) {
+  if (!cuda_ok(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, g_stream),
+          "download field"))
     return NUSIF_ERR_CUDA;
-  }
   if (!cuda_ok(cudaStreamSynchronize(g_stream), "download field sync")) return NUSIF_ERR_CUDA;
   return NUSIF_OK;
 }
@@ -182,14 +174,9 @@ int nusifUploadField(Discretization *d, int which, const double *host)
     return NUSIF_ERR_ARG;
   }
   size_t bytes = sizeof(double) * (size_t)st->dims.padded;
-  const void *mapped = ((uintptr_t)host & 15u) == 0 ? mapped_device_ptr(host) : nullptr;
-  if (mapped) {
-    if (!copy_doubles_sm(dst, static_cast<const double *>(mapped), st->dims.padded))
-      return NUSIF_ERR_CUDA;
-  } else if (!cuda_ok(cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, g_stream),
-                 "upload field")) {
+  if (!cuda_ok(cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, g_stream),
+          "upload field"))
     return NUSIF_ERR_CUDA;
-  }
   if (!cuda_ok(cudaStreamSynchronize(g_stream), "upload field sync")) return NUSIF_ERR_CUDA;
   return NUSIF_OK;
 }

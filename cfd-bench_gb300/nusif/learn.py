@@ -107,3 +107,26 @@ def validation_loss(net: UNet, data: PairSet) -> float:
     for s in range(data.x.shape[0]):
         total += net.train_step(data.x[s:s + 1], data.t[s:s + 1], update=False)
     return total / data.x.shape[0]
+
+
+def save_params(net: UNet, path, meta: dict | None = None) -> None:
+    """The network's FP32 parameters (flat, the C ABI's layout) and a
+    description of how they were trained, as a compressed .npz file."""
+    import json
+    from pathlib import Path
+    path = Path(path)
+    path.parent.mkdir(parents=True, exist_ok=True)
+    np.savez_compressed(path, params=net.params(), meta=np.array(json.dumps(meta or {})))
+
+
+def load_net(path, seed: int = 0) -> UNet:
+    """A network with the parameters saved by save_params."""
+    z = np.load(path, allow_pickle=False)
+    net = UNet(seed=seed)
+    net.set_params(z["params"])
+    return net
+
+
+def saved_meta(path) -> dict:
+    import json
+    return json.loads(str(np.load(path, allow_pickle=False)["meta"]))

@@ -62,3 +62,19 @@ def test_fp64_pipe_fraction():
     assert d["fp64_inst_peak_per_s"] == pytest.approx(bench.FP64_LANES_PER_CLOCK * mhz * 1e6)
     assert 0.0 < d["fp64_pipe_frac"] < 1.0
     assert d["fp64_pipe_frac"] == pytest.approx(d["fp64_inst_per_s"] / d["fp64_inst_peak_per_s"])
+
+
+def test_headline_network_file():
+    """The trained warm-start network the default bench line uses: the flat
+    parameter vector of the library's layout and its training record."""
+    import numpy as np
+
+    from nusif.learn import saved_meta
+    from oracle import unet_oracle as U
+    path = bench.NET_PATH
+    assert path.exists()
+    z = np.load(path, allow_pickle=False)
+    assert z["params"].dtype == np.float32 and z["params"].size == U.param_count()
+    assert np.all(np.isfinite(z["params"]))
+    meta = saved_meta(path)
+    assert meta["pairs"] > 0 and "seed" in meta["cases"]

@@ -190,9 +190,8 @@ def test_mg_ref_solve_matches_oracle(nusif_lib, oracle_mod, levels, pre, post):
 @pytest.mark.parametrize("dims", [(3, 3, 3), (8, 6, 4), (33, 17, 9)])
 def test_field_copies_pinned_pageable_unaligned(nusif_lib, dims):
     """nusifUploadField / nusifDownloadField round trips, bit for bit, from
-    page-locked host memory (copied by the SMs over the CPU-GPU link), from
-    pageable memory and from a page-locked array 8 bytes off 16-byte alignment
-    (both through cudaMemcpyAsync); (3,3,3) pads to an odd number of doubles."""
+    page-locked host memory, from pageable memory and from a page-locked array
+    8 bytes off 16-byte alignment; (3,3,3) pads to an odd number of doubles."""
     import ctypes as C
 
     import torch
