@@ -57,6 +57,9 @@ def parse_args():
     ap.add_argument("--solver", default=os.environ.get("NUSIF_BENCH_SOLVER", "auto"))
     ap.add_argument("--n", type=int, default=256, help="cells per axis of the cavity")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--arith", default="df32", choices=["df32", "fp64"],
+                    help="FP64-bound stencils (computeFG, the mixed solver's fine residual) "
+                         "in FP32 pairs (df32) or FP64 instructions (fp64)")
     ap.add_argument("--guess", default="quadratic",
                     choices=["previous", "extrapolate", "quadratic"],
                     help="initial pressure of each V-cycle solve: p(n-1), 2 p(n-1) - p(n-2), "
@@ -196,10 +199,10 @@ MG_SHAPE_FP64_TUNED = (1, 2, 4, 1.3)
 
 def bench_case(n: int, solver: str, itermax: int | None = None,
                guess: str = "previous", shape: tuple | None = None,
-               graph: bool = True) -> dict:
+               graph: bool = True, arith: str = "df32") -> dict:
     from nusif.params import config2
     vals = config2(solver=solver)
-    vals.update(imax=n, jmax=n, kmax=n)
+    vals.update(imax=n, jmax=n, kmax=n, arith=arith)
     if itermax is not None:
         vals["itermax"] = itermax
     if solver in ("mg", "mg-mixed"):
@@ -289,7 +292,8 @@ def run_gpu(args, rank, world, local):
     lib.nusifSetStream(C.c_void_p(stream.cuda_stream))
 
     solver = pick_solver(args.solver)
-    vals = bench_case(args.n, solver, args.itermax, args.guess, graph=not args.no_graph)
+    vals = bench_case(args.n, solver, args.itermax, args.guess, graph=not args.no_graph,
+                      arith=args.arith)
     net = load_headline_net(args, solver)
     if net is not None:
         vals.update(mg_probe=LEARNED_PROBE)
@@ -308,7 +312,7 @@ def run_gpu(args, rank, world, local):
                    "trained": learned_meta(args.net)}
 
     # ---- dominant kernels, timed live with CUDA events on the library stream ----
-    roofs = [] if args.no_roofline else kernel_rooflines(sim, solver, stream, ncell)
+    roofs = [] if args.no_roofline else kernel_rooflines(sim, solver, stream, ncell, args.arith)
 
     phases = step_phases(sim, solver, stream) if args.phases else None
 
@@ -321,7 +325,7 @@ def run_gpu(args, rank, world, local):
     # ---- the same solver without the network ----
     if net is not None:
         sim0 = nusif.Simulation(bench_case(args.n, solver, args.itermax, args.guess,
-                                           graph=not args.no_graph))
+                                           graph=not args.no_graph, arith=args.arith))
         alone = timed_steps(sim0, args, stream, local, world)
         sim0.close()
         learned.update({"ms_per_step_without_network": alone["ms_per_step"],
@@ -337,7 +341,7 @@ def run_gpu(args, rank, world, local):
                 (args.guess, MG_SHAPE_FP64_TUNED)]
         for g, shape in dict.fromkeys(arms):
             sim64 = nusif.Simulation(bench_case(args.n, "mg", args.itermax, g, shape,
-                                                graph=not args.no_graph))
+                                                graph=not args.no_graph, arith=args.arith))
             ref64 = timed_steps(sim64, args, stream, local, world)
             sim64.close()
             compare.append({"solver": "mg (FP64 V-cycles, same rtol 1e-6)", "guess": g,
@@ -393,6 +397,9 @@ def run_gpu(args, rank, world, local):
                                "V(%d,%d), omega %.2f" % (MG_SHAPE["mg"][0], MG_SHAPE["mg"][1],
                                                          MG_SHAPE["mg"][3])
                                if solver == "mg" else None),
+                   "arith": ("computeFG and the mixed solver's fine residual in FP32 pairs "
+                             "(double-float, about 2^-47 of the operands)" if args.arith == "df32"
+                             else "all FP64 stencils in FP64 instructions"),
                    "solve_launch": ("host-driven launches" if args.no_graph else
                                     "one CUDA graph per solve (device while-loops)"),
                    "l2": "no flush: 8 FP64 fields of %.0f MB each, far larger than L2" % (padded * 8 / 1e6),
@@ -438,11 +445,14 @@ def field_error_study(args, stream, solver: str, steps: int, net=None) -> dict:
     import torch
 
     import nusif
-    tv = bench_case(args.n, solver, args.itermax, args.guess)
+    tv = bench_case(args.n, solver, args.itermax, args.guess, arith=args.arith)
     if net is not None:
         tv.update(mg_probe=LEARNED_PROBE)
+    # the reference arm is FP64 throughout: FP64 V-cycles and every stencil in
+    # FP64 instructions (arith fp64), so the difference covers the pair arithmetic too
     sims = {"test": nusif.Simulation(tv),
-            "fp64": nusif.Simulation(bench_case(args.n, "mg", args.itermax, args.guess))}
+            "fp64": nusif.Simulation(bench_case(args.n, "mg", args.itermax, args.guess,
+                                                arith="fp64"))}
     if net is not None:
         sims["test"].set_guess_net(net)
     shape = sims["fp64"].padded_shape
@@ -471,7 +481,8 @@ def field_error_study(args, stream, solver: str, steps: int, net=None) -> dict:
             err[f]["linf"].append(float(d.abs().max()) / max(max_ref, 1e-300))
     for sim in sims.values():
         sim.close()
-    return {"against": "FP64 multigrid V(2,2), same rtol 1e-6 and warm start, stepped alongside",
+    return {"against": "FP64 multigrid V(2,2), every stencil in FP64 instructions, same rtol "
+                       "1e-6 and warm start, stepped alongside",
             "steps": steps,
             "max": {f: {k: max(v) for k, v in err[f].items()} for f in "uvwp"},
             "final": {f: {k: v[-1] for k, v in err[f].items()} for f in "uvwp"},
@@ -485,7 +496,7 @@ def rb_arm(args, stream, local, world) -> dict:
     import torch
 
     import nusif
-    vals = bench_case(args.n, "rb", args.itermax)
+    vals = bench_case(args.n, "rb", args.itermax, arith=args.arith)
     sim = nusif.Simulation(vals)
     sim.step()
     torch.cuda.synchronize()
@@ -601,14 +612,16 @@ def _roof(name, kernel_key, ms, algo_bytes, ncell, peak, src, **extra):
          "launch_ms": ms, "algorithmic_bytes_per_launch": algo_bytes,
          "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else src,
          "share_of_step": prof.get("share_of_step"),
-         "ncu_fp64_pipe_frac": prof.get("fp64_pipe_frac")}
+         "ncu": {k: prof[k] for k in ("fp64_pipe_frac", "fma_pipe_frac", "alu_pipe_frac",
+                                      "issue_active", "dram_frac") if k in prof} or None}
     d.update(extra)
     return d
 
 
-def kernel_rooflines(sim, solver, stream, ncell):
+def kernel_rooflines(sim, solver, stream, ncell, arith: str = "df32"):
     """Average launch duration (CUDA events) of the step's heaviest kernels and
-    their achieved bandwidth on algorithmic bytes. First entry: the dominant one."""
+    their achieved bandwidth on algorithmic bytes. The line's ``roofline`` is
+    the entry with the largest measured share of the step."""
     import torch
     peak, src = hbm_peak()
     lib = sim.lib
@@ -644,10 +657,17 @@ def kernel_rooflines(sim, solver, stream, ncell):
                              "k_rbgs_sweep", msr.value, 12.0 * ncell, ncell, peak, src))
             lib.nusifTimeKernel(C.byref(sim.s), sim.d.p, sim.d.rhs, 1, reps, C.byref(msr))
             abi.check(lib)
-            out.append(_roof("k_mx_residual: FP64 residual of p into FP32 (refinement)",
-                             "k_mx_residual", msr.value, 20.0 * ncell, ncell, peak, src,
-                             note="FP64-pipe bound: 9 FP64 instructions per cell",
-                             fp64=_fp64_pipe(9.0, ncell, msr.value)))
+            # p and b read (FP64), the FP32 residual written and the FP32 correction zeroed
+            if arith == "df32":
+                out.append(_roof("k_mx_residual_df: fine residual of p into FP32, double-float "
+                                 "stencil (refinement)", "k_mx_residual_df", msr.value,
+                                 20.0 * ncell, ncell, peak, src,
+                                 note="stencil in FP32 pairs on the FP32 pipe"))
+            else:
+                out.append(_roof("k_mx_residual: FP64 residual of p into FP32 (refinement)",
+                                 "k_mx_residual", msr.value, 20.0 * ncell, ncell, peak, src,
+                                 note="FP64-pipe bound: 9 FP64 instructions per cell",
+                                 fp64=_fp64_pipe(9.0, ncell, msr.value)))
         else:
             out.append(_roof("k_mg_smooth<double>: one colour pass of the fine FP64 smoother",
                              "k_mg_smooth_f64", msr.value, 12.0 * ncell, ncell, peak, src,
@@ -663,11 +683,16 @@ def kernel_rooflines(sim, solver, stream, ncell):
     e1.record(stream)
     torch.cuda.synchronize()
     ms_fg = e0.elapsed_time(e1) / reps
-    g0 = sim.d.gx == 0.0 and sim.d.gy == 0.0 and sim.d.gz == 0.0
-    fg_inst = 70.4 if g0 else 73.4  # per cell, counted from the kernel (halo share included)
-    out.append(_roof("k_fgh_flux: computeFG (FP64)", "k_fgh_flux", ms_fg, 48.0 * ncell, ncell,
-                     peak, src, note="FP64-pipe bound: about %.0f FP64 instructions per cell"
-                     % fg_inst, fp64=_fp64_pipe(fg_inst, ncell, ms_fg)))
+    if arith == "df32":
+        out.append(_roof("k_fgh_df: computeFG, face fluxes in double-float pairs", "k_fgh_df",
+                         ms_fg, 48.0 * ncell, ncell, peak, src,
+                         note="FP32-pipe / issue bound (pair arithmetic), not HBM"))
+    else:
+        g0 = sim.d.gx == 0.0 and sim.d.gy == 0.0 and sim.d.gz == 0.0
+        fg_inst = 70.4 if g0 else 73.4  # per cell, counted from the kernel (halo share included)
+        out.append(_roof("k_fgh_flux: computeFG (FP64)", "k_fgh_flux", ms_fg, 48.0 * ncell,
+                         ncell, peak, src, note="FP64-pipe bound: about %.0f FP64 instructions "
+                         "per cell" % fg_inst, fp64=_fp64_pipe(fg_inst, ncell, ms_fg)))
     return out
 
 
@@ -684,17 +709,21 @@ def run_e2e(sim, args, stream, padded):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        # queued copies: p's upload overlaps computeTimestep .. computeRHS, which do
+        # not read p; every library call waits on the device for the fields it uses
         for f in "uvwp":
-            lib.nusifUploadField(C.byref(sim.d), idx[f], ptrs[f])
+            lib.nusifUploadFieldAsync(C.byref(sim.d), idx[f], ptrs[f])
         sim.step()
         for f in "uvwp":
-            lib.nusifDownloadField(C.byref(sim.d), idx[f], ptrs[f])
+            lib.nusifDownloadFieldAsync(C.byref(sim.d), idx[f], ptrs[f])
+        lib.nusifWaitCopies()
     torch.cuda.synchronize()
     abi.check(lib)
     ms = (time.perf_counter() - t0) * 1e3 / args.steps
     return {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 4 * 8 * padded,
             "d2h_bytes_per_step": 4 * 8 * padded,
-            "path": "C ABI: nusifUploadField x4, reference step calls, nusifDownloadField x4"}
+            "path": "C ABI: nusifUploadFieldAsync x4 (pinned host arrays), the reference's "
+                    "step calls, nusifDownloadFieldAsync x4, nusifWaitCopies"}
 
 
 # ---------------------------------------------------------------- CPU side

@@ -16,11 +16,14 @@
 // 2^-53 of the operands). Skipping the renormalisation saves three
 // operations per result but, measured on computeFG, doubles the error.
 //
-// split() turns a binary64 number into a pair with 32-bit integer operations
-// (the hardware double -> float conversion runs on the FP64 pipe): hi is x
-// with its fraction truncated to 23 bits, lo the 29 dropped bits rounded to a
-// float, so hi + lo = x to 2^-47 |x|. Magnitudes below 2^-126 become 0 and
-// beyond the float range hi takes the hardware conversion (infinite).
+// split() turns a binary64 number into a pair without conversion
+// instructions (GB300 runs double -> float and integer -> float conversions on
+// its FP64 pipe): hi is x with its fraction truncated to 23 bits (integer
+// operations), lo the 29 dropped bits rounded to a float (two exact FP32
+// subtractions and one fused multiply-add), so hi + lo = x to 2^-47 |x|
+// (to 2^-97 for |x| < 2^-74).
+// Magnitudes below 2^-126 become 0 and beyond the float range hi takes the
+// hardware conversion (infinite), out of line.
 //
 // The header compiles for the device and, for CPU checks of the arithmetic,
 // for the host (plain C++ with fmaf from <cmath>).
@@ -99,15 +102,6 @@ DF_FN double from_words(unsigned hi, unsigned lo)
 #endif
 }
 
-DF_FN float u32_to_f32(unsigned r)
-{
-#ifdef __CUDA_ARCH__
-  return __uint2float_rn(r);
-#else
-  return (float)r;
-#endif
-}
-
 DF_FN float fmaf_(float a, float b, float c)
 {
 #ifdef __CUDA_ARCH__
@@ -138,32 +132,60 @@ DF_FN float mul_(float a, float b)
 #endif
 }
 
-// binary64 -> pair on the integer pipe (see the header comment)
+// Rare cases of split() and widen(), out of line on the device: GB300 runs
+// the hardware double <-> float and integer -> float conversions on its FP64
+// pipe, and a conversion the compiler if-converts into the common path would
+// issue for every value.
+#ifdef __CUDA_ARCH__
+#define DF_RARE __device__ __noinline__
+#else
+#define DF_RARE inline
+#endif
+
+// |x| outside the normal float range: zeros and tiny values (below 2^-126)
+// become zero, huge values, infinities and NaN take the hardware conversion
+DF_RARE f2 split_rare(double x)
+{
+  f2 r;
+  const unsigned h = hi_word(x);
+  const unsigned e = (h >> 20) & 0x7ffu;
+  if (e < 897u) {
+    r.hi = f32_from_bits(h & 0x80000000u);
+  } else {
+    r.hi = (float)x;
+  }
+  r.lo = 0.0f;
+  return r;
+}
+
+// float subnormals, infinities and NaN
+DF_RARE double widen_rare(float x) { return (double)x; }
+
+// binary64 -> pair on the integer and FP32 pipes (see the header comment)
 DF_FN f2 split(double x)
 {
   const unsigned h = hi_word(x), l = lo_word(x);
   const unsigned e = (h >> 20) & 0x7ffu;
+  if (e - 897u > 253u) return split_rare(x);  // truncated value outside the normal float range
   const unsigned sign = h & 0x80000000u;
   f2 r;
-  if (e - 897u <= 253u) {  // truncated value in the normal float range (exponent 1..254)
-    r.hi = f32_from_bits(sign | ((e - 896u) << 23) | ((h & 0xfffffu) << 3) | (l >> 29));
-    // the 29 dropped bits weigh 2^(e - 1023 - 52) each; that scale is a normal
-    // float for e >= 949 (below, the remainder is under 2^-97 |x|: dropped)
-    const unsigned rest = l & 0x1fffffffu;
-    const float scale = f32_from_bits(e >= 949u ? ((e - 948u) << 23) : 0u);
-    r.lo = f32_from_bits(f32_bits(mul_(u32_to_f32(rest), scale)) | sign);
-  } else if (e < 897u) {  // below 2^-126 (zeros, FP64 subnormals): zero
-    r.hi = f32_from_bits(sign);
-    r.lo = 0.0f;
-  } else {  // beyond the float range, infinities, NaN
-    r.hi = (float)x;
-    r.lo = 0.0f;
-  }
+  r.hi = f32_from_bits(sign | ((e - 896u) << 23) | ((h & 0xfffffu) << 3) | (l >> 29));
+  // the 29 dropped bits, an integer below 2^29, rounded to a float without a
+  // conversion instruction: its two parts below 2^23 and 2^6 are exact as
+  // (2^23 + n) - 2^23, and one fused multiply-add rounds their sum once
+  const unsigned rest = l & 0x1fffffffu;
+  const float top = add_(f32_from_bits(0x4b000000u | (rest >> 6)), -8388608.0f);
+  const float low = add_(f32_from_bits(0x4b000000u | (rest & 63u)), -8388608.0f);
+  const float rn = fmaf_(top, 64.0f, low);
+  // they weigh 2^(e - 1023 - 52) each; that scale is a normal float for
+  // e >= 949 (below, |x| < 2^-74 and the remainder, under 2^-97, is dropped)
+  const float scale = f32_from_bits(e >= 949u ? ((e - 948u) << 23) : 0u);
+  r.lo = f32_from_bits(f32_bits(mul_(rn, scale)) | sign);
   return r;
 }
 
 // exact binary32 -> binary64 widening on the integer pipe (normal floats and
-// zeros; anything else through the hardware conversion)
+// zeros; the rest through the hardware conversion, out of line)
 DF_FN double widen(float x)
 {
   const unsigned b = f32_bits(x);
@@ -171,7 +193,7 @@ DF_FN double widen(float x)
   if (e - 1u <= 253u)
     return from_words((b & 0x80000000u) | (((b & 0x7fffffffu) >> 3) + (896u << 20)), b << 29);
   if ((b & 0x7fffffffu) == 0u) return from_words(b & 0x80000000u, 0u);
-  return (double)x;
+  return widen_rare(x);
 }
 
 // a pair as a binary64 number (one FP64 add; both widenings are exact)

@@ -7,6 +7,7 @@
 // src/util.h:19-34). Threads map x -> i so every warp touches consecutive
 // doubles. All arithmetic is FP64 (the reference computes in double).
 #include <cfloat>
+#include <initializer_list>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -727,6 +728,15 @@ using namespace nusif;
 
 namespace {
 
+// the launch stream waits for queued asynchronous copies of these fields
+bool await_arrays(std::initializer_list<const double *> fields)
+{
+  const void *f[8];
+  int n = 0;
+  for (const double *x : fields) f[n++] = x;
+  return await_copies(f, n);
+}
+
 DiscState *need_state(const Discretization *d, const char *what)
 {
   DiscState *st = disc_state(d);
@@ -867,7 +877,7 @@ void initDiscretization(Discretization *s, Parameter *params)
 void computeTimestep(Discretization *s)
 {
   DiscState *st = need_state(s, "computeTimestep");
-  if (!st) return;
+  if (!st || !await_arrays({ s->u, s->v, s->w })) return;
   if (!launch_max3(st->dims, s->u, s->v, s->w, st->red, st->d_scalars)) return;
   if (!cuda_ok(cudaMemcpyAsync(st->h_scalars, st->d_scalars, 3 * sizeof(double),
                    cudaMemcpyDeviceToHost, stream()),
@@ -886,7 +896,7 @@ void computeTimestep(Discretization *s)
 void setBoundaryConditions(Discretization *s)
 {
   DiscState *st = need_state(s, "setBoundaryConditions");
-  if (!st) return;
+  if (!st || !await_arrays({ s->u, s->v, s->w })) return;
   const int bc[6] = { s->bcLeft, s->bcRight, s->bcBottom, s->bcTop, s->bcFront, s->bcBack };
   launch_bc(st->dims, bc, PROBLEM_NONE, 0.0, 0.0, s->u, s->v, s->w);
 }
@@ -895,14 +905,14 @@ void setBoundaryConditions(Discretization *s)
 void setSpecialBoundaryCondition(Discretization *s)
 {
   DiscState *st = need_state(s, "setSpecialBoundaryCondition");
-  if (!st) return;
+  if (!st || !await_arrays({ s->u })) return;
   launch_special(st->dims, problem_code(s->problem), st->ext.lid, st->ext.inflow, s->u);
 }
 
 void computeFG(Discretization *s)
 {
   DiscState *st = need_state(s, "computeFG");
-  if (!st) return;
+  if (!st || !await_arrays({ s->u, s->v, s->w, s->f, s->g, s->h })) return;
   launch_fgh(st->dims, s->re, s->gamma, s->gx, s->gy, s->gz, s->dt, s->grid.dx, s->grid.dy,
       s->grid.dz, s->u, s->v, s->w, s->f, s->g, s->h, nullptr, 0, st->ext.fg_fp64 != 0);
 }
@@ -910,14 +920,14 @@ void computeFG(Discretization *s)
 void computeRHS(Discretization *s)
 {
   DiscState *st = need_state(s, "computeRHS");
-  if (!st) return;
+  if (!st || !await_arrays({ s->f, s->g, s->h, s->rhs })) return;
   launch_rhs(st->dims, s->dt, s->grid.dx, s->grid.dy, s->grid.dz, s->f, s->g, s->h, s->rhs);
 }
 
 void normalizePressure(Discretization *s)
 {
   DiscState *st = need_state(s, "normalizePressure");
-  if (!st) return;
+  if (!st || !await_arrays({ s->p })) return;
   if (!launch_interior_sum(st->dims, s->p, st->red, st->d_scalars + 3)) return;
   launch_subtract_mean(st->dims, s->p, st->d_scalars + 4);
 }
@@ -925,7 +935,7 @@ void normalizePressure(Discretization *s)
 void adaptUV(Discretization *s)
 {
   DiscState *st = need_state(s, "adaptUV");
-  if (!st) return;
+  if (!st || !await_arrays({ s->f, s->g, s->h, s->p, s->u, s->v, s->w })) return;
   launch_adapt_uv(st->dims, s->dt, s->grid.dx, s->grid.dy, s->grid.dz, s->f, s->g, s->h, s->p,
       s->u, s->v, s->w);
 }
@@ -934,6 +944,7 @@ void nusifFreeDiscretization(Discretization *s)
 {
   DiscState *st = disc_state(s);
   if (!st) return;
+  await_fields(s);
   cudaStreamSynchronize(stream());
   double **fields[8] = { &s->u, &s->v, &s->w, &s->p, &s->rhs, &s->f, &s->g, &s->h };
   for (int q = 0; q < 8; q++) {

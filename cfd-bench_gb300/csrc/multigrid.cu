@@ -32,6 +32,7 @@
 #include <map>
 #include <vector>
 
+#include "df32.cuh"
 #include "fp_bits.cuh"
 #include "nusif_internal.h"
 #include "reduce.cuh"
@@ -120,6 +121,7 @@ struct MgHierarchy {
   // without its inner loop, one inner V-cycle, tail
   int n_head = 0, n_outer = 0, n_inner = 0, n_tail = 0;
   int n_inner_capture = 0;  // scratch while capturing
+  bool mx_df = true;  // mg-mixed: fine residual in double-float arithmetic (key arith)
   double *h_ptrs[2 * kMaxLevels] = {};  // exposed through Solver::r / Solver::e
 };
 
@@ -537,6 +539,116 @@ __global__ void __launch_bounds__(kNT) k_mx_residual(View<double> f, float *r32,
   if (!last) return;
   const double total = fold_partials<kNT>(partials, gridDim.x, sm);
   if (threadIdx.x == 0) {
+    st->res2 = total;
+    const int m = st->outer;  // corrections applied before this residual
+    st->done = (total <= st->tol2) || (m >= st->maxcycles);
+    if (!st->done) {
+      st->outer = m + 1;
+      st->inner_done = 0;
+      st->inner_it = 0;
+      if (count_cycles) st->cycles += 1;
+    }
+    *ticket = 0;
+  }
+}
+
+// The same residual, stop test and side effects as k_mx_residual, with the
+// stencil carried in double-float arithmetic (df32.cuh: pairs of FP32
+// numbers on the FP32 pipe, about 2^-47 of the operands) instead of nine FP64
+// instructions per cell, which bound that kernel at 256^3 (FP64 issue, not
+// HBM). The residual's error is then a few units of 2^-47 of diag |x|, which
+// near convergence is the scale of the cancellation b - A x; the stop test
+// compares it with rtol ||b||, 1e-6 to 1e-8 here, far above that error.
+// The norm is accumulated as a pair and folded in FP64.
+//
+// Mapping: a 32 x 8 tile of columns marching over kb planes. Plane k's pairs
+// (the tile and a one-cell ring) sit in shared memory, double-buffered so a
+// plane needs one barrier; the column's k-1 and k+1 pairs stay in registers.
+// Indices outside the grid are clamped to it, which is the Neumann rule
+// itself (a missing neighbour is the cell). Each value is split into its pair
+// once per block (ring cells once more by the neighbouring block).
+__global__ void __launch_bounds__(kNT) k_mx_residual_df(View<double> f, float *r32, MgState *st,
+    double *partials, unsigned *ticket, int count_cycles, float *e_zero, int kb)
+{
+  using namespace df;
+  if (solve_finished(st)) return;
+  __shared__ f2 pl[2][kBY + 2][kBX + 2];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kBX + tx;
+  const int i0 = blockIdx.x * kBX, j0 = blockIdx.y * kBY;
+  const bool active = i0 + tx < f.nx && j0 + ty < f.ny;
+  const int i = min(i0 + tx, f.nx - 1), j = min(j0 + ty, f.ny - 1);
+  const int k0 = blockIdx.z * kb, k1 = min(k0 + kb, f.nz);
+  const double *x = f.x;
+  // ring cell of this thread (threads 0..79): rows j0-1 and j0+8, columns i0-1 and i0+32
+  const bool ring = tid < 2 * kBX + 2 * kBY;
+  int rr = 0, rc = 0, roff = 0;
+  if (ring) {
+    if (tid < 2 * kBX) {
+      rc = (tid & (kBX - 1)) + 1;
+      rr = tid < kBX ? 0 : kBY + 1;
+    } else {
+      const int q = tid - 2 * kBX;
+      rr = (q & (kBY - 1)) + 1;
+      rc = q < kBY ? 0 : kBX + 1;
+    }
+    const int ri = min(max(i0 - 1 + rc, 0), f.nx - 1), rj = min(max(j0 - 1 + rr, 0), f.ny - 1);
+    roff = f.off + rj * f.sy + ri;
+  }
+  const int coff = f.off + j * f.sy + i;
+  double acc_d = 0.0;
+  if (k0 < k1) {
+    const f2 ex = from_double_rn(f.ex), ey = from_double_rn(f.ey), ez = from_double_rn(f.ez);
+    const f2 mdiag = from_double_rn(-f.diag), sh = split(st->shift);
+    const auto plane = [&](int k) { return (int64_t)min(max(k, 0), f.nz - 1) * f.sz; };
+    f2 zb = split(x[plane(k0 - 1) + coff]);
+    f2 zc = split(x[plane(k0) + coff]);
+    double xn = x[plane(k0 + 1) + coff];           // the column's next plane (raw)
+    double rn = ring ? x[plane(k0) + roff] : 0.0;  // this thread's ring cell of the next plane
+    f2 acc{ 0.0f, 0.0f };
+    int buf = 0;
+    for (int k = k0; k < k1; k++) {
+      const int64_t pk = (int64_t)k * f.sz;
+      const double bv = f.b[pk + coff];
+      pl[buf][ty + 1][tx + 1] = zc;
+      if (ring) pl[buf][rr][rc] = split(rn);
+      const f2 zt = split(xn);
+      if (k + 1 < k1) {
+        xn = x[plane(k + 2) + coff];
+        if (ring) rn = x[pk + f.sz + roff];
+      }
+      __syncthreads();
+      const f2 sx = add(pl[buf][ty + 1][tx], pl[buf][ty + 1][tx + 2]);
+      const f2 sy = add(pl[buf][ty][tx + 1], pl[buf][ty + 2][tx + 1]);
+      const f2 sz = add(zb, zt);
+      f2 t = fma(mdiag, zc, sh);
+      t = fma(sx, ex, t);
+      t = fma(sy, ey, t);
+      t = fma(sz, ez, t);
+      const f2 r = sub(split(bv), t);
+      if (active) {
+        const int64_t q = ((int64_t)k * f.ny + j) * f.nx + i;
+        r32[q] = r.hi;  // the pair is renormalised: hi is its value rounded to FP32
+        if (e_zero) e_zero[q] = 0.0f;
+        acc = add(acc, mul(r, r));
+      }
+      zb = zc;
+      zc = zt;
+      buf ^= 1;
+    }
+    acc_d = to_double(acc);
+  }
+  __shared__ double sm[kNT / 32];
+  acc_d = block_reduce_sum<kNT>(acc_d, sm);
+  __shared__ bool last;
+  const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (tid == 0) {
+    partials[bid] = acc_d;
+    last = ticket_is_last(ticket);
+  }
+  __syncthreads();
+  if (!last) return;
+  const double total = fold_partials<kNT>(partials, gridDim.x * gridDim.y * gridDim.z, sm);
+  if (tid == 0) {
     st->res2 = total;
     const int m = st->outer;  // corrections applied before this residual
     st->done = (total <= st->tol2) || (m >= st->maxcycles);
@@ -1545,6 +1657,42 @@ int flat_blocks(int64_t n)
   return (int)(b < cap ? (b > 0 ? b : 1) : cap);
 }
 
+// grid of k_mx_residual_df: 32 x 8 column tiles, the planes split into chunks
+// so that about 8 blocks per SM run (the kernel's partials fit mx_df_blocks)
+dim3 mx_df_grid(int nx, int ny, int nz, int *kb)
+{
+  const int gx = (nx + kBX - 1) / kBX, gy = (ny + kBY - 1) / kBY;
+  int gz = (int)std::max<int64_t>(1, 8 * (int64_t)sm_count_mg() / ((int64_t)gx * gy));
+  gz = std::min(gz, nz);
+  *kb = (nz + gz - 1) / gz;
+  gz = (nz + *kb - 1) / *kb;
+  return dim3(gx, gy, gz);
+}
+
+int mx_df_blocks(int nx, int ny, int nz)
+{
+  int kb;
+  const dim3 g = mx_df_grid(nx, ny, nz, &kb);
+  return (int)(g.x * g.y * g.z);
+}
+
+// the FP64 residual of mg-mixed (count_cycles, e_zero: see k_mx_residual)
+bool mx_residual(MgHierarchy *H, const View<double> &v0, MgState *st, int count_cycles,
+    float *e_zero)
+{
+  if (H->mx_df) {
+    int kb;
+    const dim3 grid = mx_df_grid(v0.nx, v0.ny, v0.nz, &kb);
+    k_mx_residual_df<<<grid, dim3(kBX, kBY), 0, stream()>>>(v0, H->b32[0], st, H->red.partials,
+        H->red.ticket, count_cycles, e_zero, kb);
+    return launched("k_mx_residual_df");
+  }
+  const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
+  k_mx_residual<<<flat_blocks(n0), kNT, 0, stream()>>>(v0, H->b32[0], st, H->red.partials,
+      H->red.ticket, count_cycles, e_zero);
+  return launched("k_mx_residual");
+}
+
 template <typename T, int FOLD>
 bool restrict_to(const View<T> &f, T *bc, const MgLevelDesc &C, const double *shift, MgState *st,
     ReduceScratch &red)
@@ -1930,9 +2078,7 @@ bool cycle_mixed(MgHierarchy *H, double *p, const double *rhs)
   MgState *st = H->d_state;
   View<double> v0 = padded_view(H->lv[0], p, rhs);
   const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
-  k_mx_residual<<<flat_blocks(n0), kNT, 0, stream()>>>(v0, H->b32[0], st, H->red.partials,
-      H->red.ticket, H->nl == 1 ? 1 : 0, nullptr);
-  if (!launched("k_mx_residual")) return false;
+  if (!mx_residual(H, v0, st, H->nl == 1 ? 1 : 0, nullptr)) return false;
   const int inner = H->nl == 1 ? 1 : H->inner;
   for (int q = 0; q < inner; q++)
     if (!vcycle<float>(H, 0, H->x32, H->b32, q == 0, true)) return false;
@@ -1955,6 +2101,7 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
   H->maxcycles = x.mg_maxcycles;
   H->inner = x.mg_inner < 1 ? 1 : x.mg_inner;
   H->theta = x.mg_theta;
+  H->mx_df = !x.arith_fp64;
   H->keep_on_skip = (H->pre % 2 != 0 || H->post % 2 != 0) ? 1 : 0;
   H->guess = x.mg_guess == 1 || x.mg_guess == 2 ? x.mg_guess : 0;
   H->use_graph = x.mg_graph != 0;
@@ -2038,7 +2185,9 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
     }
   }
   const int64_t n0 = (int64_t)d->grid.imax * d->grid.jmax * d->grid.kmax;
-  if (!reduce_scratch_alloc(H->red, flat_blocks(n0) + 16)) return false;
+  const int red_blocks = std::max(flat_blocks(n0),
+      mx_df_blocks(d->grid.imax, d->grid.jmax, d->grid.kmax));
+  if (!reduce_scratch_alloc(H->red, red_blocks + 16)) return false;
   if (!cuda_ok(cudaMalloc(&H->stats2, sizeof(double) * (size_t)flat_blocks(n0)),
           "cudaMalloc(rhs partials)"))
     return false;
@@ -2197,9 +2346,7 @@ bool cycle_mixed_nested(MgHierarchy *H, double *p, const double *rhs, cudaStream
   MgState *st = H->d_state;
   View<double> v0 = padded_view(H->lv[0], p, rhs);
   const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
-  k_mx_residual<<<flat_blocks(n0), kNT, 0, stream()>>>(v0, H->b32[0], st, H->red.partials,
-      H->red.ticket, 0, H->x32[0]);
-  if (!launched("k_mx_residual")) return false;
+  if (!mx_residual(H, v0, st, 0, H->x32[0])) return false;
   cudaStream_t s = stream();
   cudaGraphConditionalHandle h;
   if (!make_handle(s, 0, 0, &h)) return false;
@@ -2428,7 +2575,6 @@ bool mg_time_kernel(SolverState *ss, const double *p, const double *rhs, int whi
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   View<double> v0 = padded_view(H->lv[0], pcopy, rhs);
-  const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
   // which >= 2 (mg-mixed): one FP32 V-cycle from level which - 2 down, from
   // zero on that level's current right-hand side, captured once as a CUDA
   // graph and replayed (as inside a solve)
@@ -2463,9 +2609,7 @@ bool mg_time_kernel(SolverState *ss, const double *p, const double *rhs, int whi
       if (which >= 2) {
         ok = cuda_ok(cudaGraphLaunch(vge, stream()), "timing graph launch");
       } else if (which == 1 && H->mode == 1) {
-        k_mx_residual<<<flat_blocks(n0), kNT, 0, stream()>>>(v0, H->b32[0], tst, H->red.partials,
-            H->red.ticket, 0, nullptr);
-        ok = launched("k_mx_residual");
+        ok = mx_residual(H, v0, tst, 0, nullptr);
       } else if (H->mode == 1) {
         ok = fused_sweeps(H, 0, 1, false, tst);  // one whole sweep
       } else {

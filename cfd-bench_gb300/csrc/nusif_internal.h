@@ -14,6 +14,11 @@ void fail(int code, const char *fmt, ...);  // records or exits per error mode
 bool cuda_ok(cudaError_t e, const char *what);  // false after recording a failure
 bool has_error();                              // an error is pending (record mode)
 cudaStream_t stream();
+// asynchronous field copies (runtime.cpp): make the launch stream wait for the
+// queued copies of these device arrays / of every array / of d's eight fields
+bool await_copies(const void *const *ptrs, int n);
+bool await_all_copies();
+bool await_fields(const Discretization *d);
 // after every kernel launch: counts it and checks the launch error
 bool launched(const char *what);
 unsigned long long launch_count();
@@ -43,6 +48,8 @@ struct Extras {
   int mg_guess_probe = 1;    // key mg_probe: learned guess every P-th step after 2 rejections
   int mg_maxcycles = 100;
   int fg_fp64 = 0;           // key fg_arith: computeFG in FP64 instructions (fp64) or FP32 pairs (df32)
+  int arith_fp64 = 0;        // key arith: every FP64-bound stencil in FP64 instructions (fp64)
+                             // or FP32 pairs (df32); also sets fg_arith
 };
 Extras *extras_for(const Parameter *p, bool create);
 

@@ -68,6 +68,7 @@ int nusifCollectResult(const Discretization *d, double *ug, double *vg, double *
     fail(NUSIF_ERR_ARG, "nusifCollectResult: unknown discretization or null output");
     return NUSIF_ERR_ARG;
   }
+  if (!await_fields(d)) return NUSIF_ERR_CUDA;
   const Dims &g = st->dims;
   const int64_t n = (int64_t)g.imax * g.jmax * g.kmax;
   double *dev = nullptr;

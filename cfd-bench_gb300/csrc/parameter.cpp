@@ -114,6 +114,15 @@ int apply_extra(Parameter *param, const char *tok, const char *val)
     }
     hit = 1;
   }
+  if (starts_with(tok, "arith")) {
+    if (strcmp(v, "fp64") == 0) x->arith_fp64 = x->fg_fp64 = 1;
+    else if (strcmp(v, "df32") == 0) x->arith_fp64 = x->fg_fp64 = 0;
+    else {
+      fail(NUSIF_ERR_ARG, "unknown arith '%s' (df32, fp64)", v);
+      return 1;
+    }
+    hit = 1;
+  }
   if (starts_with(tok, "mg_guess")) {
     if (strcmp(v, "previous") == 0) x->mg_guess = 0;
     else if (strcmp(v, "extrapolate") == 0) x->mg_guess = 1;

@@ -8,6 +8,7 @@
 #include <mutex>
 #include <string>
 #include <unordered_map>
+#include <vector>
 
 #include "nusif_internal.h"
 
@@ -111,6 +112,100 @@ void disc_state_erase(const Discretization *d)
   t.erase(it);
 }
 
+// ---- asynchronous field copies ----
+// nusifUploadFieldAsync / nusifDownloadFieldAsync queue a copy on a copy
+// stream of the library (one per device), after the work already queued on
+// the launch stream; the copy's completion event is kept per device pointer.
+// The first later entry point that touches that pointer makes the launch
+// stream wait for the event (on the device: the host does not wait), so an
+// upload can overlap the kernels that do not read its field, and a queued
+// download is never overwritten by a later kernel.
+namespace {
+std::mutex g_copy_mu;
+std::unordered_map<int, cudaStream_t> g_copy_streams;     // device -> copy stream
+std::unordered_map<const void *, cudaEvent_t> g_pending;  // device pointer -> its last copy
+std::vector<cudaEvent_t> g_spare_events;
+
+cudaEvent_t take_event()
+{
+  if (!g_spare_events.empty()) {
+    cudaEvent_t e = g_spare_events.back();
+    g_spare_events.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (!cuda_ok(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "copy event")) return nullptr;
+  return e;
+}
+
+cudaStream_t copy_stream()
+{
+  int dev = 0;
+  if (!cuda_ok(cudaGetDevice(&dev), "copy stream device")) return nullptr;
+  auto it = g_copy_streams.find(dev);
+  if (it != g_copy_streams.end()) return it->second;
+  cudaStream_t s = nullptr;
+  if (!cuda_ok(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "copy stream")) return nullptr;
+  g_copy_streams[dev] = s;
+  return s;
+}
+
+// queue one copy of `bytes` touching the device array `field`
+bool queue_copy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, const void *field)
+{
+  std::lock_guard<std::mutex> lock(g_copy_mu);
+  cudaStream_t cs = copy_stream();
+  if (!cs) return false;
+  cudaEvent_t after = take_event();
+  if (!after) return false;
+  // after the launch stream's work so far (which may read or write the field)
+  bool ok = cuda_ok(cudaEventRecord(after, g_stream), "copy order record") &&
+            cuda_ok(cudaStreamWaitEvent(cs, after, 0), "copy order wait") &&
+            cuda_ok(cudaMemcpyAsync(dst, src, bytes, kind, cs), "field copy");
+  g_spare_events.push_back(after);  // the wait is queued: the event may be recorded again
+  if (!ok) return false;
+  auto it = g_pending.find(field);
+  cudaEvent_t done = it != g_pending.end() ? it->second : take_event();
+  if (!done) return false;
+  g_pending[field] = done;
+  return cuda_ok(cudaEventRecord(done, cs), "copy done record");
+}
+
+}  // namespace
+
+bool await_copies(const void *const *ptrs, int n)
+{
+  std::lock_guard<std::mutex> lock(g_copy_mu);
+  if (g_pending.empty()) return true;
+  bool ok = true;
+  for (int q = 0; q < n; q++) {
+    auto it = g_pending.find(ptrs[q]);
+    if (it == g_pending.end()) continue;
+    ok = cuda_ok(cudaStreamWaitEvent(g_stream, it->second, 0), "wait for field copy") && ok;
+    g_spare_events.push_back(it->second);
+    g_pending.erase(it);
+  }
+  return ok;
+}
+
+bool await_all_copies()
+{
+  std::lock_guard<std::mutex> lock(g_copy_mu);
+  bool ok = true;
+  for (auto &kv : g_pending) {
+    ok = cuda_ok(cudaStreamWaitEvent(g_stream, kv.second, 0), "wait for field copy") && ok;
+    g_spare_events.push_back(kv.second);
+  }
+  g_pending.clear();
+  return ok;
+}
+
+bool await_fields(const Discretization *d)
+{
+  const void *f[8] = { d->u, d->v, d->w, d->p, d->rhs, d->f, d->g, d->h };
+  return await_copies(f, 8);
+}
+
 static double *field_ptr(const Discretization *d, int which)
 {
   switch (which) {
@@ -158,6 +253,8 @@ int nusifDownloadField(const Discretization *d, int which, double *host)
     return NUSIF_ERR_ARG;
   }
   size_t bytes = sizeof(double) * (size_t)st->dims.padded;
+  const void *fp = src;
+  if (!await_copies(&fp, 1)) return NUSIF_ERR_CUDA;
   if (!cuda_ok(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, g_stream),
           "download field"))
     return NUSIF_ERR_CUDA;
@@ -174,10 +271,61 @@ int nusifUploadField(Discretization *d, int which, const double *host)
     return NUSIF_ERR_ARG;
   }
   size_t bytes = sizeof(double) * (size_t)st->dims.padded;
+  const void *fp = dst;
+  if (!await_copies(&fp, 1)) return NUSIF_ERR_CUDA;
   if (!cuda_ok(cudaMemcpyAsync(dst, host, bytes, cudaMemcpyHostToDevice, g_stream),
           "upload field"))
     return NUSIF_ERR_CUDA;
   if (!cuda_ok(cudaStreamSynchronize(g_stream), "upload field sync")) return NUSIF_ERR_CUDA;
+  return NUSIF_OK;
+}
+
+int nusifUploadFieldAsync(Discretization *d, int which, const double *host)
+{
+  DiscState *st = disc_state(d);
+  double *dst = field_ptr(d, which);
+  if (!st || !dst || !host) {
+    fail(NUSIF_ERR_ARG, "nusifUploadFieldAsync: unknown discretization or field %d", which);
+    return NUSIF_ERR_ARG;
+  }
+  const size_t bytes = sizeof(double) * (size_t)st->dims.padded;
+  return queue_copy(dst, host, bytes, cudaMemcpyHostToDevice, dst) ? NUSIF_OK : NUSIF_ERR_CUDA;
+}
+
+int nusifDownloadFieldAsync(const Discretization *d, int which, double *host)
+{
+  DiscState *st = disc_state(d);
+  double *src = field_ptr(d, which);
+  if (!st || !src || !host) {
+    fail(NUSIF_ERR_ARG, "nusifDownloadFieldAsync: unknown discretization or field %d", which);
+    return NUSIF_ERR_ARG;
+  }
+  const size_t bytes = sizeof(double) * (size_t)st->dims.padded;
+  return queue_copy(host, src, bytes, cudaMemcpyDeviceToHost, src) ? NUSIF_OK : NUSIF_ERR_CUDA;
+}
+
+int nusifWaitCopies(void)
+{
+  std::vector<std::pair<int, cudaStream_t>> streams;
+  {
+    std::lock_guard<std::mutex> lock(g_copy_mu);
+    for (auto &kv : g_copy_streams) streams.push_back(kv);
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  bool ok = true;
+  for (auto &kv : streams) {
+    // a copy stream's work belongs to its device
+    if (!cuda_ok(cudaSetDevice(kv.first), "copy device") ||
+        !cuda_ok(cudaStreamSynchronize(kv.second), "field copies sync"))
+      ok = false;
+  }
+  cudaSetDevice(dev);
+  if (!ok) return NUSIF_ERR_CUDA;
+  // every queued copy has ended: nothing is pending any more
+  std::lock_guard<std::mutex> lock(g_copy_mu);
+  for (auto &kv : g_pending) g_spare_events.push_back(kv.second);
+  g_pending.clear();
   return NUSIF_OK;
 }
 

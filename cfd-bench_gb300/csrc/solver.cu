@@ -25,6 +25,7 @@
 #include <cstring>
 #include <unordered_map>
 
+#include "df32.cuh"
 #include "nusif_internal.h"
 #include "reduce.cuh"
 #include "solver_internal.h"
@@ -46,7 +47,16 @@ __device__ __forceinline__ bool solve_done(const SolveState *st)
 // Relax one colour (ACCUM: collect r^2; GHOSTS: write the six-face Neumann
 // ghosts of both cells of the pair after the update). When fold_n > 0 the
 // last block folds partials[0..fold_n) and advances the solve state.
-template <bool ACCUM, bool GHOSTS>
+//
+// DF: the residual r = rhs - lap in double-float arithmetic (df32.cuh: pairs
+// of FP32 numbers on the FP32 pipe, about 2^-47 of diag |p|) instead of ten
+// FP64 instructions per update, which bound the pass on GB300's FP64 pipe.
+// The update p - factor r adds the pair factor r to the exact p in two FP64
+// additions, so p itself is carried in binary64 as in the reference; r^2 is
+// accumulated as a pair and folded in FP64. At the benchmark size (diag
+// 3.9e5, eps 1e-6 on the RMS residual) the pair error of r is about 3e-3 of
+// eps: the stop test and the iteration count do not see it.
+template <bool ACCUM, bool GHOSTS, bool DF>
 __global__ void __launch_bounds__(kNT) k_sor_pass(SorArgs A, int colour, double *__restrict__ p,
     const double *__restrict__ rhs, SolveState *st, double *__restrict__ partials, int slot0,
     unsigned *ticket, int fold_n)
@@ -59,6 +69,15 @@ __global__ void __launch_bounds__(kNT) k_sor_pass(SorArgs A, int colour, double 
   const int k1 = min(k0 + A.kb - 1, g.kmax);
   const int sj = g.sj, sk = g.sk;
   double acc = 0.0;
+  df::f2 acc2{ 0.0f, 0.0f };
+  df::f2 ix{}, iy{}, iz{}, mdiag{}, mfac{};
+  if (DF) {
+    ix = df::from_double_rn(A.idx2);
+    iy = df::from_double_rn(A.idy2);
+    iz = df::from_double_rn(A.idz2);
+    mdiag = df::from_double_rn(-A.diag);
+    mfac = df::from_double_rn(-A.factor);
+  }
   if (j <= g.jmax) {
     for (int k = k0; k <= k1; k++) {
       const int i = 2 * t + 1 + ((1 + j + k + colour) & 1);
@@ -66,11 +85,23 @@ __global__ void __launch_bounds__(kNT) k_sor_pass(SorArgs A, int colour, double 
       if (i <= g.imax) {
         const int64_t c = row + i;
         const double pc = p[c];
-        const double lap = (p[c - 1] + p[c + 1]) * A.idx2 + (p[c - sj] + p[c + sj]) * A.idy2 +
-                           (p[c - sk] + p[c + sk]) * A.idz2 - A.diag * pc;
-        const double r = rhs[c] - lap;
-        p[c] = pc - A.factor * r;
-        if (ACCUM) acc += r * r;
+        if constexpr (DF) {
+          using namespace df;
+          f2 lap = mul(mdiag, split(pc));
+          lap = fma(add(split(p[c - 1]), split(p[c + 1])), ix, lap);
+          lap = fma(add(split(p[c - sj]), split(p[c + sj])), iy, lap);
+          lap = fma(add(split(p[c - sk]), split(p[c + sk])), iz, lap);
+          const f2 r = sub(split(rhs[c]), lap);
+          const f2 d = mul(mfac, r);
+          p[c] = (pc + widen(d.hi)) + widen(d.lo);
+          if (ACCUM) acc2 = add(acc2, mul(r, r));
+        } else {
+          const double lap = (p[c - 1] + p[c + 1]) * A.idx2 + (p[c - sj] + p[c + sj]) * A.idy2 +
+                             (p[c - sk] + p[c + sk]) * A.idz2 - A.diag * pc;
+          const double r = rhs[c] - lap;
+          p[c] = pc - A.factor * r;
+          if (ACCUM) acc += r * r;
+        }
       }
       if (GHOSTS) {
 #pragma unroll
@@ -92,6 +123,7 @@ __global__ void __launch_bounds__(kNT) k_sor_pass(SorArgs A, int colour, double 
     }
   }
   if (!ACCUM) return;
+  if (DF) acc = df::to_double(acc2);
   __shared__ double sm[kNT / 32];
   acc = block_reduce_sum<kNT>(acc, sm);
   __shared__ bool last;
@@ -213,31 +245,38 @@ int sor_blocks(const SorArgs &A)
   return (int)(gr.x * gr.y * gr.z);
 }
 
-bool launch_rb_iteration(const SorArgs &A, double *p, const double *rhs, SolveState *st,
+template <bool DF>
+bool rb_iteration(const SorArgs &A, double *p, const double *rhs, SolveState *st,
     ReduceScratch &red)
 {
   const dim3 grid = sor_grid(A), blk(kBX, kBY);
   const int nb = sor_blocks(A);
-  k_sor_pass<true, false><<<grid, blk, 0, stream()>>>(A, 1, p, rhs, st, red.partials, 0,
+  k_sor_pass<true, false, DF><<<grid, blk, 0, stream()>>>(A, 1, p, rhs, st, red.partials, 0,
       red.ticket, 0);
   if (!launched("k_sor_pass(odd)")) return false;
-  k_sor_pass<true, true><<<grid, blk, 0, stream()>>>(A, 0, p, rhs, st, red.partials, nb,
+  k_sor_pass<true, true, DF><<<grid, blk, 0, stream()>>>(A, 0, p, rhs, st, red.partials, nb,
       red.ticket, 2 * nb);
   return launched("k_sor_pass(even)");
+}
+
+bool launch_rb_iteration(const SorArgs &A, double *p, const double *rhs, SolveState *st,
+    ReduceScratch &red, bool df)
+{
+  return df ? rb_iteration<true>(A, p, rhs, st, red) : rb_iteration<false>(A, p, rhs, st, red);
 }
 
 bool launch_sor_sweep(const SorArgs &A, double *p, const double *rhs, bool ghosts)
 {
   const dim3 grid = sor_grid(A), blk(kBX, kBY);
-  k_sor_pass<false, false><<<grid, blk, 0, stream()>>>(A, 1, p, rhs, nullptr, nullptr, 0,
+  k_sor_pass<false, false, false><<<grid, blk, 0, stream()>>>(A, 1, p, rhs, nullptr, nullptr, 0,
       nullptr, 0);
   if (!launched("k_sor_pass(odd)")) return false;
   if (ghosts)
-    k_sor_pass<false, true><<<grid, blk, 0, stream()>>>(A, 0, p, rhs, nullptr, nullptr, 0,
-        nullptr, 0);
+    k_sor_pass<false, true, false><<<grid, blk, 0, stream()>>>(A, 0, p, rhs, nullptr, nullptr,
+        0, nullptr, 0);
   else
-    k_sor_pass<false, false><<<grid, blk, 0, stream()>>>(A, 0, p, rhs, nullptr, nullptr, 0,
-        nullptr, 0);
+    k_sor_pass<false, false, false><<<grid, blk, 0, stream()>>>(A, 0, p, rhs, nullptr, nullptr,
+        0, nullptr, 0);
   return launched("k_sor_pass(even)");
 }
 
@@ -322,7 +361,8 @@ static double solve_rb(Solver *s, SolverState *ss, double *p, const double *rhs)
   if (chunk > s->itermax) chunk = s->itermax;
   while (!h->done) {
     for (int q = 0; q < chunk; q++)
-      if (!launch_rb_iteration(A, p, rhs, ss->d_state, ss->red)) return NAN;
+      if (!launch_rb_iteration(A, p, rhs, ss->d_state, ss->red, !ss->ext.arith_fp64))
+        return NAN;
     if (!cuda_ok(cudaMemcpyAsync(h, ss->d_state, sizeof(SolveState), cudaMemcpyDeviceToHost,
                      stream()),
             "solve state download"))
@@ -432,6 +472,8 @@ double solve(Solver *s, double *p, const double *rhs)
     fail(NUSIF_ERR_STATE, "solve: solver not initialised by initSolver");
     return NAN;
   }
+  const void *fields[2] = { p, rhs };
+  if (!await_copies(fields, 2)) return NAN;
   switch (ss->kind) {
   case SOLVER_RB: return solve_rb(s, ss, p, rhs);
   case SOLVER_MG_REF: return solve_mg_ref(s, ss, p, rhs);

@@ -26,8 +26,9 @@ struct SorArgs {
 SorArgs make_sor_args(const Dims &g, double dx, double dy, double dz, double omega);
 dim3 sor_grid(const SorArgs &A);
 int sor_blocks(const SorArgs &A);
+// df: the SOR residual in double-float arithmetic (key arith df32)
 bool launch_rb_iteration(const SorArgs &A, double *p, const double *rhs, SolveState *st,
-    ReduceScratch &red);
+    ReduceScratch &red, bool df = false);
 bool launch_sor_sweep(const SorArgs &A, double *p, const double *rhs, bool ghosts);
 bool launch_residual_ref(const SorArgs &A, const double *p, const double *rhs, SolveState *st,
     ReduceScratch &red);

@@ -90,6 +90,9 @@ SIGNATURES = [
     ("nusifGetStream", C.c_void_p, []),
     ("nusifDownloadField", C.c_int, [C.POINTER(Discretization), C.c_int, c_double_p]),
     ("nusifUploadField", C.c_int, [C.POINTER(Discretization), C.c_int, c_double_p]),
+    ("nusifUploadFieldAsync", C.c_int, [C.POINTER(Discretization), C.c_int, c_double_p]),
+    ("nusifDownloadFieldAsync", C.c_int, [C.POINTER(Discretization), C.c_int, c_double_p]),
+    ("nusifWaitCopies", C.c_int, []),
     ("nusifSolverIterations", C.c_int, [C.POINTER(Solver)]),
     ("nusifParameterSet", C.c_int, [C.POINTER(Parameter), C.c_char_p, C.c_char_p]),
     ("nusifFreeDiscretization", None, [C.POINTER(Discretization)]),

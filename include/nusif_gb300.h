@@ -161,6 +161,20 @@ NUSIF_API void *nusifGetStream(void);
 /* copies between a host array of (imax+2)(jmax+2)(kmax+2) doubles and a field */
 NUSIF_API int nusifDownloadField(const Discretization *d, int which, double *host);
 NUSIF_API int nusifUploadField(Discretization *d, int which, const double *host);
+/* The same copies queued asynchronously (no counterpart in the reference,
+ * whose fields live in host memory): each runs on a copy stream of the
+ * library after the work already queued on the launch stream, and the first
+ * later call taking the Discretization (or solve() with the field as p or
+ * rhs) waits for it on the device, not on the host -- so an upload of p
+ * overlaps computeTimestep .. computeRHS, which do not read p. The host array
+ * must stay untouched, and a downloaded one unread, until nusifWaitCopies()
+ * returns; pinned host memory makes the copies asynchronous. Entry points
+ * that take bare device pointers and the batch API do not wait per field:
+ * call nusifWaitCopies() before them (nusifBatchStep does). */
+NUSIF_API int nusifUploadFieldAsync(Discretization *d, int which, const double *host);
+NUSIF_API int nusifDownloadFieldAsync(const Discretization *d, int which, double *host);
+/* blocks until every queued asynchronous field copy has finished */
+NUSIF_API int nusifWaitCopies(void);
 /* iteration count of the last solve() (the reference prints it under VERBOSE,
  * solver-rb.c:163-166); V-cycles for mg and mg-mixed */
 NUSIF_API int nusifSolverIterations(const Solver *s);
@@ -170,8 +184,9 @@ NUSIF_API int nusifParameterSet(Parameter *param, const char *key, const char *v
 NUSIF_API void nusifFreeDiscretization(Discretization *d);
 NUSIF_API void nusifFreeSolver(Solver *s);
 /* Red-black SOR solve that allocates no memory. No counterpart in the
- * reference. Same result as solve() with the rb solver on the same p, rhs
- * (device arrays in the padded layout) and parameters, for callers that cannot
+ * reference. Same result as solve() with the rb solver and the key arith fp64
+ * (the residual in FP64 instructions, as here) on the same p, rhs (device
+ * arrays in the padded layout) and parameters, for callers that cannot
  * call cudaMalloc (hosts that hand out only pre-sized device buffers, runtimes
  * that reserve all device memory at start-up). Its scratch is a fixed
  * 256.5 KiB __device__ array of the library: grids needing more than 32768

@@ -57,12 +57,14 @@ def test_operators_at_256_match_oracle(nusif_lib, oracle_mod, arith):
             assert rel_err(sim.field(name), ref) < 1e-13, name
 
 
-def test_red_black_at_256_matches_oracle(nusif_lib, oracle_mod):
-    """Twelve red-black SOR iterations at 256^3: the reference's carried
-    residual and the pressure agree with the oracle."""
+@pytest.mark.parametrize("arith", ["df32", "fp64"])
+def test_red_black_at_256_matches_oracle(nusif_lib, oracle_mod, arith):
+    """Twelve red-black SOR iterations at 256^3 (residual in FP32 pairs and in
+    FP64 instructions): the reference's carried residual and the pressure
+    agree with the oracle."""
     from nusif import Simulation
     o = oracle_mod
-    v = _vals(itermax=12, eps=1e-30)
+    v = _vals(itermax=12, eps=1e-30, arith=arith)
     rng = np.random.default_rng(2562)
     with Simulation(v) as sim:
         g = o.grid(N, N, N, v["xlength"], v["ylength"], v["zlength"])

@@ -92,6 +92,68 @@ def test_mg_mixed_matches_oracle(nusif_lib, oracle_mod, dims):
         assert true_rel == pytest.approx(rel, rel=1e-3)
 
 
+@pytest.mark.parametrize("dims", [(64, 32, 16), (33, 17, 9), (40, 24, 20)])
+def test_mixed_residual_in_pairs_matches_fp64(nusif_lib, oracle_mod, dims):
+    """The mixed solver's fine residual in FP32 pairs (key arith df32, the
+    default) against the FP64-instruction kernel (arith fp64). rtol 1e30
+    stops every solve after its first residual, so solve() returns ||b - A p||
+    / ||b|| of the given p: a random p (no cancellation: 1e-12 relative) and
+    the oracle's FP64 solution to 1e-9, where b - A p cancels down to 1e-9 of
+    ||b|| and the pair arithmetic's error (a few 2^-47 diag |p|) must stay
+    below 2% of the norm, 1e-11 of ||b|| -- three orders under the rtol of
+    every benchmark case (1e-6, 1e-8)."""
+    o = oracle_mod
+    rng = np.random.default_rng(29)
+    rhs = None
+    rels = {}
+    for arith in ("df32", "fp64"):
+        with _sim(dims, "mg-mixed", 1e30, arith=arith) as sim:
+            g = sim.d.grid
+            if rhs is None:
+                rhs = rng.standard_normal(sim.padded_shape)
+                p_rand = rng.standard_normal(sim.padded_shape)
+                og = o.grid(*dims, g.xlength, g.ylength, g.zlength)
+                p_conv = np.zeros(sim.padded_shape)
+                cyc, rel_c = o.op_mg_solve(og, "mg", p_conv, rhs, rtol=1e-9, maxcycles=400)
+                assert cyc < 400 and rel_c <= 1e-9
+            sim.set_field("rhs", rhs)
+            out = []
+            for p in (p_rand, p_conv):
+                sim.set_field("p", p)
+                out.append(sim.solve())
+                # one residual, no correction (the solve still writes p's Neumann ghosts)
+                np.testing.assert_array_equal(sim.field("p")[1:-1, 1:-1, 1:-1],
+                                              p[1:-1, 1:-1, 1:-1])
+            rels[arith] = out
+    assert rels["df32"][0] == pytest.approx(rels["fp64"][0], rel=1e-12)
+    assert rels["fp64"][1] == pytest.approx(rel_c, rel=1e-3)
+    assert rels["df32"][1] == pytest.approx(rels["fp64"][1], rel=2e-2)
+
+
+@pytest.mark.parametrize("dims", [(32, 32, 32), (33, 17, 9)])
+def test_mixed_solve_in_pairs_matches_fp64_residual(nusif_lib, dims):
+    """A whole mixed solve with the residual in pairs and in FP64 instructions:
+    both end below rtol, with cycle counts within one (a residual within 2^-47
+    of a FP32 rounding boundary can round its FP32 copy the other way) and
+    pressures within 5e-8 of their magnitude (both are rtol = 1e-8 solutions)."""
+    rng = np.random.default_rng(31)
+    p0 = rhs = None
+    res = {}
+    for arith in ("df32", "fp64"):
+        with _sim(dims, "mg-mixed", 1e-8, mg_cycles=60, arith=arith) as sim:
+            if p0 is None:
+                p0 = rng.standard_normal(sim.padded_shape)
+                rhs = rng.standard_normal(sim.padded_shape)
+            sim.set_field("p", p0)
+            sim.set_field("rhs", rhs)
+            rel = sim.solve()
+            res[arith] = (rel, sim.iterations, _interior_demeaned(sim.field("p")))
+    (r1, c1, a), (r2, c2, b) = res["df32"], res["fp64"]
+    assert r1 <= 1e-8 and r2 <= 1e-8
+    assert abs(c1 - c2) <= 1
+    assert np.max(np.abs(a - b)) <= 5e-8 * np.max(np.abs(b))
+
+
 @pytest.mark.parametrize("solver", ["mg", "mg-mixed"])
 def test_mg_zero_rhs_returns_at_once(nusif_lib, solver):
     with _sim((16, 16, 16), solver, 1e-6) as sim:

@@ -148,10 +148,14 @@ def test_operators_match_oracle_random(nusif_lib, oracle_mod, dims, bci, arith):
             np.testing.assert_array_equal(sim.field(f), inputs[f])
 
 
+@pytest.mark.parametrize("arith", ["df32", "fp64"])
 @pytest.mark.parametrize("dims", [(8, 8, 8), (17, 9, 13), (33, 33, 33), (2, 5, 3)])
-def test_rb_solve_matches_oracle(nusif_lib, oracle_mod, dims):
+def test_rb_solve_matches_oracle(nusif_lib, oracle_mod, dims, arith):
+    """Red-black SOR with its residual in FP32 pairs (arith df32, the default)
+    and in FP64 instructions: the same iteration count as the oracle, the
+    carried residual and the pressure to 1e-11."""
     o = oracle_mod
-    v = _case(dims, BCS[0], itermax=60, eps=1e-9)
+    v = _case(dims, BCS[0], itermax=60, eps=1e-9, arith=arith)
     rng = np.random.default_rng(7)
     with _sim(v) as sim:
         g = o.grid(*dims, v["xlength"], v["ylength"], v["zlength"])
@@ -220,3 +224,43 @@ def test_field_copies_pinned_pageable_unaligned(nusif_lib, dims):
             assert nusif_lib.nusifDownloadField(C.byref(sim.d), idx[name], ptr) == 0
             abi.check(nusif_lib)
             np.testing.assert_array_equal(buf, a)
+
+
+def test_queued_field_copies_match_synchronous_copies(nusif_lib):
+    """Three time steps of a 24^3 cavity, each step's u, v, w, p uploaded from
+    and downloaded to pinned host arrays: with the queued copies
+    (nusifUploadFieldAsync / nusifDownloadFieldAsync / nusifWaitCopies, the
+    library's kernels waiting on the device for the fields they use) the host
+    arrays end bit-identical to the same loop with the synchronous copies."""
+    import ctypes as C
+
+    import torch
+
+    from nusif import Simulation, abi
+    from nusif.params import cavity
+    vals = cavity(24, te=1e9, solver="mg-mixed", rtol=1e-8, mg_guess="quadratic")
+    idx = abi.FIELD_INDEX
+    out = {}
+    for mode in ("sync", "queued"):
+        with Simulation(vals) as sim:
+            n = int(np.prod(sim.padded_shape))
+            host = {f: torch.zeros(n, dtype=torch.float64, pin_memory=True) for f in "uvwp"}
+            ptrs = {f: C.cast(host[f].data_ptr(), abi.c_double_p) for f in "uvwp"}
+            for _ in range(3):
+                for f in "uvwp":
+                    fn = nusif_lib.nusifUploadField if mode == "sync" else \
+                        nusif_lib.nusifUploadFieldAsync
+                    assert fn(C.byref(sim.d), idx[f], ptrs[f]) == 0
+                sim.step()
+                for f in "uvwp":
+                    fn = nusif_lib.nusifDownloadField if mode == "sync" else \
+                        nusif_lib.nusifDownloadFieldAsync
+                    assert fn(C.byref(sim.d), idx[f], ptrs[f]) == 0
+                assert nusif_lib.nusifWaitCopies() == 0
+                abi.check(nusif_lib)
+            out[mode] = {f: host[f].numpy().copy() for f in "uvwp"}
+            for f in "uvwp":  # the device fields are the downloaded ones
+                np.testing.assert_array_equal(sim.field(f).reshape(-1), out[mode][f])
+    for f in "uvwp":
+        assert np.any(out["sync"][f] != 0.0) or f != "u"
+        np.testing.assert_array_equal(out["queued"][f], out["sync"][f])
