@@ -25,7 +25,9 @@
 // state once per chunk.
 #include <algorithm>
 #include <array>
+#include <climits>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -567,8 +569,14 @@ __global__ void __launch_bounds__(kNT) k_mx_residual(View<double> f, float *r32,
 // Indices outside the grid are clamped to it, which is the Neumann rule
 // itself (a missing neighbour is the cell). Each value is split into its pair
 // once per block (ring cells once more by the neighbouring block).
-__global__ void __launch_bounds__(kNT) k_mx_residual_df(View<double> f, float *r32, MgState *st,
-    double *partials, unsigned *ticket, int count_cycles, float *e_zero, int kb)
+// the operator's constants as pairs, formed on the host (GB300 runs double
+// <-> float conversions on its FP64 pipe)
+struct DfStencil {
+  df::f2 ex, ey, ez, mdiag;
+};
+
+__global__ void __launch_bounds__(kNT, 4) k_mx_residual_df(View<double> f, DfStencil cs, float *r32,
+    MgState *st, double *partials, unsigned *ticket, int count_cycles, float *e_zero, int kb)
 {
   using namespace df;
   if (solve_finished(st)) return;
@@ -597,8 +605,7 @@ __global__ void __launch_bounds__(kNT) k_mx_residual_df(View<double> f, float *r
   const int coff = f.off + j * f.sy + i;
   double acc_d = 0.0;
   if (k0 < k1) {
-    const f2 ex = from_double_rn(f.ex), ey = from_double_rn(f.ey), ez = from_double_rn(f.ez);
-    const f2 mdiag = from_double_rn(-f.diag), sh = split(st->shift);
+    const f2 ex = cs.ex, ey = cs.ey, ez = cs.ez, mdiag = cs.mdiag, sh = split(st->shift);
     const auto plane = [&](int k) { return (int64_t)min(max(k, 0), f.nz - 1) * f.sz; };
     f2 zb = split(x[plane(k0 - 1) + coff]);
     f2 zc = split(x[plane(k0) + coff]);
@@ -1657,16 +1664,26 @@ int flat_blocks(int64_t n)
   return (int)(b < cap ? (b > 0 ? b : 1) : cap);
 }
 
-// grid of k_mx_residual_df: 32 x 8 column tiles, the planes split into chunks
-// so that about 8 blocks per SM run (the kernel's partials fit mx_df_blocks)
+// grid of k_mx_residual_df: 32 x 8 column tiles, the planes split into
+// chunks of kb; kb minimises (waves of resident blocks) x (kb + 2 planes read
+// per chunk), four blocks of the kernel being resident per SM (the kernel's
+// partials fit mx_df_blocks)
 dim3 mx_df_grid(int nx, int ny, int nz, int *kb)
 {
-  const int gx = (nx + kBX - 1) / kBX, gy = (ny + kBY - 1) / kBY;
-  int gz = (int)std::max<int64_t>(1, 8 * (int64_t)sm_count_mg() / ((int64_t)gx * gy));
-  gz = std::min(gz, nz);
-  *kb = (nz + gz - 1) / gz;
-  gz = (nz + *kb - 1) / *kb;
-  return dim3(gx, gy, gz);
+  const int64_t gx = (nx + kBX - 1) / kBX, gy = (ny + kBY - 1) / kBY;
+  const int64_t wave = 4 * (int64_t)sm_count_mg();
+  int best = nz;
+  int64_t best_cost = INT64_MAX;
+  for (int c = 4; c <= 64; c++) {
+    const int64_t blocks = gx * gy * ((nz + c - 1) / c);
+    const int64_t cost = ((blocks + wave - 1) / wave) * (c + 2);
+    if (cost < best_cost) {
+      best_cost = cost;
+      best = c;
+    }
+  }
+  *kb = std::min(best, nz);
+  return dim3((unsigned)gx, (unsigned)gy, (unsigned)((nz + *kb - 1) / *kb));
 }
 
 int mx_df_blocks(int nx, int ny, int nz)
@@ -1683,8 +1700,10 @@ bool mx_residual(MgHierarchy *H, const View<double> &v0, MgState *st, int count_
   if (H->mx_df) {
     int kb;
     const dim3 grid = mx_df_grid(v0.nx, v0.ny, v0.nz, &kb);
-    k_mx_residual_df<<<grid, dim3(kBX, kBY), 0, stream()>>>(v0, H->b32[0], st, H->red.partials,
-        H->red.ticket, count_cycles, e_zero, kb);
+    const DfStencil cs{ df::from_double_rn(v0.ex), df::from_double_rn(v0.ey),
+                        df::from_double_rn(v0.ez), df::from_double_rn(-v0.diag) };
+    k_mx_residual_df<<<grid, dim3(kBX, kBY), 0, stream()>>>(v0, cs, H->b32[0], st,
+        H->red.partials, H->red.ticket, count_cycles, e_zero, kb);
     return launched("k_mx_residual_df");
   }
   const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;

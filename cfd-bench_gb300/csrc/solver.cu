@@ -70,35 +70,51 @@ __global__ void __launch_bounds__(kNT) k_sor_pass(SorArgs A, int colour, double 
   const int sj = g.sj, sk = g.sk;
   double acc = 0.0;
   df::f2 acc2{ 0.0f, 0.0f };
-  df::f2 ix{}, iy{}, iz{}, mdiag{}, mfac{};
-  if (DF) {
-    ix = df::from_double_rn(A.idx2);
-    iy = df::from_double_rn(A.idy2);
-    iz = df::from_double_rn(A.idz2);
-    mdiag = df::from_double_rn(-A.diag);
-    mfac = df::from_double_rn(-A.factor);
-  }
-  if (j <= g.jmax) {
+  // The eight values a plane's update reads, loaded one plane ahead: none of
+  // them is written by this pass before it is used (they are the other colour,
+  // or this thread's own cell of the next plane, or ghosts that only their
+  // own boundary cell reads), so the loads of plane k + 1 overlap the
+  // arithmetic and the store of plane k.
+  struct Stencil {
+    double c, w, e, s, n, b, t, r;
+  };
+  const auto load = [&](int k, Stencil &v) {
+    const int i = 2 * t + 1 + ((1 + j + k + colour) & 1);
+    if (i > g.imax) return;
+    const int64_t c = (int64_t)k * sk + (int64_t)j * sj + i;
+    v.c = p[c];
+    v.w = p[c - 1];
+    v.e = p[c + 1];
+    v.s = p[c - sj];
+    v.n = p[c + sj];
+    v.b = p[c - sk];
+    v.t = p[c + sk];
+    v.r = rhs[c];
+  };
+  if (j <= g.jmax && k0 <= k1) {
+    Stencil cur{}, nxt{};
+    load(k0, cur);
     for (int k = k0; k <= k1; k++) {
+      if (k < k1) load(k + 1, nxt);
       const int i = 2 * t + 1 + ((1 + j + k + colour) & 1);
       const int64_t row = (int64_t)k * sk + (int64_t)j * sj;
       if (i <= g.imax) {
         const int64_t c = row + i;
-        const double pc = p[c];
+        const double pc = cur.c;
         if constexpr (DF) {
           using namespace df;
-          f2 lap = mul(mdiag, split(pc));
-          lap = fma(add(split(p[c - 1]), split(p[c + 1])), ix, lap);
-          lap = fma(add(split(p[c - sj]), split(p[c + sj])), iy, lap);
-          lap = fma(add(split(p[c - sk]), split(p[c + sk])), iz, lap);
-          const f2 r = sub(split(rhs[c]), lap);
-          const f2 d = mul(mfac, r);
+          f2 lap = mul(A.pmdiag, split(pc));
+          lap = fma(add(split(cur.w), split(cur.e)), A.pidx2, lap);
+          lap = fma(add(split(cur.s), split(cur.n)), A.pidy2, lap);
+          lap = fma(add(split(cur.b), split(cur.t)), A.pidz2, lap);
+          const f2 r = sub(split(cur.r), lap);
+          const f2 d = mul(A.pmfactor, r);
           p[c] = (pc + widen(d.hi)) + widen(d.lo);
           if (ACCUM) acc2 = add(acc2, mul(r, r));
         } else {
-          const double lap = (p[c - 1] + p[c + 1]) * A.idx2 + (p[c - sj] + p[c + sj]) * A.idy2 +
-                             (p[c - sk] + p[c + sk]) * A.idz2 - A.diag * pc;
-          const double r = rhs[c] - lap;
+          const double lap = (cur.w + cur.e) * A.idx2 + (cur.s + cur.n) * A.idy2 +
+                             (cur.b + cur.t) * A.idz2 - A.diag * pc;
+          const double r = cur.r - lap;
           p[c] = pc - A.factor * r;
           if (ACCUM) acc += r * r;
         }
@@ -120,6 +136,7 @@ __global__ void __launch_bounds__(kNT) k_sor_pass(SorArgs A, int colour, double 
           if (k == g.kmax) p[c + sk] = val;
         }
       }
+      cur = nxt;
     }
   }
   if (!ACCUM) return;
@@ -220,6 +237,11 @@ SorArgs make_sor_args(const Dims &g, double dx, double dy, double dz, double ome
   A.diag = 2.0 * (A.idx2 + A.idy2 + A.idz2);
   // src/solver-rb.c:46-47
   A.factor = omega * 0.5 * (dx2 * dy2 * dz2) / (dy2 * dz2 + dx2 * dz2 + dx2 * dy2);
+  A.pidx2 = df::from_double_rn(A.idx2);
+  A.pidy2 = df::from_double_rn(A.idy2);
+  A.pidz2 = df::from_double_rn(A.idz2);
+  A.pmdiag = df::from_double_rn(-A.diag);
+  A.pmfactor = df::from_double_rn(-A.factor);
   // planes per block: the largest power of two <= 16 that still gives >= 4 waves of blocks
   int sms = 152;
   int dev = 0;

@@ -1,6 +1,7 @@
 // Solver-side internal declarations (not part of the C ABI).
 #pragma once
 
+#include "df32.cuh"
 #include "nusif_internal.h"
 
 namespace nusif {
@@ -20,6 +21,9 @@ struct SolveState {
 struct SorArgs {
   Dims g;
   double idx2, idy2, idz2, diag, factor;
+  // the same constants as pairs of FP32 numbers (df32.cuh), formed on the
+  // host: GB300 runs double <-> float conversions on its FP64 pipe
+  df::f2 pidx2, pidy2, pidz2, pmdiag, pmfactor;
   int kb;  // k planes per block
 };
 

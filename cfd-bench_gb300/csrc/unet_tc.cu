@@ -1,22 +1,24 @@
 // 3x3x3 convolutions of the U-Net on the 5th-generation tensor cores
 // (tcgen05.mma, accumulators in tensor memory, operands staged by TMA).
 //
-// Implicit GEMM: M = 128 consecutive cells of the channels-last volume (one
-// tile; a tile covers whole x-rows, or one 128-cell piece of a longer row, so
-// it lies in one z-plane), N = output channels, K = 27 taps x input channels.
-// A tap contributes one K block: the tile's cells shifted by the tap, every
-// input channel, and the tap's weights [N][K]. Per tap and source one elected
-// thread issues a TMA tiled load of the shifted box (all C channels x the
-// tile's x/y extent: one C x 2-byte row per cell) - out-of-range x and y read
-// as zero, which is the convolution's zero padding; a tap whose z leaves the
-// volume is skipped for the whole tile - and one of the tap's weight rows for
-// that source's channels. The loads use the swizzle whose span is the row
-// (32, 64 or 128 bytes for 16, 32 or 64 channels), which is also the
-// canonical K-major operand layout of the tensor cores for that span (8-row
-// atoms; stride offset 8 rows). Another thread issues one tcgen05.mma
+// Implicit GEMM: M = 128 cells of one z-plane (a tile of 16 x-columns by 8
+// y-rows), N = output channels, K = 27 taps x input channels. The tile's rows
+// are ordered x-major over 8-cell y-columns, so each x-column is one 8-row
+// swizzle atom of the K-major operand layout. A stage carries one (dz, dy)
+// row of taps: per source one TMA tiled load of the 18 x-columns x 8 y-rows
+// around the tile (x from x0 - 1 to x0 + 16, through a tensor map whose
+// second dimension is y and third x, so the box lands column by column), and
+// one load of the row's three tap weights [3][N][C]. The three dx taps of the
+// row read that one box through descriptors offset by 0, 1 and 2 atoms, so a
+// cell row is loaded once per (dz, dy) instead of once per tap. Out-of-range
+// x and y read as zero, which is the convolution's zero padding; a dz plane
+// outside the volume is skipped for the whole tile. The swizzle is the one
+// whose span is the cell row (32, 64 or 128 bytes for 16, 32 or 64 channels),
+// which is also the canonical K-major operand layout for that span (8-row
+// atoms; stride offset 8 rows). The MMA thread issues one tcgen05.mma
 // (kind::f16, BF16 x BF16 -> FP32, M = 128, N = channels out, K = 16) per 16
-// input channels, the descriptors advanced by 32 bytes along the swizzled row,
-// and commits the stage back to the producer. Accumulators are
+// input channels per tap, the descriptors advanced by 32 bytes along the
+// swizzled row, and commits the stage back to the producer. Accumulators are
 // double-buffered in tensor memory, so four epilogue warps drain one tile
 // (tcgen05.ld, bias, ReLU, BF16 or FP32 rows) while the next tile's products
 // accumulate.
@@ -40,6 +42,8 @@ namespace nusif {
 namespace {
 
 constexpr int kTileM = 128;
+constexpr int kTileX = 16, kTileY = 8;  // tile: 16 x-columns of 8 y-cells
+constexpr int kBoxX = kTileX + 2;       // loaded columns: the tile and one on each side
 constexpr int kThreads = 192;  // warp 0 TMA producer, warp 1 MMA issuer, warps 2-5 epilogue
 constexpr int kMaxStages = 16;
 constexpr uint32_t kBarBytes = 512;  // barrier and flag region at the start of shared memory
@@ -48,12 +52,12 @@ constexpr uint64_t kWaitNs = 1000000000ull;  // bound of every mbarrier wait
 struct TcParams {
   int N;                 // output channels (MMA N)
   int C0, C1;            // channels of source 0 and source 1 (0: none): 16, 32 or 64
-  uint32_t a_off[2], b_off[2];  // offsets of each source's cell rows and weight rows in a tap block
-  uint32_t tap_bytes;    // one tap's block of a stage
-  int taps;              // taps per stage: 1, 3 (one dz, dy row) or 9 (one dz plane)
+  uint32_t a_off[2], b_off[2];  // offsets of each source's cell box and tap weights in a stage
+  uint32_t atom[2];      // bytes of one x-column (8 cell rows) of each source
+  uint32_t wtap[2];      // bytes of one tap's weights [N][C] of each source
   uint32_t stage_bytes, tx_bytes;
   int X, Y, Z, B;        // volume
-  int xbox, ybox;        // tile extent in x and y (xbox * ybox = 128)
+  int tx, ty;            // tiles per row (X / 16) and per column (Y / 8)
   int ntiles;
   int stages;
   int tmem_cols;         // allocated tensor-memory columns (>= 2 N, power of two)
@@ -216,12 +220,11 @@ struct Tile {
 
 __device__ __forceinline__ Tile tile_of(const TcParams &P, int t)
 {
-  const int64_t cell0 = (int64_t)t * kTileM;
   Tile r;
-  r.x0 = (int)(cell0 % P.X);
-  const int64_t row = cell0 / P.X;
-  r.y0 = (int)(row % P.Y);
-  r.zb = (int)(row / P.Y);
+  r.x0 = (t % P.tx) * kTileX;
+  const int rest = t / P.tx;
+  r.y0 = (rest % P.ty) * kTileY;
+  r.zb = rest / P.ty;
   r.z = r.zb % P.Z;
   return r;
 }
@@ -281,9 +284,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
     bool ok = true;
     for (int t = blockIdx.x; ok && t < P.ntiles; t += gridDim.x) {
       const Tile tl = tile_of(P, t);
-      for (int tap0 = 0; tap0 < 27; tap0 += P.taps) {
-        const int dz0 = tap0 / 9 - 1;  // a stage's taps share dz
-        if (tl.z + dz0 < 0 || tl.z + dz0 >= P.Z) continue;
+      for (int row = 0; row < 9; row++) {  // (dz, dy) rows of taps; a stage per row
+        const int dz = row / 3 - 1, dy = row % 3 - 1;
+        if (tl.z + dz < 0 || tl.z + dz >= P.Z) continue;
         if (!mbar_wait(smem_u32(empty + stage), phase ^ 1u, abort_flag, P.err)) {
           ok = false;
           break;
@@ -292,16 +295,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
         const uint32_t fb = smem_u32(full + stage);
         const uint32_t sa = smem_u32(stage_base + (size_t)stage * stage_bytes);
         mbar_expect_tx(fb, P.tx_bytes);
-        for (int q = 0; q < P.taps; q++) {
-          const int tap = tap0 + q;
-          const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-          const uint32_t tb = sa + (uint32_t)q * P.tap_bytes;
-          tma_load_4d(tb + P.a_off[0], &tm_a0, fb, 0, tl.x0 + dx, tl.y0 + dy, tl.zb + dz);
-          tma_load_3d(tb + P.b_off[0], &tm_w0, fb, 0, 0, tap);
-          if (P.C1 > 0) {
-            tma_load_4d(tb + P.a_off[1], &tm_a1, fb, 0, tl.x0 + dx, tl.y0 + dy, tl.zb + dz);
-            tma_load_3d(tb + P.b_off[1], &tm_w1, fb, P.C0, 0, tap);
-          }
+        // the box (C, 8 y, 18 x) at y0 + dy, x0 - 1; the row's three taps' weights
+        tma_load_4d(sa + P.a_off[0], &tm_a0, fb, 0, tl.y0 + dy, tl.x0 - 1, tl.zb + dz);
+        tma_load_3d(sa + P.b_off[0], &tm_w0, fb, 0, 0, 3 * row);
+        if (P.C1 > 0) {
+          tma_load_4d(sa + P.a_off[1], &tm_a1, fb, 0, tl.y0 + dy, tl.x0 - 1, tl.zb + dz);
+          tma_load_3d(sa + P.b_off[1], &tm_w1, fb, P.C0, 0, 3 * row);
         }
         armed[stage] = true;
         armed_par[stage] = phase;
@@ -331,23 +330,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
       fence_after();
       const uint32_t d = tmem + (uint32_t)(acc * (P.tmem_cols / 2));
       uint32_t accumulate = 0;
-      for (int tap0 = 0; tap0 < 27; tap0 += P.taps) {
-        const int dz0 = tap0 / 9 - 1;
-        if (tl.z + dz0 < 0 || tl.z + dz0 >= P.Z) continue;
+      for (int row = 0; row < 9; row++) {
+        const int dz = row / 3 - 1;
+        if (tl.z + dz < 0 || tl.z + dz >= P.Z) continue;
         if (!mbar_wait(smem_u32(full + stage), phase, abort_flag, P.err)) {
           ok = false;
           break;
         }
         fence_after();
         const uint32_t sa = smem_u32(stage_base + (size_t)stage * stage_bytes);
-        for (int q = 0; q < P.taps; q++) {
-          const uint32_t tb = sa + (uint32_t)q * P.tap_bytes;
+        for (int q = 0; q < 3; q++) {  // dx = q - 1: the box read q atoms in
           for (int src = 0; src < 2; src++) {
             const int cs = src == 0 ? P.C0 : P.C1;
-            const uint32_t row = 2u * (uint32_t)cs;
+            const uint32_t rb = 2u * (uint32_t)cs;
             for (int j = 0; j < cs / 16; j++) {
-              const uint64_t adesc = smem_desc_sw(tb + P.a_off[src] + 32u * j, row);
-              const uint64_t bdesc = smem_desc_sw(tb + P.b_off[src] + 32u * j, row);
+              const uint64_t adesc =
+                  smem_desc_sw(sa + P.a_off[src] + (uint32_t)q * P.atom[src] + 32u * j, rb);
+              const uint64_t bdesc =
+                  smem_desc_sw(sa + P.b_off[src] + (uint32_t)q * P.wtap[src] + 32u * j, rb);
               mma_f16(d, adesc, bdesc, P.idesc, accumulate);
               accumulate = 1;
               issued = true;
@@ -394,7 +394,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
       tmem_wait_ld();
       fence_before();
       mbar_arrive(smem_u32(acc_empty + acc));
-      const int64_t cell = (int64_t)t * kTileM + row;
+      // accumulator row = x-column * 8 + y within the tile
+      const Tile tl = tile_of(P, t);
+      const int64_t cell =
+          ((int64_t)tl.zb * P.Y + tl.y0 + (row & 7)) * P.X + tl.x0 + (row >> 3);
       if (P.out_ch == 1) {  // one channel (the output layer, its weights padded to 16 rows)
         const float x = v[0] + (P.bias ? __ldg(P.bias) : 0.0f);
         static_cast<float *>(P.out)[cell] = P.relu ? fmaxf(x, 0.0f) : x;
@@ -456,19 +459,20 @@ CUtensorMapSwizzle swizzle_for(int channels)
                         : channels == 32 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_32B;
 }
 
-// channels-last BF16 volume [zb][y][x][C] as a 4-D map (C, X, Y, Z*B), box
-// (C, xbox, ybox, 1): one C x 2-byte row per cell, swizzled over that span
-bool map_volume(CUtensorMap *m, const void *base, int C, int X, int Y, int ZB, int xbox, int ybox)
+// channels-last BF16 volume [zb][y][x][C] as a 4-D map (C, Y, X, Z*B) -- y
+// before x, so a box (C, 8, 18, 1) lands as 18 x-columns of 8 cell rows --
+// one C x 2-byte row per cell, swizzled over that span
+bool map_volume(CUtensorMap *m, const void *base, int C, int X, int Y, int ZB)
 {
   auto fn = encode_fn();
   if (!fn) {
     fail(NUSIF_ERR_CUDA, "unet: cuTensorMapEncodeTiled unavailable");
     return false;
   }
-  const cuuint64_t dims[4] = { (cuuint64_t)C, (cuuint64_t)X, (cuuint64_t)Y, (cuuint64_t)ZB };
-  const cuuint64_t strides[3] = { (cuuint64_t)C * 2, (cuuint64_t)X * C * 2,
+  const cuuint64_t dims[4] = { (cuuint64_t)C, (cuuint64_t)Y, (cuuint64_t)X, (cuuint64_t)ZB };
+  const cuuint64_t strides[3] = { (cuuint64_t)X * C * 2, (cuuint64_t)C * 2,
     (cuuint64_t)Y * X * C * 2 };
-  const cuuint32_t box[4] = { (cuuint32_t)C, (cuuint32_t)xbox, (cuuint32_t)ybox, 1 };
+  const cuuint32_t box[4] = { (cuuint32_t)C, (cuuint32_t)kTileY, (cuuint32_t)kBoxX, 1 };
   const cuuint32_t es[4] = { 1, 1, 1, 1 };
   const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(base), dims,
       strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_for(C),
@@ -480,8 +484,9 @@ bool map_volume(CUtensorMap *m, const void *base, int C, int X, int Y, int ZB, i
   return true;
 }
 
-// weights [27][N][K] as a 3-D map (K, N, 27), box (C, N, 1): the C columns of
-// one source, swizzled like that source's cell rows
+// weights [27][N][K] as a 3-D map (K, N, 27), box (C, N, 3): the C columns of
+// one source for one (dz, dy) row of three taps, swizzled like that source's
+// cell rows
 bool map_weights(CUtensorMap *m, const void *base, int K, int N, int C)
 {
   auto fn = encode_fn();
@@ -491,7 +496,7 @@ bool map_weights(CUtensorMap *m, const void *base, int K, int N, int C)
   }
   const cuuint64_t dims[3] = { (cuuint64_t)K, (cuuint64_t)N, 27 };
   const cuuint64_t strides[2] = { (cuuint64_t)K * 2, (cuuint64_t)N * K * 2 };
-  const cuuint32_t box[3] = { (cuuint32_t)C, (cuuint32_t)N, 1 };
+  const cuuint32_t box[3] = { (cuuint32_t)C, (cuuint32_t)N, 3 };
   const cuuint32_t es[3] = { 1, 1, 1 };
   const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void *>(base), dims,
       strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle_for(C),
@@ -521,23 +526,23 @@ template <int NCH>
 bool launch_tc(const CUtensorMap &a0, const CUtensorMap &a1, const CUtensorMap &w0,
     const CUtensorMap &w1, TcParams P)
 {
-  // per source: 128 cell rows, then N weight rows, each region 1024-byte aligned
-  // (the 128-byte swizzle's atom)
+  // per source: the box of 18 x-columns (8 cell rows each), then the row's
+  // three taps' weights [3][N][C], each region 1024-byte aligned (the
+  // 128-byte swizzle's atom; an x-column and a tap's weights are whole
+  // multiples of every swizzle's 8-row repeat)
   uint32_t off = 0, tx = 0;
   for (int src = 0; src < 2; src++) {
-    const uint32_t row = 2u * (uint32_t)(src == 0 ? P.C0 : P.C1);
+    const uint32_t rb = 2u * (uint32_t)(src == 0 ? P.C0 : P.C1);
+    P.atom[src] = (uint32_t)kTileY * rb;
+    P.wtap[src] = (uint32_t)NCH * rb;
     P.a_off[src] = off;
-    off = align1k(off + kTileM * row);
+    off = align1k(off + (uint32_t)kBoxX * P.atom[src]);
     P.b_off[src] = off;
-    off = align1k(off + (uint32_t)NCH * row);
-    tx += kTileM * row + (uint32_t)NCH * row;
+    off = align1k(off + 3u * P.wtap[src]);
+    if (src == 0 || P.C1 > 0) tx += (uint32_t)kBoxX * P.atom[src] + 3u * P.wtap[src];
   }
-  P.tap_bytes = off;
-  // taps per stage: a whole dz plane (9) or dz, dy row (3) while the stage stays
-  // within 48 KB, so each barrier round trip carries several taps' products
-  P.taps = 9u * off <= 48u * 1024u ? 9 : 3u * off <= 48u * 1024u ? 3 : 1;
-  P.stage_bytes = (uint32_t)P.taps * off;
-  P.tx_bytes = (uint32_t)P.taps * tx;
+  P.stage_bytes = off;
+  P.tx_bytes = tx;
   const size_t stage_bytes = P.stage_bytes;
   // as many stages as fit in ~96 KB (at least 2, at most kMaxStages): two
   // blocks per SM, each keeping its stages' loads in flight
@@ -585,12 +590,7 @@ bool tc_conv_supported(int X, int Y, int Z, int B, int N, int C0, int C1)
   auto ok_c = [](int c) { return c == 16 || c == 32 || c == 64; };
   if (!ok_c(C0) || (C1 != 0 && !ok_c(C1))) return false;
   if (N != 16 && N != 32 && N != 48 && N != 64 && N != 96) return false;
-  if (X <= kTileM) {
-    if (kTileM % X) return false;
-    if (Y % (kTileM / X)) return false;
-  } else if (X % kTileM) {
-    return false;
-  }
+  if (X % kTileX || Y % kTileY) return false;
   return encode_fn() != nullptr;
 }
 
@@ -606,9 +606,9 @@ bool tc_conv(const void *s0, int C0, const void *s1, int C1, int B, int Z, int Y
   P.Y = Y;
   P.Z = Z;
   P.B = B;
-  P.xbox = X < kTileM ? X : kTileM;
-  P.ybox = kTileM / P.xbox;
-  P.ntiles = (int)((int64_t)B * Z * Y * X / kTileM);
+  P.tx = X / kTileX;
+  P.ty = Y / kTileY;
+  P.ntiles = (int)((int64_t)B * Z * P.ty * P.tx);
   P.bias = bias;
   P.relu = relu;
   P.out_bf16 = out_bf16 ? 1 : 0;
@@ -620,10 +620,10 @@ bool tc_conv(const void *s0, int C0, const void *s1, int C1, int B, int Z, int Y
   P.out = out;
   P.err = err;
   CUtensorMap a0, a1, w0, w1;
-  if (!map_volume(&a0, s0, C0, X, Y, Z * B, P.xbox, P.ybox)) return false;
+  if (!map_volume(&a0, s0, C0, X, Y, Z * B)) return false;
   if (!map_weights(&w0, w, C0 + C1, N, C0)) return false;
   if (C1 > 0) {
-    if (!map_volume(&a1, s1, C1, X, Y, Z * B, P.xbox, P.ybox)) return false;
+    if (!map_volume(&a1, s1, C1, X, Y, Z * B)) return false;
     if (!map_weights(&w1, w, C0 + C1, N, C1)) return false;
   } else {
     a1 = a0;
