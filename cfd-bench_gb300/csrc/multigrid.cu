@@ -1128,6 +1128,236 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
   cp_async_wait<0>();
 }
 
+// The same exact red-black sweep for levels whose rows are a multiple of 128
+// cells and whose columns a multiple of 8 (the finest levels of the benchmark
+// grids), with the work in registers instead of shared memory: a block owns a
+// 128 x 8 tile of (i, j) columns and a chunk of planes; warp w handles row
+// j0 - 1 + w (rows j0 - 1 and j0 + 8 are the first-colour ring), lane l the
+// four cells i0 + 4l .. i0 + 4l + 3 of that row as one float4. Each thread
+// keeps its column's x_old at k - 1, k, k + 1 and the half-updated planes
+// (first colour new, second colour old) at k - 2, k - 1, k in registers, takes
+// its x-neighbours from the neighbouring lanes by shuffle, and reads only the
+// y-neighbours from shared memory (x_old of plane k, the half-updated plane
+// k - 1, double-buffered), so a plane needs one barrier. Lanes 0 and 31 also
+// carry the ring columns i0 - 1 and i0 + 128. Planes walk with the same
+// one-plane lag as k_rbgs_sweep (first colour at k, second colour at k - 1)
+// and the same expressions, so the two kernels give the same bits; walls are
+// the same mirrors (a neighbour outside the domain holds the wall cell's old
+// value, in x_old and in the half-updated planes).
+constexpr int kVX = 128, kVY = 8;
+constexpr int kVWarps = kVY + 2;       // rows j0 - 1 .. j0 + 8
+constexpr int kVThreads = 32 * kVWarps;
+constexpr int kVRow = kVX + 8;         // staged row: columns i0 - 4 .. i0 + 131 (tile at 4)
+
+__global__ void __launch_bounds__(kVThreads, 2) k_rbgs_sweep_v(View<float> v,
+    float *__restrict__ xnew, int kc, const MgState *st, int keep)
+{
+  const int nx = v.nx, ny = v.ny, nz = v.nz;
+  const int i0 = blockIdx.x * kVX, j0 = blockIdx.y * kVY;
+  const int k0 = blockIdx.z * kc, k1 = min(k0 + kc, nz);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t sz = v.sz;
+  if (mg_done(st)) {
+    // a sweep skipped inside a V-cycle leaves x where the next kernels look
+    // (see k_rbgs_sweep): copy the tile rows of the chunk
+    if (keep && !solve_finished(st) && w >= 1 && w <= kVY) {
+      const int64_t c0 = (int64_t)(j0 + w - 1) * v.sy + i0 + 4 * lane;
+      for (int k = k0; k < k1; k++)
+        *reinterpret_cast<float4 *>(xnew + c0 + k * sz) =
+            *reinterpret_cast<const float4 *>(v.x + c0 + k * sz);
+    }
+    return;
+  }
+  __shared__ __align__(16) float sx[2][kVY + 4][kVRow];  // x_old(k): rows j0 - 2 .. j0 + 9
+  __shared__ __align__(16) float sr[2][kVWarps][kVRow];  // half-updated plane: rows j0 - 1 .. j0 + 8
+  const int j = j0 - 1 + w;
+  const bool row_in = j >= 0 && j < ny;
+  const bool tile_row = w >= 1 && w <= kVY;
+  const int jc = min(max(j, 0), ny - 1);
+  const float *__restrict__ xrow = v.x + (int64_t)jc * v.sy + i0 + 4 * lane;
+  const float *__restrict__ brow = v.b + (int64_t)jc * v.sy + i0 + 4 * lane;
+  // the extra staged rows j0 - 2 (warp 0) and j0 + 9 (warp 9), x_old only
+  const bool extra = w == 0 || w == kVWarps - 1;
+  const int je = w == 0 ? j0 - 2 : j0 + 9;
+  const float *__restrict__ xext = v.x + (int64_t)min(max(je, 0), ny - 1) * v.sy + i0 + 4 * lane;
+  const int srow_ext = w == 0 ? 0 : kVY + 3;
+  const auto lde = [&](int k) {
+    return *reinterpret_cast<const float4 *>(xext + (int64_t)min(max(k, 0), nz - 1) * sz);
+  };
+  // ring columns: lane 0 holds i0 - 2, i0 - 1; lane 31 holds i0 + 128, i0 + 129
+  // (mirrored at the x walls: the wall cell's own value)
+  const bool left_wall = i0 == 0, right_wall = i0 + kVX == nx;
+  const int hc_col = lane == 0 ? i0 - 1 : i0 + kVX;     // ring column of this lane
+  const int ho_col = lane == 0 ? i0 - 2 : i0 + kVX + 1;  // the one beyond it
+  const bool ring_lane = lane == 0 || lane == 31;
+  const bool ring_in = ring_lane && (lane == 0 ? !left_wall : !right_wall);
+  const float *__restrict__ xrc = v.x + (int64_t)jc * v.sy;  // this row, for the ring columns
+  const float *__restrict__ brc = v.b + (int64_t)jc * v.sy;
+  const float ex = v.ex, ey = v.ey, ez = v.ez, dg = v.diag, idg = v.inv_diag;
+
+  auto ldx = [&](int k) {
+    return *reinterpret_cast<const float4 *>(xrow + (int64_t)min(max(k, 0), nz - 1) * sz);
+  };
+  auto ldb = [&](int k) {
+    return *reinterpret_cast<const float4 *>(brow + (int64_t)min(max(k, 0), nz - 1) * sz);
+  };
+  // ring column values of plane k: (column hc_col, column ho_col), mirrored at walls
+  auto ldh = [&](int k, float own_edge) {
+    const int64_t pk = (int64_t)min(max(k, 0), nz - 1) * sz;
+    float2 h;
+    if (ring_in) {
+      h.x = xrc[pk + hc_col];
+      h.y = xrc[pk + ho_col];
+    } else {
+      h.x = own_edge;  // the wall cell itself (the caller passes this lane's edge cell)
+      h.y = own_edge;
+    }
+    return h;
+  };
+
+  // registers: x_old at k - 1, k, k + 1 (and k + 2 in flight), b at k - 1, k (k + 1
+  // in flight), the half-updated planes at k - 2, k - 1, k; ring column of x_old at
+  // k - 1, k, k + 1 and its b at k
+  float4 om = ldx(k0 - 2), oc = ldx(k0 - 1), op = ldx(k0), on = ldx(k0 + 1);
+  float4 bm = make_float4(0.f, 0.f, 0.f, 0.f), bc = ldb(k0 - 1), bn = ldb(k0);
+  float4 rm2 = oc, rm1 = oc, rc = oc;
+  float4 ec = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (extra) ec = lde(k0 - 1);
+  const auto edge = [&](const float4 &q) { return lane == 0 ? q.x : q.w; };
+  float2 hm = make_float2(0.f, 0.f), hc = make_float2(0.f, 0.f), hp = make_float2(0.f, 0.f);
+  float hb = 0.0f;
+  if (ring_lane) {
+    hm = ldh(k0 - 2, edge(om));
+    hc = ldh(k0 - 1, edge(oc));
+    hp = ldh(k0, edge(op));
+  }
+  for (int k = k0 - 1; k <= k1; k++) {
+    const int s = k & 1;
+    const bool kin = k >= 0 && k < nz;
+    // ---- stage x_old(k) of this row, the extra rows and the ring columns ----
+    *reinterpret_cast<float4 *>(&sx[s][w + 1][4 + 4 * lane]) = oc;
+    if (extra) *reinterpret_cast<float4 *>(&sx[s][srow_ext][4 + 4 * lane]) = ec;
+    if (ring_lane) {
+      const int c_in = lane == 0 ? 3 : kVX + 4;  // staged column of the ring cell
+      sx[s][w + 1][c_in] = hc.x;
+      if (ring_in && kin) hb = brc[(int64_t)k * sz + hc_col];
+    }
+    // loads for the coming planes, issued before the barrier: x_old(k + 3),
+    // b(k + 2), the extra row's x_old(k + 1), the ring column's x_old(k + 2)
+    const float4 onext = ldx(k + 3);
+    const float4 bnext = ldb(k + 2);
+    float4 enext = ec;
+    if (extra) enext = lde(k + 1);
+    float2 hnext = make_float2(0.f, 0.f);
+    if (ring_lane) hnext = ldh(k + 2, edge(on));
+    __syncthreads();
+    // ---- first colour of plane k on this row: (i + j + k) even ----
+    {
+      const float left = __shfl_up_sync(0xffffffffu, oc.w, 1);
+      const float right = __shfl_down_sync(0xffffffffu, oc.x, 1);
+      const float l0 = lane == 0 ? hc.x : left;     // cell i0 + 4l - 1
+      const float r3 = lane == 31 ? hc.x : right;   // cell i0 + 4l + 4
+      const float4 yn = *reinterpret_cast<const float4 *>(&sx[s][w][4 + 4 * lane]);
+      const float4 ys = *reinterpret_cast<const float4 *>(&sx[s][w + 2][4 + 4 * lane]);
+      rc = oc;
+      if (kin && row_in) {
+        const bool even = ((j + k) & 1) == 0;  // cells 0 and 2 are first colour, else 1 and 3
+        if (even) {
+          {
+            const float sxs = l0 + oc.y, sys = yn.x + ys.x, szs = om.x + op.x;
+            const float lap = sxs * ex + sys * ey + szs * ez - dg * oc.x;
+            rc.x = oc.x - (bc.x - lap) * idg;
+          }
+          {
+            const float sxs = oc.y + oc.w, sys = yn.z + ys.z, szs = om.z + op.z;
+            const float lap = sxs * ex + sys * ey + szs * ez - dg * oc.z;
+            rc.z = oc.z - (bc.z - lap) * idg;
+          }
+        } else {
+          {
+            const float sxs = oc.x + oc.z, sys = yn.y + ys.y, szs = om.y + op.y;
+            const float lap = sxs * ex + sys * ey + szs * ez - dg * oc.y;
+            rc.y = oc.y - (bc.y - lap) * idg;
+          }
+          {
+            const float sxs = oc.z + r3, sys = yn.w + ys.w, szs = om.w + op.w;
+            const float lap = sxs * ex + sys * ey + szs * ez - dg * oc.w;
+            rc.w = oc.w - (bc.w - lap) * idg;
+          }
+        }
+      }
+    }
+    *reinterpret_cast<float4 *>(&sr[s][w][4 + 4 * lane]) = rc;
+    // the ring column's first-colour value (column i0 - 1 is first colour when
+    // j + k is odd, column i0 + 128 when it is even)
+    if (ring_lane) {
+      const int c_in = lane == 0 ? 3 : kVX + 4;
+      float hr = hc.x;
+      const bool first = lane == 0 ? ((j + k) & 1) != 0 : ((j + k) & 1) == 0;
+      if (first && ring_in && kin && tile_row) {
+        const float inner = lane == 0 ? oc.x : oc.w;  // the tile's edge cell
+        const float sxs = lane == 0 ? hc.y + inner : inner + hc.y;
+        const float sys = sx[s][w][c_in] + sx[s][w + 2][c_in];
+        const float szs = hm.x + hp.x;
+        const float lap = sxs * ex + sys * ey + szs * ez - dg * hc.x;
+        hr = hc.x - (hb - lap) * idg;
+      }
+      sr[s][w][c_in] = hr;
+    }
+    // ---- second colour of plane k - 1 on the tile rows: (i + j + k - 1) odd ----
+    const int ke = k - 1;
+    if (ke >= k0 && ke < k1 && tile_row) {
+      const int se = ke & 1;
+      const float left = __shfl_up_sync(0xffffffffu, rm1.w, 1);
+      const float right = __shfl_down_sync(0xffffffffu, rm1.x, 1);
+      const float l0 = lane == 0 ? sr[se][w][3] : left;
+      const float r3 = lane == 31 ? sr[se][w][kVX + 4] : right;
+      const float4 yn = *reinterpret_cast<const float4 *>(&sr[se][w - 1][4 + 4 * lane]);
+      const float4 ys = *reinterpret_cast<const float4 *>(&sr[se][w + 1][4 + 4 * lane]);
+      float4 out = rm1;
+      const bool even = ((j + k) & 1) == 0;  // second colour of plane k - 1: cells 0 and 2
+      if (even) {
+        {
+          const float sxs = l0 + rm1.y, sys = yn.x + ys.x, szs = rm2.x + rc.x;
+          const float lap = sxs * ex + sys * ey + szs * ez - dg * rm1.x;
+          out.x = rm1.x - (bm.x - lap) * idg;
+        }
+        {
+          const float sxs = rm1.y + rm1.w, sys = yn.z + ys.z, szs = rm2.z + rc.z;
+          const float lap = sxs * ex + sys * ey + szs * ez - dg * rm1.z;
+          out.z = rm1.z - (bm.z - lap) * idg;
+        }
+      } else {
+        {
+          const float sxs = rm1.x + rm1.z, sys = yn.y + ys.y, szs = rm2.y + rc.y;
+          const float lap = sxs * ex + sys * ey + szs * ez - dg * rm1.y;
+          out.y = rm1.y - (bm.y - lap) * idg;
+        }
+        {
+          const float sxs = rm1.z + r3, sys = yn.w + ys.w, szs = rm2.w + rc.w;
+          const float lap = sxs * ex + sys * ey + szs * ez - dg * rm1.w;
+          out.w = rm1.w - (bm.w - lap) * idg;
+        }
+      }
+      *reinterpret_cast<float4 *>(xnew + (int64_t)ke * sz + (int64_t)j * v.sy + i0 + 4 * lane) = out;
+    }
+    // ---- rotate ----
+    rm2 = rm1;
+    rm1 = rc;
+    om = oc;
+    oc = op;
+    op = on;
+    on = onext;
+    bm = bc;
+    bc = bn;
+    bn = bnext;
+    hm = hc;
+    hc = hp;
+    hp = hnext;
+    ec = enext;
+  }
+}
+
 // x_f += trilinear interpolation of x_c when x was coarsened (rx == 2): one
 // thread per coarse x-position and fine (j, k) produces both x-children, so
 // the three coarse values of each (y, z) line are loaded once for two cells.
@@ -1825,20 +2055,63 @@ bool coarse_solve(const View<T> &v, int nsweeps, const MgState *st, const T *min
 // recomputed) and the grid runs in ceil(blocks / resident) waves; the rule
 // minimises waves * (kc + 2). The chunk depth changes only how the work is
 // split: every cell is computed the same way, so results do not depend on it.
+// The one-kernel FP32 sweep of a level: k_rbgs_sweep_v where the rows are a
+// multiple of 128 cells and the columns of 8 (the environment variable
+// NUSIF_SWEEP=tile64 selects k_rbgs_sweep everywhere, for comparisons), else
+// k_rbgs_sweep.
+struct SweepShape {
+  bool vec;
+  int gx, gy, threads;
+};
+
+SweepShape sweep_shape(const MgLevelDesc &L)
+{
+  const char *e = getenv("NUSIF_SWEEP");
+  const bool legacy = e && strcmp(e, "tile64") == 0;
+  SweepShape r;
+  r.vec = !legacy && L.n[0] % kVX == 0 && L.n[1] % kVY == 0;
+  if (r.vec) {
+    r.gx = L.n[0] / kVX;
+    r.gy = L.n[1] / kVY;
+    r.threads = kVThreads;
+  } else {
+    r.gx = (L.n[0] + kSX - 1) / kSX;
+    r.gy = (L.n[1] + kSY - 1) / kSY;
+    r.threads = 256;
+  }
+  return r;
+}
+
+void launch_rbgs(const SweepShape &sh, const View<float> &v, float *xb, int kc, const MgState *st,
+    int keep)
+{
+  const dim3 grid(sh.gx, sh.gy, (v.nz + kc - 1) / kc);
+  if (sh.vec)
+    k_rbgs_sweep_v<<<grid, kVThreads, 0, stream()>>>(v, xb, kc, st, keep);
+  else
+    k_rbgs_sweep<<<grid, 256, 0, stream()>>>(v, xb, kc, st, keep);
+}
+
 int sweep_chunk_rule(const MgLevelDesc &L)
 {
-  static int resident = 0;
-  if (resident == 0) {
+  const SweepShape sh = sweep_shape(L);
+  static int resident[2] = { 0, 0 };
+  int &res = resident[sh.vec ? 1 : 0];
+  if (res == 0) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_sweep, 256, 0);
-    resident = (per_sm > 0 ? per_sm : 1) * sm_count_mg();
+    if (sh.vec)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_sweep_v, kVThreads, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rbgs_sweep, 256, 0);
+    res = (per_sm > 0 ? per_sm : 1) * sm_count_mg();
   }
-  const int gx = (L.n[0] + kSX - 1) / kSX, gy = (L.n[1] + kSY - 1) / kSY, nz = L.n[2];
+  const int resident_blocks = res;
+  const int gx = sh.gx, gy = sh.gy, nz = L.n[2];
   int kc = nz;
   int64_t best = -1;
   for (int c = 1; c <= nz; c++) {
     const int64_t blocks = (int64_t)gx * gy * ((nz + c - 1) / c);
-    const int64_t cost = ((blocks + resident - 1) / resident) * (int64_t)(c + 2);
+    const int64_t cost = ((blocks + resident_blocks - 1) / resident_blocks) * (int64_t)(c + 2);
     if (best < 0 || cost < best) {
       best = cost;
       kc = c;
@@ -1854,8 +2127,10 @@ int sweep_chunk_tuned(const MgLevelDesc &L, float *x, float *xb, float *b)
 {
   int dev = 0;
   cudaGetDevice(&dev);
-  static std::map<std::array<int, 4>, int> cache;  // (device, nx, ny, nz) -> planes per block
-  const std::array<int, 4> key = { dev, L.n[0], L.n[1], L.n[2] };
+  const SweepShape sh = sweep_shape(L);
+  // (device, nx, ny, nz, kernel) -> planes per block
+  static std::map<std::array<int, 5>, int> cache;
+  const std::array<int, 5> key = { dev, L.n[0], L.n[1], L.n[2], sh.vec ? 1 : 0 };
   const auto hit = cache.find(key);
   if (hit != cache.end()) return hit->second;
   const int rule = sweep_chunk_rule(L);
@@ -1874,7 +2149,7 @@ int sweep_chunk_tuned(const MgLevelDesc &L, float *x, float *xb, float *b)
     }
     idle = fresh;
   }
-  const int gx = (L.n[0] + kSX - 1) / kSX, gy = (L.n[1] + kSY - 1) / kSY, nz = L.n[2];
+  const int nz = L.n[2];
   const View<float> v = compact_view<float>(L, x, b);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
@@ -1887,11 +2162,9 @@ int sweep_chunk_tuned(const MgLevelDesc &L, float *x, float *xb, float *b)
   const int cand[] = { rule, 1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64 };
   for (const int c : cand) {
     if (c > nz) continue;
-    const dim3 grid(gx, gy, (nz + c - 1) / c);
-    k_rbgs_sweep<<<grid, 256, 0, stream()>>>(v, xb, c, idle, 0);  // warm-up
+    launch_rbgs(sh, v, xb, c, idle, 0);  // warm-up
     cudaEventRecord(e0, stream());
-    for (int r = 0; r < 3; r++)
-      k_rbgs_sweep<<<grid, 256, 0, stream()>>>(v, xb, c, idle, 0);
+    for (int r = 0; r < 3; r++) launch_rbgs(sh, v, xb, c, idle, 0);
     cudaEventRecord(e1, stream());
     float ms = 0.0f;
     if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess)
@@ -1915,9 +2188,8 @@ bool fused_sweeps(MgHierarchy *H, int l, int count, bool zero_first, const MgSta
     const View<float> v = compact_view<float>(L, H->x32[l], H->b32[l]);
     return sweeps<float>(v, count, zero_first, nullptr, st);
   }
-  const int gx = (L.n[0] + kSX - 1) / kSX, gy = (L.n[1] + kSY - 1) / kSY;
+  const SweepShape sh = sweep_shape(L);
   const int kc = H->kc[l] > 0 ? H->kc[l] : sweep_chunk_rule(L);
-  const dim3 grid(gx, gy, (L.n[2] + kc - 1) / kc);
   for (int s = 0; s < count; s++) {
     const View<float> v = compact_view<float>(L, H->x32[l], H->b32[l]);
     if (zero_first && s == 0) {
@@ -1928,8 +2200,8 @@ bool fused_sweeps(MgHierarchy *H, int l, int count, bool zero_first, const MgSta
           H->keep_on_skip);
       if (!launched("k_rb_zero_sweep")) return false;
     } else {
-      k_rbgs_sweep<<<grid, 256, 0, stream()>>>(v, H->x32b[l], kc, st, H->keep_on_skip);
-      if (!launched("k_rbgs_sweep")) return false;
+      launch_rbgs(sh, v, H->x32b[l], kc, st, H->keep_on_skip);
+      if (!launched(sh.vec ? "k_rbgs_sweep_v" : "k_rbgs_sweep")) return false;
     }
     float *t = H->x32[l];
     H->x32[l] = H->x32b[l];

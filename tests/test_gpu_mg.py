@@ -254,6 +254,37 @@ def test_fp32_one_kernel_sweep_is_exact_red_black(nusif_lib, dims):
         assert np.max(np.abs(got - want)) <= 2e-5 * scale, (s, np.max(np.abs(got - want)) / scale)
 
 
+@pytest.mark.parametrize("dims", [(128, 24, 40), (256, 16, 12), (128, 8, 70), (384, 40, 9)])
+def test_register_tiled_sweep_equals_shared_memory_sweep(nusif_lib, dims, monkeypatch):
+    """k_rbgs_sweep_v (rows a multiple of 128 cells, columns of 8: x-neighbours
+    by shuffle, z-neighbours in registers) gives the same bits as k_rbgs_sweep
+    (NUSIF_SWEEP=tile64), from a start and from zero, for one to three sweeps,
+    on chunked planes and x-tiles with both x walls inside one tile row."""
+    import ctypes as C
+
+    import torch
+    nx, ny, nz = dims
+    rng = np.random.default_rng(37)
+    x = torch.from_numpy(rng.standard_normal((nz, ny, nx)).astype(np.float32)).cuda()
+    b = torch.from_numpy(rng.standard_normal((nz, ny, nx)).astype(np.float32)).cuda()
+    h = (1.1 / nx, 0.7 / ny, 1.3 / nz)
+    for start in (x, None):
+        for s in (1, 2, 3):
+            got = {}
+            for kernel in ("tile64", "vector"):
+                if kernel == "tile64":
+                    monkeypatch.setenv("NUSIF_SWEEP", "tile64")
+                else:
+                    monkeypatch.delenv("NUSIF_SWEEP", raising=False)
+                out = torch.empty_like(x)
+                rc = nusif_lib.nusifSmoothRBF32(
+                    C.c_void_p(start.data_ptr()) if start is not None else None,
+                    C.c_void_p(b.data_ptr()), C.c_void_p(out.data_ptr()), nx, ny, nz, *h, s)
+                assert rc == 0
+                got[kernel] = out.cpu().numpy()
+            np.testing.assert_array_equal(got["vector"], got["tile64"])
+
+
 @pytest.mark.parametrize("solver,pre,post", [("mg", 2, 2), ("mg-mixed", 2, 2), ("mg-mixed", 3, 3),
                                              ("mg-mixed", 3, 1), ("mg-mixed", 2, 1)])
 def test_graph_solve_matches_host_driven_solve(nusif_lib, solver, pre, post):
