@@ -1131,23 +1131,25 @@ __global__ void __launch_bounds__(256) k_rbgs_sweep(View<float> v, float *__rest
 // The same exact red-black sweep for levels whose rows are a multiple of 128
 // cells and whose columns a multiple of 8 (the finest levels of the benchmark
 // grids), with the work in registers instead of shared memory: a block owns a
-// 128 x 8 tile of (i, j) columns and a chunk of planes; warp w handles row
-// j0 - 1 + w (rows j0 - 1 and j0 + 8 are the first-colour ring), lane l the
-// four cells i0 + 4l .. i0 + 4l + 3 of that row as one float4. Each thread
-// keeps its column's x_old at k - 1, k, k + 1 and the half-updated planes
-// (first colour new, second colour old) at k - 2, k - 1, k in registers, takes
-// its x-neighbours from the neighbouring lanes by shuffle, and reads only the
-// y-neighbours from shared memory (x_old of plane k, the half-updated plane
-// k - 1, double-buffered), so a plane needs one barrier. Lanes 0 and 31 also
-// carry the ring columns i0 - 1 and i0 + 128. Planes walk with the same
-// one-plane lag as k_rbgs_sweep (first colour at k, second colour at k - 1)
-// and the same expressions, so the two kernels give the same bits; walls are
-// the same mirrors (a neighbour outside the domain holds the wall cell's old
-// value, in x_old and in the half-updated planes).
+// 128 x 8 tile of (i, j) columns and a chunk of planes; warp w < 10 handles
+// row j0 - 1 + w (rows j0 - 1 and j0 + 8 are the first-colour ring), lane l
+// the four cells i0 + 4l .. i0 + 4l + 3 of that row as one float4. Each such
+// thread keeps its column's x_old at k - 1, k, k + 1 and the half-updated
+// planes (first colour new, second colour old) at k - 2, k - 1, k in
+// registers and takes its x-neighbours from the neighbouring lanes by
+// shuffle; only the y-neighbours come from shared memory (x_old of plane k
+// and the half-updated plane k - 1, double-buffered), so a plane needs one
+// barrier. Warp 10 carries the ring columns i0 - 1 and i0 + 128 for the ten
+// rows (lanes 0-9 and 16-25), so the row warps run no per-lane ring code.
+// Planes walk with the same one-plane lag as k_rbgs_sweep (first colour at k,
+// second colour at k - 1) and the same expressions, so the two kernels give
+// the same bits; walls are the same mirrors (a neighbour outside the domain
+// holds the wall cell's old value, in x_old and in the half-updated planes).
 constexpr int kVX = 128, kVY = 8;
-constexpr int kVWarps = kVY + 2;       // rows j0 - 1 .. j0 + 8
-constexpr int kVThreads = 32 * kVWarps;
+constexpr int kVRows = kVY + 2;        // rows j0 - 1 .. j0 + 8
+constexpr int kVThreads = 32 * (kVRows + 1);
 constexpr int kVRow = kVX + 8;         // staged row: columns i0 - 4 .. i0 + 131 (tile at 4)
+constexpr int kVL = 3, kVR = kVX + 4;  // staged columns of the ring cells i0 - 1, i0 + 128
 
 __global__ void __launch_bounds__(kVThreads, 2) k_rbgs_sweep_v(View<float> v,
     float *__restrict__ xnew, int kc, const MgState *st, int keep)
@@ -1156,115 +1158,123 @@ __global__ void __launch_bounds__(kVThreads, 2) k_rbgs_sweep_v(View<float> v,
   const int i0 = blockIdx.x * kVX, j0 = blockIdx.y * kVY;
   const int k0 = blockIdx.z * kc, k1 = min(k0 + kc, nz);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t sz = v.sz;
+  const int sy = v.sy, sz = v.sz;
   if (mg_done(st)) {
     // a sweep skipped inside a V-cycle leaves x where the next kernels look
     // (see k_rbgs_sweep): copy the tile rows of the chunk
     if (keep && !solve_finished(st) && w >= 1 && w <= kVY) {
-      const int64_t c0 = (int64_t)(j0 + w - 1) * v.sy + i0 + 4 * lane;
+      const int c0 = (j0 + w - 1) * sy + i0 + 4 * lane;
       for (int k = k0; k < k1; k++)
-        *reinterpret_cast<float4 *>(xnew + c0 + k * sz) =
-            *reinterpret_cast<const float4 *>(v.x + c0 + k * sz);
+        *reinterpret_cast<float4 *>(xnew + c0 + (int64_t)k * sz) =
+            *reinterpret_cast<const float4 *>(v.x + c0 + (int64_t)k * sz);
     }
     return;
   }
   __shared__ __align__(16) float sx[2][kVY + 4][kVRow];  // x_old(k): rows j0 - 2 .. j0 + 9
-  __shared__ __align__(16) float sr[2][kVWarps][kVRow];  // half-updated plane: rows j0 - 1 .. j0 + 8
+  __shared__ __align__(16) float sr[2][kVRows][kVRow];   // half-updated plane: rows j0 - 1 .. j0 + 8
+  const float ex = v.ex, ey = v.ey, ez = v.ez, dg = v.diag, idg = v.inv_diag;
+  const auto plane = [&](int k) { return min(max(k, 0), nz - 1) * sz; };  // < 2^31
+
+  if (w == kVRows) {
+    // ---------------- ring columns: lane r < 10 left, 16 <= lane < 26 right ----------------
+    const int r = lane & 15;
+    const bool right = lane >= 16;
+    const bool act = r < kVRows;
+    const int j = j0 - 1 + r;
+    const int jc = min(max(j, 0), ny - 1);
+    const bool wall = right ? i0 + kVX == nx : i0 == 0;
+    const int col = right ? i0 + kVX : i0 - 1;       // the ring cell
+    const int beyond = right ? i0 + kVX + 1 : i0 - 2;
+    const int edge = right ? i0 + kVX - 1 : i0;      // the tile's edge cell beside it
+    const int scol = right ? kVR : kVL;
+    const bool in = act && !wall && j >= 0 && j < ny && r >= 1 && r <= kVY;
+    const float *__restrict__ xr = v.x + jc * sy;
+    const float *__restrict__ br = v.b + jc * sy;
+    // the ring cell's x_old at k - 1, k, k + 1 (the wall cell's own value outside the domain)
+    const auto ld = [&](int k) { return act ? xr[plane(k) + (wall ? edge : col)] : 0.0f; };
+    float hm = ld(k0 - 2), hc = ld(k0 - 1), hp = ld(k0);
+    // b and the column beyond the ring cell, one plane ahead (ring cells in the domain)
+    const auto ldb2 = [&](int k) {
+      return in ? make_float2(br[plane(k) + col], xr[plane(k) + beyond]) : make_float2(0.f, 0.f);
+    };
+    float2 bb = ldb2(k0 - 1);
+    for (int k = k0 - 1; k <= k1; k++) {
+      const int s = k & 1;
+      if (act) sx[s][r + 1][scol] = hc;
+      const bool kin = k >= 0 && k < nz;
+      const float hb = bb.x, hby = bb.y;
+      const float hnext = ld(k + 2);
+      const float2 bbnext = ldb2(k + 1);
+      __syncthreads();
+      if (act) {
+        float hr = hc;
+        const bool first = right ? ((j + k) & 1) == 0 : ((j + k) & 1) != 0;
+        if (first && in && kin) {
+          const float inner = sx[s][r + 1][right ? kVR - 1 : kVL + 1];  // the tile's edge cell
+          const float sxs = right ? inner + hby : hby + inner;
+          const float sys = sx[s][r][scol] + sx[s][r + 2][scol];
+          const float szs = hm + hp;
+          const float lap = sxs * ex + sys * ey + szs * ez - dg * hc;
+          hr = hc - (hb - lap) * idg;
+        }
+        sr[s][r][scol] = hr;
+      }
+      hm = hc;
+      hc = hp;
+      hp = hnext;
+      bb = bbnext;
+    }
+    return;
+  }
+
+  // ---------------- row warps ----------------
   const int j = j0 - 1 + w;
   const bool row_in = j >= 0 && j < ny;
   const bool tile_row = w >= 1 && w <= kVY;
   const int jc = min(max(j, 0), ny - 1);
-  const float *__restrict__ xrow = v.x + (int64_t)jc * v.sy + i0 + 4 * lane;
-  const float *__restrict__ brow = v.b + (int64_t)jc * v.sy + i0 + 4 * lane;
+  const float *__restrict__ xrow = v.x + jc * sy + i0 + 4 * lane;
+  const float *__restrict__ brow = v.b + jc * sy + i0 + 4 * lane;
+  float *__restrict__ orow = xnew + j * sy + i0 + 4 * lane;  // used for tile rows only
   // the extra staged rows j0 - 2 (warp 0) and j0 + 9 (warp 9), x_old only
-  const bool extra = w == 0 || w == kVWarps - 1;
+  const bool extra = w == 0 || w == kVRows - 1;
   const int je = w == 0 ? j0 - 2 : j0 + 9;
-  const float *__restrict__ xext = v.x + (int64_t)min(max(je, 0), ny - 1) * v.sy + i0 + 4 * lane;
+  const float *__restrict__ xext = v.x + min(max(je, 0), ny - 1) * sy + i0 + 4 * lane;
   const int srow_ext = w == 0 ? 0 : kVY + 3;
-  const auto lde = [&](int k) {
-    return *reinterpret_cast<const float4 *>(xext + (int64_t)min(max(k, 0), nz - 1) * sz);
-  };
-  // ring columns: lane 0 holds i0 - 2, i0 - 1; lane 31 holds i0 + 128, i0 + 129
-  // (mirrored at the x walls: the wall cell's own value)
-  const bool left_wall = i0 == 0, right_wall = i0 + kVX == nx;
-  const int hc_col = lane == 0 ? i0 - 1 : i0 + kVX;     // ring column of this lane
-  const int ho_col = lane == 0 ? i0 - 2 : i0 + kVX + 1;  // the one beyond it
-  const bool ring_lane = lane == 0 || lane == 31;
-  const bool ring_in = ring_lane && (lane == 0 ? !left_wall : !right_wall);
-  const float *__restrict__ xrc = v.x + (int64_t)jc * v.sy;  // this row, for the ring columns
-  const float *__restrict__ brc = v.b + (int64_t)jc * v.sy;
-  const float ex = v.ex, ey = v.ey, ez = v.ez, dg = v.diag, idg = v.inv_diag;
+  const auto ldx = [&](int k) { return *reinterpret_cast<const float4 *>(xrow + plane(k)); };
+  const auto ldb = [&](int k) { return *reinterpret_cast<const float4 *>(brow + plane(k)); };
+  const auto lde = [&](int k) { return *reinterpret_cast<const float4 *>(xext + plane(k)); };
 
-  auto ldx = [&](int k) {
-    return *reinterpret_cast<const float4 *>(xrow + (int64_t)min(max(k, 0), nz - 1) * sz);
-  };
-  auto ldb = [&](int k) {
-    return *reinterpret_cast<const float4 *>(brow + (int64_t)min(max(k, 0), nz - 1) * sz);
-  };
-  // ring column values of plane k: (column hc_col, column ho_col), mirrored at walls
-  auto ldh = [&](int k, float own_edge) {
-    const int64_t pk = (int64_t)min(max(k, 0), nz - 1) * sz;
-    float2 h;
-    if (ring_in) {
-      h.x = xrc[pk + hc_col];
-      h.y = xrc[pk + ho_col];
-    } else {
-      h.x = own_edge;  // the wall cell itself (the caller passes this lane's edge cell)
-      h.y = own_edge;
-    }
-    return h;
-  };
-
-  // registers: x_old at k - 1, k, k + 1 (and k + 2 in flight), b at k - 1, k (k + 1
-  // in flight), the half-updated planes at k - 2, k - 1, k; ring column of x_old at
-  // k - 1, k, k + 1 and its b at k
+  // x_old at k - 1, k, k + 1 (k + 2 and k + 3 in flight), b at k - 1, k (k + 1 and
+  // k + 2 in flight), the half-updated planes at k - 2, k - 1, k
   float4 om = ldx(k0 - 2), oc = ldx(k0 - 1), op = ldx(k0), on = ldx(k0 + 1);
   float4 bm = make_float4(0.f, 0.f, 0.f, 0.f), bc = ldb(k0 - 1), bn = ldb(k0);
   float4 rm2 = oc, rm1 = oc, rc = oc;
   float4 ec = make_float4(0.f, 0.f, 0.f, 0.f);
   if (extra) ec = lde(k0 - 1);
-  const auto edge = [&](const float4 &q) { return lane == 0 ? q.x : q.w; };
-  float2 hm = make_float2(0.f, 0.f), hc = make_float2(0.f, 0.f), hp = make_float2(0.f, 0.f);
-  float hb = 0.0f;
-  if (ring_lane) {
-    hm = ldh(k0 - 2, edge(om));
-    hc = ldh(k0 - 1, edge(oc));
-    hp = ldh(k0, edge(op));
-  }
   for (int k = k0 - 1; k <= k1; k++) {
     const int s = k & 1;
     const bool kin = k >= 0 && k < nz;
-    // ---- stage x_old(k) of this row, the extra rows and the ring columns ----
     *reinterpret_cast<float4 *>(&sx[s][w + 1][4 + 4 * lane]) = oc;
     if (extra) *reinterpret_cast<float4 *>(&sx[s][srow_ext][4 + 4 * lane]) = ec;
-    if (ring_lane) {
-      const int c_in = lane == 0 ? 3 : kVX + 4;  // staged column of the ring cell
-      sx[s][w + 1][c_in] = hc.x;
-      if (ring_in && kin) hb = brc[(int64_t)k * sz + hc_col];
-    }
-    // loads for the coming planes, issued before the barrier: x_old(k + 3),
-    // b(k + 2), the extra row's x_old(k + 1), the ring column's x_old(k + 2)
+    // loads for the coming planes, issued before the barrier
     const float4 onext = ldx(k + 3);
     const float4 bnext = ldb(k + 2);
     float4 enext = ec;
     if (extra) enext = lde(k + 1);
-    float2 hnext = make_float2(0.f, 0.f);
-    if (ring_lane) hnext = ldh(k + 2, edge(on));
     __syncthreads();
     // ---- first colour of plane k on this row: (i + j + k) even ----
     {
-      const float left = __shfl_up_sync(0xffffffffu, oc.w, 1);
-      const float right = __shfl_down_sync(0xffffffffu, oc.x, 1);
-      const float l0 = lane == 0 ? hc.x : left;     // cell i0 + 4l - 1
-      const float r3 = lane == 31 ? hc.x : right;   // cell i0 + 4l + 4
+      float left = __shfl_up_sync(0xffffffffu, oc.w, 1);
+      float right = __shfl_down_sync(0xffffffffu, oc.x, 1);
+      if (lane == 0) left = sx[s][w + 1][kVL];
+      if (lane == 31) right = sx[s][w + 1][kVR];
       const float4 yn = *reinterpret_cast<const float4 *>(&sx[s][w][4 + 4 * lane]);
       const float4 ys = *reinterpret_cast<const float4 *>(&sx[s][w + 2][4 + 4 * lane]);
       rc = oc;
       if (kin && row_in) {
-        const bool even = ((j + k) & 1) == 0;  // cells 0 and 2 are first colour, else 1 and 3
-        if (even) {
+        if (((j + k) & 1) == 0) {  // cells 0 and 2
           {
-            const float sxs = l0 + oc.y, sys = yn.x + ys.x, szs = om.x + op.x;
+            const float sxs = left + oc.y, sys = yn.x + ys.x, szs = om.x + op.x;
             const float lap = sxs * ex + sys * ey + szs * ez - dg * oc.x;
             rc.x = oc.x - (bc.x - lap) * idg;
           }
@@ -1273,14 +1283,14 @@ __global__ void __launch_bounds__(kVThreads, 2) k_rbgs_sweep_v(View<float> v,
             const float lap = sxs * ex + sys * ey + szs * ez - dg * oc.z;
             rc.z = oc.z - (bc.z - lap) * idg;
           }
-        } else {
+        } else {  // cells 1 and 3
           {
             const float sxs = oc.x + oc.z, sys = yn.y + ys.y, szs = om.y + op.y;
             const float lap = sxs * ex + sys * ey + szs * ez - dg * oc.y;
             rc.y = oc.y - (bc.y - lap) * idg;
           }
           {
-            const float sxs = oc.z + r3, sys = yn.w + ys.w, szs = om.w + op.w;
+            const float sxs = oc.z + right, sys = yn.w + ys.w, szs = om.w + op.w;
             const float lap = sxs * ex + sys * ey + szs * ez - dg * oc.w;
             rc.w = oc.w - (bc.w - lap) * idg;
           }
@@ -1288,37 +1298,20 @@ __global__ void __launch_bounds__(kVThreads, 2) k_rbgs_sweep_v(View<float> v,
       }
     }
     *reinterpret_cast<float4 *>(&sr[s][w][4 + 4 * lane]) = rc;
-    // the ring column's first-colour value (column i0 - 1 is first colour when
-    // j + k is odd, column i0 + 128 when it is even)
-    if (ring_lane) {
-      const int c_in = lane == 0 ? 3 : kVX + 4;
-      float hr = hc.x;
-      const bool first = lane == 0 ? ((j + k) & 1) != 0 : ((j + k) & 1) == 0;
-      if (first && ring_in && kin && tile_row) {
-        const float inner = lane == 0 ? oc.x : oc.w;  // the tile's edge cell
-        const float sxs = lane == 0 ? hc.y + inner : inner + hc.y;
-        const float sys = sx[s][w][c_in] + sx[s][w + 2][c_in];
-        const float szs = hm.x + hp.x;
-        const float lap = sxs * ex + sys * ey + szs * ez - dg * hc.x;
-        hr = hc.x - (hb - lap) * idg;
-      }
-      sr[s][w][c_in] = hr;
-    }
     // ---- second colour of plane k - 1 on the tile rows: (i + j + k - 1) odd ----
     const int ke = k - 1;
     if (ke >= k0 && ke < k1 && tile_row) {
       const int se = ke & 1;
-      const float left = __shfl_up_sync(0xffffffffu, rm1.w, 1);
-      const float right = __shfl_down_sync(0xffffffffu, rm1.x, 1);
-      const float l0 = lane == 0 ? sr[se][w][3] : left;
-      const float r3 = lane == 31 ? sr[se][w][kVX + 4] : right;
+      float left = __shfl_up_sync(0xffffffffu, rm1.w, 1);
+      float right = __shfl_down_sync(0xffffffffu, rm1.x, 1);
+      if (lane == 0) left = sr[se][w][kVL];
+      if (lane == 31) right = sr[se][w][kVR];
       const float4 yn = *reinterpret_cast<const float4 *>(&sr[se][w - 1][4 + 4 * lane]);
       const float4 ys = *reinterpret_cast<const float4 *>(&sr[se][w + 1][4 + 4 * lane]);
       float4 out = rm1;
-      const bool even = ((j + k) & 1) == 0;  // second colour of plane k - 1: cells 0 and 2
-      if (even) {
+      if (((j + k) & 1) == 0) {  // second colour of plane k - 1: cells 0 and 2
         {
-          const float sxs = l0 + rm1.y, sys = yn.x + ys.x, szs = rm2.x + rc.x;
+          const float sxs = left + rm1.y, sys = yn.x + ys.x, szs = rm2.x + rc.x;
           const float lap = sxs * ex + sys * ey + szs * ez - dg * rm1.x;
           out.x = rm1.x - (bm.x - lap) * idg;
         }
@@ -1334,12 +1327,12 @@ __global__ void __launch_bounds__(kVThreads, 2) k_rbgs_sweep_v(View<float> v,
           out.y = rm1.y - (bm.y - lap) * idg;
         }
         {
-          const float sxs = rm1.z + r3, sys = yn.w + ys.w, szs = rm2.w + rc.w;
+          const float sxs = rm1.z + right, sys = yn.w + ys.w, szs = rm2.w + rc.w;
           const float lap = sxs * ex + sys * ey + szs * ez - dg * rm1.w;
           out.w = rm1.w - (bm.w - lap) * idg;
         }
       }
-      *reinterpret_cast<float4 *>(xnew + (int64_t)ke * sz + (int64_t)j * v.sy + i0 + 4 * lane) = out;
+      *reinterpret_cast<float4 *>(orow + (int64_t)ke * sz) = out;
     }
     // ---- rotate ----
     rm2 = rm1;
@@ -1351,9 +1344,6 @@ __global__ void __launch_bounds__(kVThreads, 2) k_rbgs_sweep_v(View<float> v,
     bm = bc;
     bc = bn;
     bn = bnext;
-    hm = hc;
-    hc = hp;
-    hp = hnext;
     ec = enext;
   }
 }
