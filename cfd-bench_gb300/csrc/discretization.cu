@@ -342,7 +342,7 @@ struct FluxArgsDF {
 };
 
 template <bool GRAVITY>
-__global__ void __launch_bounds__(kDX *kDY, 2) k_fgh_df(FluxArgsDF A, const double *__restrict__ u,
+__global__ void __launch_bounds__(kDX *kDY, 3) k_fgh_df(FluxArgsDF A, const double *__restrict__ u,
     const double *__restrict__ v, const double *__restrict__ w, double *__restrict__ f,
     double *__restrict__ gg, double *__restrict__ h)
 {
