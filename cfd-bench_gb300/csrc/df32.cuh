@@ -268,5 +268,41 @@ DF_FN f2 dot2(f2 a, f2 x, f2 b, f2 y)
   return renorm(s.hi, add_(add_(s.lo, add_(p.lo, q.lo)), cross));
 }
 
+// The same operations without the final renormalisation (an "unnormalised"
+// pair: hi + lo is the value, |lo| may exceed ulp(hi)/2). Safe where the result
+// only feeds further pair arithmetic -- two_sum and two_prod stay exact for any
+// inputs and the low parts' FP32 rounding stays a few 2^-47 of the operands --
+// and not where the sign of hi is read (an unnormalised hi can be 0 or carry the
+// wrong sign when the value is tiny).
+DF_FN f2 add_u(f2 a, f2 b)
+{
+  const f2 s = two_sum(a.hi, b.hi);
+  return f2{ s.hi, add_(s.lo, add_(a.lo, b.lo)) };
+}
+
+DF_FN f2 sub_u(f2 a, f2 b) { return add_u(a, neg(b)); }
+
+DF_FN f2 mul_u(f2 a, f2 b)
+{
+  const f2 p = two_prod(a.hi, b.hi);
+  return f2{ p.hi, add_(p.lo, fmaf_(a.hi, b.lo, mul_(a.lo, b.hi))) };
+}
+
+DF_FN f2 fma_u(f2 a, f2 b, f2 c)
+{
+  const f2 p = two_prod(a.hi, b.hi);
+  const f2 s = two_sum(p.hi, c.hi);
+  return f2{ s.hi, add_(add_(s.lo, p.lo), add_(c.lo, fmaf_(a.hi, b.lo, mul_(a.lo, b.hi)))) };
+}
+
+DF_FN f2 dot2_u(f2 a, f2 x, f2 b, f2 y)
+{
+  const f2 p = two_prod(a.hi, x.hi), q = two_prod(b.hi, y.hi);
+  const f2 s = two_sum(p.hi, q.hi);
+  const float cross =
+      fmaf_(a.hi, x.lo, fmaf_(a.lo, x.hi, fmaf_(b.hi, y.lo, mul_(b.lo, y.hi))));
+  return f2{ s.hi, add_(add_(s.lo, add_(p.lo, q.lo)), cross) };
+}
+
 }  // namespace df
 }  // namespace nusif

@@ -446,12 +446,14 @@ __global__ void __launch_bounds__(kDX *kDY, 3) k_fgh_df(FluxArgsDF A, const doub
       const int64_t c = (int64_t)k * sk + (int64_t)j * sj + i;
       const double uc = __ldg(u + c), vc = __ldg(v + c), wc = __ldg(w + c);
       // F(imax), G(jmax), H(kmax) are wall faces carrying the velocity (discretization.c:609-651)
-      const f2 sf = add(add(sub(xp.f, xm.f), sub(yp.f, ym.f)), sub(zp.f, zm.f));
+      // the flux sums stay unnormalised pairs (df32.cuh add_u): they only feed update()
+      const f2 sf = add_u(add_u(sub_u(xp.f, xm.f), sub_u(yp.f, ym.f)), sub_u(zp.f, zm.f));
       f[c] = (i == g.imax) ? uc : update(uc, sf, A.gx, mdt, GRAVITY);
       const f2 zc = g_zconv(A.az, zgp.gc, zgm.gc, V.c, V.z);
-      const f2 sg = add(add(add(sub(xp.g, xm.g), sub(yp.g, ym.g)), sub(zgp.gv, zgm.gv)), zc);
+      const f2 sg =
+          add_u(add_u(add_u(sub_u(xp.g, xm.g), sub_u(yp.g, ym.g)), sub_u(zgp.gv, zgm.gv)), zc);
       gg[c] = (j == g.jmax) ? vc : update(vc, sg, A.gy, mdt, GRAVITY);
-      const f2 sh = add(add(sub(xp.h, xm.h), sub(yp.h, ym.h)), sub(zp.h, zm.h));
+      const f2 sh = add_u(add_u(sub_u(xp.h, xm.h), sub_u(yp.h, ym.h)), sub_u(zp.h, zm.h));
       h[c] = (k == g.kmax) ? wc : update(wc, sh, A.gz, mdt, GRAVITY);
       // low wall faces F(0), G(0), H(0) carry the velocity (discretization.c:601-643)
       if (i == 1) f[c - 1] = __ldg(u + c - 1);

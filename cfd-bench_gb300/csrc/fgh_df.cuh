@@ -37,10 +37,10 @@ DF_FN AxisCoef axis_coef(double P, double M, double nu)
 // transported by the doubled velocity cp
 DF_FN f2 face_flux(const AxisCoef &a, f2 cp, f2 qa, f2 qb)
 {
-  const bool negative = f32_bits(cp.hi) >> 31;
-  const f2 A = fma(cp, negative ? a.M : a.P, a.nu);
-  const f2 B = fma(cp, negative ? a.P : a.M, a.mnu);
-  return dot2(A, qa, B, qb);
+  const bool negative = f32_bits(cp.hi) >> 31;  // cp is renormalised: hi carries the sign
+  const f2 A = fma_u(cp, negative ? a.M : a.P, a.nu);
+  const f2 B = fma_u(cp, negative ? a.P : a.M, a.mnu);
+  return dot2_u(A, qa, B, qb);
 }
 
 // the three components' fluxes across one x-, y- or z-face
@@ -84,7 +84,7 @@ DF_FN Face z_face(const AxisCoef &a, const Quad &u, const Quad &v, const Quad &w
   r.f = face_flux(a, add(w.c, w.x), u.c, u.z);
   r.h = face_flux(a, add(w.c, w.z), w.c, w.z);
   r.g = f2{ 0.0f, 0.0f };
-  gz.gv = mul(a.nu, sub(v.c, v.z));
+  gz.gv = mul_u(a.nu, sub_u(v.c, v.z));
   gz.gc = add(w.c, w.y);
   return r;
 }
@@ -95,16 +95,16 @@ DF_FN Face z_face(const AxisCoef &a, const Quad &u, const Quad &v, const Quad &w
 DF_FN f2 g_zconv(const AxisCoef &a, f2 gp, f2 gm, f2 vc, f2 vt)
 {
   const bool np = f32_bits(gp.hi) >> 31, nm = f32_bits(gm.hi) >> 31;
-  const f2 xp = dot2(np ? a.M : a.P, vc, np ? a.P : a.M, vt);
-  const f2 xm = dot2(nm ? a.P : a.M, vc, nm ? a.M : a.P, vt);
-  return dot2(gp, xp, neg(gm), xm);
+  const f2 xp = dot2_u(np ? a.M : a.P, vc, np ? a.P : a.M, vt);
+  const f2 xm = dot2_u(nm ? a.P : a.M, vc, nm ? a.M : a.P, vt);
+  return dot2_u(gp, xp, neg(gm), xm);
 }
 
 // q + dt * (g - s) as a binary64 number: the flux sum s and the gravity g as
 // pairs, q exact (mdt = -dt as a pair; two FP64 adds)
 DF_FN double update(double q, f2 s, f2 g, f2 mdt, bool gravity)
 {
-  const f2 t = gravity ? sub(s, g) : s;
+  const f2 t = gravity ? sub_u(s, g) : s;
   const f2 d = mul(t, mdt);
   return (q + widen(d.hi)) + widen(d.lo);
 }
