@@ -653,8 +653,13 @@ def kernel_rooflines(sim, solver, stream, ncell, arith: str = "df32"):
         abi.check(lib)
         if solver == "mg-mixed":
             # one whole red-black sweep: x read, b read, x written (FP32)
-            out.append(_roof("k_rbgs_sweep<float>: one fine FP32 red-black sweep (one kernel)",
-                             "k_rbgs_sweep", msr.value, 12.0 * ncell, ncell, peak, src))
+            i, j, _ = sim.dims
+            vec = i % 128 == 0 and j % 8 == 0  # the register-tiled kernel's levels
+            out.append(_roof("k_rbgs_sweep_v: one fine FP32 red-black sweep (register-tiled, one "
+                             "kernel)" if vec else
+                             "k_rbgs_sweep: one fine FP32 red-black sweep (one kernel)",
+                             "k_rbgs_sweep" if vec else "k_rbgs_sweep_tile64", msr.value,
+                             12.0 * ncell, ncell, peak, src))
             lib.nusifTimeKernel(C.byref(sim.s), sim.d.p, sim.d.rhs, 1, reps, C.byref(msr))
             abi.check(lib)
             # p and b read (FP64), the FP32 residual written and the FP32 correction zeroed
