@@ -122,6 +122,10 @@ struct MgHierarchy {
   // kernels per part of the graph (counted at capture): head, one outer unit
   // without its inner loop, one inner V-cycle, tail
   int n_head = 0, n_outer = 0, n_inner = 0, n_tail = 0;
+  // mg-mixed graph without nested loops: kernels of the unrolled prefix (always
+  // launched) and of one iteration of the loop that follows it
+  int n_prefix = 0, n_body = 0;
+  bool unrolled = false;
   int n_inner_capture = 0;  // scratch while capturing
   bool mx_df = true;  // mg-mixed: fine residual in double-float arithmetic (key arith)
   double *h_ptrs[2 * kMaxLevels] = {};  // exposed through Solver::r / Solver::e
@@ -624,19 +628,21 @@ __global__ void __launch_bounds__(kNT, 4) k_mx_residual_df(View<double> f, DfSte
         if (ring) rn = x[pk + f.sz + roff];
       }
       __syncthreads();
-      const f2 sx = add(pl[buf][ty + 1][tx], pl[buf][ty + 1][tx + 2]);
-      const f2 sy = add(pl[buf][ty][tx + 1], pl[buf][ty + 2][tx + 1]);
-      const f2 sz = add(zb, zt);
-      f2 t = fma(mdiag, zc, sh);
-      t = fma(sx, ex, t);
-      t = fma(sy, ey, t);
-      t = fma(sz, ez, t);
+      // unnormalised pairs inside the stencil (only pair arithmetic follows),
+      // the residual itself renormalised (its hi is the FP32 copy)
+      const f2 sx = add_u(pl[buf][ty + 1][tx], pl[buf][ty + 1][tx + 2]);
+      const f2 sy = add_u(pl[buf][ty][tx + 1], pl[buf][ty + 2][tx + 1]);
+      const f2 sz = add_u(zb, zt);
+      f2 t = fma_u(mdiag, zc, sh);
+      t = fma_u(sx, ex, t);
+      t = fma_u(sy, ey, t);
+      t = fma_u(sz, ez, t);
       const f2 r = sub(split(bv), t);
       if (active) {
         const int64_t q = ((int64_t)k * f.ny + j) * f.nx + i;
         r32[q] = r.hi;  // the pair is renormalised: hi is its value rounded to FP32
         if (e_zero) e_zero[q] = 0.0f;
-        acc = add(acc, mul(r, r));
+        acc = add(acc, mul_u(r, r));
       }
       zb = zc;
       zc = zt;
@@ -1638,17 +1644,32 @@ __device__ void open_solve(MgState *st, double nb2)
 // side has mean ~0); when shift * sum b exceeds half of sum b^2 it raises
 // need_norm instead, and k_mg_rhs_norm computes the norm about the mean in a
 // second pass.
+// DF: the per-thread sums of b and b^2 as double-float pairs (df32.cuh) on the
+// FP32 pipe instead of two FP64 instructions per cell; the block and grid folds
+// stay in FP64.
+template <bool DF>
 __global__ void __launch_bounds__(kNT) k_mg_rhs_stats(View<double> f, MgState *st,
     double *partials, double *partials2, unsigned *ticket)
 {
   const int64_t n = (int64_t)f.nx * f.ny * f.nz;
   double acc = 0.0, acc2 = 0.0;
+  df::f2 s1{ 0.0f, 0.0f }, s2{ 0.0f, 0.0f };
   const int64_t q0 = blockIdx.x * (int64_t)kNT + threadIdx.x, stride = (int64_t)gridDim.x * kNT;
   FlatWalk w(q0, stride, f.nx, f.ny);
   for (int64_t q = q0; q < n; q += stride, w.advance(f.nx, f.ny)) {
     const double b = f.b[f.off + (int64_t)w.k * f.sz + (int64_t)w.j * f.sy + w.i];
-    acc += b;
-    acc2 = fma(b, b, acc2);
+    if constexpr (DF) {
+      const df::f2 bp = df::split(b);
+      s1 = df::add(s1, bp);
+      s2 = df::add(s2, df::mul_u(bp, bp));
+    } else {
+      acc += b;
+      acc2 = fma(b, b, acc2);
+    }
+  }
+  if constexpr (DF) {
+    acc = df::to_double(s1);
+    acc2 = df::to_double(s2);
   }
   __shared__ double sm[kNT / 32];
   acc = block_reduce_sum<kNT>(acc, sm);
@@ -2283,34 +2304,38 @@ bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero, bool inner_test)
 
 // initial guess by extrapolation in time (whole padded arrays, ghosts
 // included): linear p <- 2 p(n-1) - p(n-2), or (quadratic, once two earlier
-// solutions exist) p <- 3 p(n-1) - 3 p(n-2) + p(n-3); the history shifts by
-// one. *hist counts the earlier solutions kept (0, 1, 2) on the device, so the
-// same launches serve host-driven and graph-captured steps.
-__global__ void k_extrapolate(double *__restrict__ p, double *__restrict__ p_prev,
-    double *__restrict__ p2, int64_t n, const int *hist, int quadratic)
+// solutions exist) p <- 3 p(n-1) - 3 p(n-2) + p(n-3). hist[0] counts the
+// earlier solutions kept (0, 1, 2) on the device, so the same launches serve
+// host-driven and graph-captured steps. The quadratic history lives in two
+// buffers whose roles alternate (hist[1]): buf[par] holds p(n-2), buf[par ^ 1]
+// p(n-3), which this step overwrites with p(n-1) -- the next step's p(n-2) --
+// so no history value is copied (40 bytes per cell instead of 48). The linear
+// history is one buffer updated in place.
+__global__ void k_extrapolate(double *__restrict__ p, double *buf0, double *buf1, int64_t n,
+    const int *hist, int quadratic)
 {
-  const int h = *hist;
+  const int h = hist[0], par = quadratic ? hist[1] : 0;
+  // linear: a and b are the same buffer (each cell read, then written)
+  const double *a = par ? buf1 : buf0;                  // p(n-2)
+  double *b = quadratic ? (par ? buf0 : buf1) : buf0;   // p(n-3), then p(n-1)
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x) {
     const double cur = p[q];
-    if (h == 0) {
-      p_prev[q] = cur;
-      continue;
+    if (h >= 1) {
+      const double prev = a[q];
+      if (quadratic && h >= 2)
+        p[q] = 3.0 * (cur - prev) + b[q];
+      else
+        p[q] = 2.0 * cur - prev;
     }
-    const double prev = p_prev[q];
-    if (quadratic && h >= 2) {
-      p[q] = 3.0 * (cur - prev) + p2[q];
-    } else {
-      p[q] = 2.0 * cur - prev;
-    }
-    if (quadratic) p2[q] = prev;
-    p_prev[q] = cur;
+    b[q] = cur;
   }
 }
 
-__global__ void k_hist_advance(int *hist)
+__global__ void k_hist_advance(int *hist, int quadratic)
 {
-  if (*hist < 2) *hist += 1;
+  if (hist[0] < 2) hist[0] += 1;
+  if (quadratic) hist[1] ^= 1;
 }
 
 __global__ void k_mx_fold(View<float> e, double *p, int p_sj, int p_sk, const MgState *st)
@@ -2332,6 +2357,56 @@ __global__ void k_mx_fold(View<float> e, double *p, int p_sj, int p_sk, const Mg
     if (k == 0) p[pc - p_sk] = np;
     if (k == e.nz - 1) p[pc + p_sk] = np;
   }
+}
+
+// The same fold four cells at a time (rows a multiple of 4 cells): one
+// 16-byte load of e and four independent loads of p per thread and step, so
+// more of each thread's memory accesses are in flight.
+__global__ void __launch_bounds__(kNT) k_mx_fold4(View<float> e, double *__restrict__ p,
+    int p_sj, int p_sk, const MgState *st)
+{
+  if (solve_finished(st)) return;
+  const int nq = e.nx / 4;
+  const int64_t n = (int64_t)nq * e.ny * e.nz;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = g / nq;
+    const int i = 4 * (int)(g - row * nq);
+    const int j = (int)(row % e.ny), k = (int)(row / e.ny);
+    const float4 ev = *reinterpret_cast<const float4 *>(e.x + row * e.nx + i);
+    double *pp = p + (int64_t)(k + 1) * p_sk + (int64_t)(j + 1) * p_sj + (i + 1);
+    const double a0 = pp[0], a1 = pp[1], a2 = pp[2], a3 = pp[3];
+    const double n0 = a0 + to_f64(ev.x), n1 = a1 + to_f64(ev.y), n2 = a2 + to_f64(ev.z),
+                 n3 = a3 + to_f64(ev.w);
+    pp[0] = n0;
+    pp[1] = n1;
+    pp[2] = n2;
+    pp[3] = n3;
+    if (i == 0) pp[-1] = n0;
+    if (i + 4 == e.nx) pp[4] = n3;
+    const bool jl = j == 0, jh = j == e.ny - 1, kl = k == 0, kh = k == e.nz - 1;
+    if (jl || jh || kl || kh) {
+      const double nv[4] = { n0, n1, n2, n3 };
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (jl) pp[q - p_sj] = nv[q];
+        if (jh) pp[q + p_sj] = nv[q];
+        if (kl) pp[q - p_sk] = nv[q];
+        if (kh) pp[q + p_sk] = nv[q];
+      }
+    }
+  }
+}
+
+bool launch_fold(const View<float> &e, double *p, int p_sj, int p_sk, const MgState *st)
+{
+  const int64_t n = (int64_t)e.nx * e.ny * e.nz;
+  if (e.nx % 4 == 0) {
+    k_mx_fold4<<<flat_blocks(n / 4), kNT, 0, stream()>>>(e, p, p_sj, p_sk, st);
+    return launched("k_mx_fold4");
+  }
+  k_mx_fold<<<flat_blocks(n), kNT, 0, stream()>>>(e, p, p_sj, p_sk, st);
+  return launched("k_mx_fold");
 }
 
 bool cycle_fp64(MgHierarchy *H, double *p, const double *rhs)
@@ -2358,14 +2433,12 @@ bool cycle_mixed(MgHierarchy *H, double *p, const double *rhs)
 {
   MgState *st = H->d_state;
   View<double> v0 = padded_view(H->lv[0], p, rhs);
-  const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
   if (!mx_residual(H, v0, st, H->nl == 1 ? 1 : 0, nullptr)) return false;
   const int inner = H->nl == 1 ? 1 : H->inner;
   for (int q = 0; q < inner; q++)
     if (!vcycle<float>(H, 0, H->x32, H->b32, q == 0, true)) return false;
   View<float> e = compact_view<float>(H->lv[0], H->x32[0], H->b32[0]);
-  k_mx_fold<<<flat_blocks(n0), kNT, 0, stream()>>>(e, p, v0.sy, v0.sz, st);
-  return launched("k_mx_fold");
+  return launch_fold(e, p, v0.sy, v0.sz, st);
 }
 
 }  // namespace
@@ -2395,8 +2468,8 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
     if (!cuda_ok(cudaMalloc(&H->p_prev, padded), "cudaMalloc(p_prev)")) return false;
     if (H->guess == 2 && !cuda_ok(cudaMalloc(&H->p_prev2, padded), "cudaMalloc(p_prev2)"))
       return false;
-    if (!cuda_ok(cudaMalloc(&H->d_hist, sizeof(int)), "cudaMalloc(hist)") ||
-        !cuda_ok(cudaMemset(H->d_hist, 0, sizeof(int)), "hist init"))
+    if (!cuda_ok(cudaMalloc(&H->d_hist, 2 * sizeof(int)), "cudaMalloc(hist)") ||
+        !cuda_ok(cudaMemset(H->d_hist, 0, 2 * sizeof(int)), "hist init"))
       return false;
   }
   H->rtol = x.rtol;
@@ -2533,6 +2606,13 @@ __global__ void k_inner_continue(MgState *st, cudaGraphConditionalHandle h, int 
   cudaGraphSetConditional(h, (st->done == 0 && st->inner_done == 0 && n < inner) ? 1u : 0u);
 }
 
+// before the units loop that follows an unrolled prefix: enter it while the
+// solve is open
+__global__ void k_loop_open(const MgState *st, cudaGraphConditionalHandle h)
+{
+  cudaGraphSetConditional(h, st->done == 0 ? 1u : 0u);
+}
+
 // the extrapolated warm start of p (mg_guess 1 / 2), before the solve
 bool enqueue_warm_start(MgHierarchy *H, const View<double> &v0, double *p)
 {
@@ -2541,7 +2621,7 @@ bool enqueue_warm_start(MgHierarchy *H, const View<double> &v0, double *p)
   k_extrapolate<<<flat_blocks(padded), kNT, 0, stream()>>>(p, H->p_prev, H->p_prev2, padded,
       H->d_hist, H->guess == 2 ? 1 : 0);
   if (!launched("k_extrapolate")) return false;
-  k_hist_advance<<<1, 1, 0, stream()>>>(H->d_hist);
+  k_hist_advance<<<1, 1, 0, stream()>>>(H->d_hist, H->guess == 2 ? 1 : 0);
   return launched("k_hist_advance");
 }
 
@@ -2552,7 +2632,8 @@ bool enqueue_solve_head(MgHierarchy *H, const View<double> &v0)
   if (!launched("k_mg_state_init")) return false;
   const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
   const int blocks = flat_blocks(n0);
-  k_mg_rhs_stats<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->stats2,
+  (H->mx_df ? k_mg_rhs_stats<true> : k_mg_rhs_stats<false>)<<<blocks, kNT, 0, stream()>>>(
+      v0, H->d_state, H->red.partials, H->stats2,
       H->red.ticket);
   if (!launched("k_mg_rhs_stats")) return false;
   k_mg_rhs_norm<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);
@@ -2626,7 +2707,6 @@ bool cycle_mixed_nested(MgHierarchy *H, double *p, const double *rhs, cudaStream
 {
   MgState *st = H->d_state;
   View<double> v0 = padded_view(H->lv[0], p, rhs);
-  const int64_t n0 = (int64_t)v0.nx * v0.ny * v0.nz;
   if (!mx_residual(H, v0, st, 0, H->x32[0])) return false;
   cudaStream_t s = stream();
   cudaGraphConditionalHandle h;
@@ -2643,8 +2723,46 @@ bool cycle_mixed_nested(MgHierarchy *H, double *p, const double *rhs, cudaStream
     return false;
   H->n_inner_capture = (int)(launch_count() - c0);
   View<float> e = compact_view<float>(H->lv[0], H->x32[0], H->b32[0]);
-  k_mx_fold<<<flat_blocks(n0), kNT, 0, stream()>>>(e, p, v0.sy, v0.sz, st);
-  return launched("k_mx_fold");
+  return launch_fold(e, p, v0.sy, v0.sz, st);
+}
+
+// mg-mixed without nested while-loops: a graph's conditional nodes cost tens
+// of microseconds per evaluation, about a sixth of an FP32 V-cycle, so the
+// common solve -- one refinement step of mg_inner V-cycles, then the FP64-class
+// residual that finds it converged -- runs as straight-line launches: residual,
+// mg_inner V-cycles (each stops at once when the correction has met its target
+// or the solve is done; the first starts from the zeroed correction with the
+// zero-start sweep), fold, residual. Only if that residual finds the solve
+// still open does a while-loop of further refinement steps (the same launches
+// and its own residual) run. The sequence is the host-driven cycle_mixed's,
+// kernel for kernel, so the results are the same bits.
+bool enqueue_mixed_unrolled(MgHierarchy *H, double *p, const double *rhs, cudaStream_t body)
+{
+  MgState *st = H->d_state;
+  View<double> v0 = padded_view(H->lv[0], p, rhs);
+  View<float> e = compact_view<float>(H->lv[0], H->x32[0], H->b32[0]);
+  const auto unit = [&]() {
+    for (int q = 0; q < H->inner; q++)
+      if (!vcycle<float>(H, 0, H->x32, H->b32, q == 0, true)) return false;
+    return launch_fold(e, p, v0.sy, v0.sz, st) && mx_residual(H, v0, st, 0, H->x32[0]);
+  };
+  const unsigned long long c0 = launch_count();
+  if (!mx_residual(H, v0, st, 0, H->x32[0]) || !unit()) return false;
+  cudaStream_t s = stream();
+  cudaGraphConditionalHandle h;
+  if (!make_handle(s, 0, 0, &h)) return false;
+  k_loop_open<<<1, 1, 0, s>>>(st, h);
+  if (!launched("k_loop_open")) return false;
+  H->n_prefix = (int)(launch_count() - c0);
+  const unsigned long long c1 = launch_count();
+  const bool ok = capture_while(s, body, h, [&] {
+    if (!unit()) return false;
+    k_mg_continue<<<1, 1, 0, stream()>>>(st, h, H->maxcycles + 2);
+    return launched("k_mg_continue");
+  });
+  H->n_body = (int)(launch_count() - c1);
+  H->unrolled = ok;
+  return ok;
 }
 
 // The solve's units as a while-loop of the graph captured on the library
@@ -2655,6 +2773,8 @@ bool cycle_mixed_nested(MgHierarchy *H, double *p, const double *rhs, cudaStream
 bool enqueue_units_loop(MgHierarchy *H, double *p, const double *rhs, cudaStream_t outer_body,
     cudaStream_t inner_body)
 {
+  if (H->mode == 1 && H->nl > 1) return enqueue_mixed_unrolled(H, p, rhs, outer_body);
+  H->unrolled = false;
   cudaStream_t s = stream();
   cudaGraphConditionalHandle h;
   if (!make_handle(s, 1, cudaGraphCondAssignDefault, &h)) return false;
@@ -2782,9 +2902,12 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
         !cuda_ok(cudaStreamSynchronize(stream()), "mg sync"))
       return NAN;
     // the kernels the graph ran: head, outer units, inner V-cycles, tail
-    const bool nested = H->mode == 1 && H->nl > 1;
-    set_launch_count(launch_count() + H->n_head + (unsigned long long)h->loops * H->n_outer +
-                     (nested ? (unsigned long long)h->cycles * H->n_inner : 0ull) + H->n_tail);
+    if (H->unrolled)
+      set_launch_count(launch_count() + H->n_head + H->n_prefix +
+                       (unsigned long long)h->loops * H->n_body + H->n_tail);
+    else
+      set_launch_count(launch_count() + H->n_head + (unsigned long long)h->loops * H->n_outer +
+                       H->n_tail);
   } else {
     memset(h, 0, sizeof(*h));
     h->rtol2 = H->rtol * H->rtol;
@@ -2794,7 +2917,8 @@ double mg_solve(Solver *s, SolverState *ss, double *p, const double *rhs)
                      stream()),
             "mg state upload"))
       return NAN;
-    k_mg_rhs_stats<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->stats2,
+    (H->mx_df ? k_mg_rhs_stats<true> : k_mg_rhs_stats<false>)<<<blocks, kNT, 0, stream()>>>(
+        v0, H->d_state, H->red.partials, H->stats2,
         H->red.ticket);
     if (!launched("k_mg_rhs_stats")) return NAN;
     k_mg_rhs_norm<<<blocks, kNT, 0, stream()>>>(v0, H->d_state, H->red.partials, H->red.ticket);

@@ -103,14 +103,15 @@ __global__ void __launch_bounds__(kNT) k_sor_pass(SorArgs A, int colour, double 
         const double pc = cur.c;
         if constexpr (DF) {
           using namespace df;
-          f2 lap = mul(A.pmdiag, split(pc));
-          lap = fma(add(split(cur.w), split(cur.e)), A.pidx2, lap);
-          lap = fma(add(split(cur.s), split(cur.n)), A.pidy2, lap);
-          lap = fma(add(split(cur.b), split(cur.t)), A.pidz2, lap);
+          // unnormalised pairs inside the stencil, r renormalised
+          f2 lap = mul_u(A.pmdiag, split(pc));
+          lap = fma_u(add_u(split(cur.w), split(cur.e)), A.pidx2, lap);
+          lap = fma_u(add_u(split(cur.s), split(cur.n)), A.pidy2, lap);
+          lap = fma_u(add_u(split(cur.b), split(cur.t)), A.pidz2, lap);
           const f2 r = sub(split(cur.r), lap);
-          const f2 d = mul(A.pmfactor, r);
+          const f2 d = mul_u(A.pmfactor, r);
           p[c] = (pc + widen(d.hi)) + widen(d.lo);
-          if (ACCUM) acc2 = add(acc2, mul(r, r));
+          if (ACCUM) acc2 = add(acc2, mul_u(r, r));
         } else {
           const double lap = (cur.w + cur.e) * A.idx2 + (cur.s + cur.n) * A.idy2 +
                              (cur.b + cur.t) * A.idz2 - A.diag * pc;

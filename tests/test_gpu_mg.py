@@ -211,6 +211,32 @@ def test_mg_extrapolated_guess(nusif_lib, solver, guess):
         assert rel_err(fields[guess][f], fields["previous"][f]) < 1e-5, f
 
 
+@pytest.mark.parametrize("guess", ["extrapolate", "quadratic"])
+def test_warm_start_values(nusif_lib, guess):
+    """The warm start itself: with rtol 1e30 a solve stops after its first
+    residual, so p after solve() is the extrapolated start. Four solves from
+    pressures A, B, C, D give A, 2B - A, then 3C - 3B + A and 3D - 3C + B
+    (quadratic; the history buffers alternate roles) or 2C - B and 2D - C
+    (linear), over the whole interior."""
+    rng = np.random.default_rng(43)
+    with _sim((24, 16, 12), "mg-mixed", 1e30, mg_guess=guess) as sim:
+        shape = sim.padded_shape
+        pres = [rng.standard_normal(shape) for _ in range(4)]
+        sim.set_field("rhs", rng.standard_normal(shape))
+        got = []
+        for q in range(4):
+            sim.set_field("p", pres[q])
+            sim.solve()
+            got.append(sim.field("p")[1:-1, 1:-1, 1:-1])
+        A, B, C, D = (x[1:-1, 1:-1, 1:-1] for x in pres)
+        if guess == "quadratic":
+            want = [A, 2 * B - A, 3 * (C - B) + A, 3 * (D - C) + B]
+        else:
+            want = [A, 2 * B - A, 2 * C - B, 2 * D - C]
+        for q in range(4):
+            assert rel_err(got[q], want[q]) < 1e-15, q
+
+
 def _rb_sweep_f32(x, b, h):
     """Two-pass red-black Gauss-Seidel (first colour (i+j+k) even, 0-based),
     ghost-free Neumann operator, float32 with float64 sums (numpy)."""
