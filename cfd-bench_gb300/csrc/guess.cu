@@ -18,6 +18,8 @@
 // Every reduction folds per-block partials in a fixed order (deterministic).
 #include <cmath>
 
+#include "df32.cuh"
+#include "fp_bits.cuh"
 #include "nusif_internal.h"
 #include "reduce.cuh"
 #include "solver_internal.h"
@@ -73,17 +75,51 @@ struct GGeom {
   }
 };
 
-// b - s - A p at fine interior cell (i, j, k), Neumann operator without ghosts
-__device__ __forceinline__ double resid(const GGeom &g, const double *p, const double *b,
-    double s, int i, int j, int k)
+// b - s - A p at fine interior cell (i, j, k), Neumann operator without
+// ghosts, in double-float pairs (about 2^-47 of the operands) on the FP32
+// pipe; nb = the pair of b - s at the cell
+struct GPairs {
+  df::f2 ex, ey, ez, ms;  // 1/h^2 per axis, -s
+};
+
+__device__ __forceinline__ df::f2 resid_df(const GGeom &g, const GPairs &c, const double *p,
+    const double *b, int i, int j, int k, df::f2 &nb)
 {
-  const int64_t c = g.pidx(i, j, k);
-  const double xc = p[c];
-  const double sx = (i > 0 ? p[c - 1] : xc) + (i < g.nx - 1 ? p[c + 1] : xc);
-  const double sy = (j > 0 ? p[c - g.sj] : xc) + (j < g.ny - 1 ? p[c + g.sj] : xc);
-  const double sz = (k > 0 ? p[c - g.sk] : xc) + (k < g.nz - 1 ? p[c + g.sk] : xc);
-  const double lap = g.ex * (sx - 2.0 * xc) + g.ey * (sy - 2.0 * xc) + g.ez * (sz - 2.0 * xc);
-  return (b[c] - s) - lap;
+  using namespace df;
+  const int64_t q = g.pidx(i, j, k);
+  const f2 xc = split(p[q]);
+  const f2 x2 = f2{ 2.0f * xc.hi, 2.0f * xc.lo };  // exact
+  const f2 xw = i > 0 ? split(p[q - 1]) : xc, xe = i < g.nx - 1 ? split(p[q + 1]) : xc;
+  const f2 xs = j > 0 ? split(p[q - g.sj]) : xc, xn = j < g.ny - 1 ? split(p[q + g.sj]) : xc;
+  const f2 xb = k > 0 ? split(p[q - g.sk]) : xc, xt = k < g.nz - 1 ? split(p[q + g.sk]) : xc;
+  f2 lap = mul_u(c.ex, sub_u(add_u(xw, xe), x2));
+  lap = fma_u(c.ey, sub_u(add_u(xs, xn), x2), lap);
+  lap = fma_u(c.ez, sub_u(add_u(xb, xt), x2), lap);
+  nb = add(split(b[q]), c.ms);
+  return sub(nb, lap);
+}
+
+// the features of one coarse cell: 8 children's residuals and b - s, their
+// means (pairs) and the sums of their squares (FP32 over the 8 children)
+__device__ __forceinline__ void coarse_features(const GGeom &g, const GPairs &c, const double *p,
+    const double *b, int I, int J, int K, df::f2 &rs, df::f2 &bs, float &rr2, float &bb2)
+{
+  using namespace df;
+  rs = f2{ 0.0f, 0.0f };
+  bs = f2{ 0.0f, 0.0f };
+  rr2 = 0.0f;
+  bb2 = 0.0f;
+#pragma unroll
+  for (int ch = 0; ch < 8; ch++) {
+    f2 nb;
+    const f2 rr = resid_df(g, c, p, b, 2 * I + (ch & 1), 2 * J + ((ch >> 1) & 1), 2 * K + (ch >> 2), nb);
+    rs = add(rs, rr);
+    bs = add(bs, nb);
+    rr2 = fmaf_(rr.hi, rr.hi, rr2);
+    bb2 = fmaf_(nb.hi, nb.hi, bb2);
+  }
+  rs = f2{ 0.125f * rs.hi, 0.125f * rs.lo };
+  bs = f2{ 0.125f * bs.hi, 0.125f * bs.lo };
 }
 
 template <int K>
@@ -117,34 +153,30 @@ __global__ void k_g_fold_shift(const double *partial, int nb, int64_t n, GuessSt
 }
 
 // one thread per coarse cell: restricted residual and rhs (unnormalised) into
-// x, and the four sums of squares
-__global__ void __launch_bounds__(kNT) k_g_features(GGeom g, const double *p, const double *b,
-    const GuessStats *st, float *x, double *partial)
+// x, and the four sums of squares; the residuals in double-float pairs (the
+// warm start's residual cancels b - A p to a small fraction of b), the squares
+// in FP32 over a coarse cell's children, then in FP64
+__global__ void __launch_bounds__(kNT) k_g_features(GGeom g, GPairs pc, const double *p,
+    const double *b, const GuessStats *st, float *x, double *partial)
 {
   const int cx = g.nx / 2, cy = g.ny / 2, cz = g.nz / 2;
   const int64_t n = (int64_t)cx * cy * cz;
-  const double s = st->shift;
+  GPairs c = pc;
+  c.ms = df::split(-st->shift);
   double v[4] = { 0.0, 0.0, 0.0, 0.0 };
   for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n; q += (int64_t)gridDim.x * kNT) {
     const int I = (int)(q % cx);
     const int64_t r = q / cx;
     const int J = (int)(r % cy), K = (int)(r / cy);
-    double rs = 0.0, bs = 0.0;
-    for (int c = 0; c < 8; c++) {
-      const int i = 2 * I + (c & 1), j = 2 * J + ((c >> 1) & 1), k = 2 * K + (c >> 2);
-      const double rr = resid(g, p, b, s, i, j, k);
-      const double bb = b[g.pidx(i, j, k)] - s;
-      rs += rr;
-      bs += bb;
-      v[0] += rr * rr;
-      v[1] += bb * bb;
-    }
-    rs *= 0.125;
-    bs *= 0.125;
-    v[2] += rs * rs;
-    v[3] += bs * bs;
-    x[2 * q] = (float)rs;
-    x[2 * q + 1] = (float)bs;
+    df::f2 rs, bs;
+    float rr2, bb2;
+    coarse_features(g, c, p, b, I, J, K, rs, bs, rr2, bb2);
+    v[0] += to_f64(rr2);
+    v[1] += to_f64(bb2);
+    v[2] += to_f64(rs.hi * rs.hi);
+    v[3] += to_f64(bs.hi * bs.hi);
+    x[2 * q] = rs.hi;
+    x[2 * q + 1] = bs.hi;
   }
   block_partials<4>(v, partial);
 }
@@ -198,13 +230,15 @@ __global__ void k_g_target(GGeom g, const double *pconv, const double *p0, const
 
 // p1 = p0 + P(out * sigma_r / kappa) on the interior, Neumann ghosts from it;
 // trilinear weights 3/4 and 1/4 toward the coarse neighbour on the fine
-// cell's side (clamped at the walls), as the multigrid prolongation
+// cell's side (clamped at the walls), as the multigrid prolongation. The
+// correction is interpolated in FP32 (the network's output is BF16-rounded)
+// and added to the binary64 p0 in one FP64 addition.
 __global__ void k_g_candidate(GGeom g, const double *p0, const float *out, const GuessStats *st,
     double *p1)
 {
   const int cx = g.nx / 2, cy = g.ny / 2, cz = g.nz / 2;
   const int64_t n = (int64_t)g.nx * g.ny * g.nz;
-  const double scale = st->sigma_r / g.kappa;
+  const float scale = (float)(st->sigma_r / g.kappa);
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(q % g.nx);
@@ -218,14 +252,15 @@ __global__ void k_g_candidate(GGeom g, const double *p0, const float *out, const
       const int nb = (F[a] & 1) ? P[a] + 1 : P[a] - 1;
       Q[a] = (nb < 0 || nb >= C[a]) ? P[a] : nb;
     }
-    double e = 0.0;
+    float e = 0.0f;
+#pragma unroll
     for (int c = 0; c < 8; c++) {
       const int X = (c & 1) ? Q[0] : P[0], Y = ((c >> 1) & 1) ? Q[1] : P[1], Z = (c >> 2) ? Q[2] : P[2];
-      const double w = ((c & 1) ? 0.25 : 0.75) * (((c >> 1) & 1) ? 0.25 : 0.75) * ((c >> 2) ? 0.25 : 0.75);
-      e += w * (double)out[((int64_t)Z * cy + Y) * cx + X];
+      const float w = ((c & 1) ? 0.25f : 0.75f) * (((c >> 1) & 1) ? 0.25f : 0.75f) * ((c >> 2) ? 0.25f : 0.75f);
+      e = fmaf(w, out[((int64_t)Z * cy + Y) * cx + X], e);
     }
     const int64_t pc = g.pidx(i, j, k);
-    const double v = p0[pc] + e * scale;
+    const double v = p0[pc] + to_f64(e * scale);
     p1[pc] = v;
     if (i == 0) p1[pc - 1] = v;
     if (i == g.nx - 1) p1[pc + 1] = v;
@@ -236,28 +271,26 @@ __global__ void k_g_candidate(GGeom g, const double *p0, const float *out, const
   }
 }
 
-// ||b - s - A p1||^2 summed in exactly the order k_g_features sums p0's (same
-// grid, same per-thread walk over coarse cells and children), so that p1 == p0
-// gives the same number bit for bit
-__global__ void __launch_bounds__(kNT) k_g_cand_norm(GGeom g, const double *p1, const double *b,
-    const GuessStats *st, double *partial)
+// ||b - s - A p1||^2 with the very arithmetic and summation order of
+// k_g_features (same grid, same per-thread walk over coarse cells and
+// children), so that p1 == p0 gives the same numbers bit for bit
+__global__ void __launch_bounds__(kNT) k_g_cand_norm(GGeom g, GPairs pc, const double *p1,
+    const double *b, const GuessStats *st, double *partial)
 {
   const int cx = g.nx / 2, cy = g.ny / 2, cz = g.nz / 2;
   const int64_t n = (int64_t)cx * cy * cz;
-  const double s = st->shift;
+  GPairs c = pc;
+  c.ms = df::split(-st->shift);
   double v[2] = { 0.0, 0.0 };
   for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n; q += (int64_t)gridDim.x * kNT) {
     const int I = (int)(q % cx);
     const int64_t r = q / cx;
     const int J = (int)(r % cy), K = (int)(r / cy);
-    double rs = 0.0;
-    for (int c = 0; c < 8; c++) {
-      const double rr = resid(g, p1, b, s, 2 * I + (c & 1), 2 * J + ((c >> 1) & 1), 2 * K + (c >> 2));
-      rs += rr;
-      v[0] += rr * rr;
-    }
-    rs *= 0.125;
-    v[1] += rs * rs;
+    df::f2 rs, bs;
+    float rr2, bb2;
+    coarse_features(g, c, p1, b, I, J, K, rs, bs, rr2, bb2);
+    v[0] += to_f64(rr2);
+    v[1] += to_f64(rs.hi * rs.hi);
   }
   block_partials<2>(v, partial);
 }
@@ -284,6 +317,17 @@ __global__ void k_g_take(double *p, const double *p1, int64_t n, const GuessStat
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x)
     p[q] = p1[q];
+}
+
+// the operator's constants as pairs, formed on the host
+GPairs gpairs(const GGeom &g)
+{
+  GPairs c;
+  c.ex = df::from_double_rn(g.ex);
+  c.ey = df::from_double_rn(g.ey);
+  c.ez = df::from_double_rn(g.ez);
+  c.ms = df::f2{ 0.0f, 0.0f };  // -shift, filled in on the device
+  return c;
 }
 
 GGeom geom(const Grid *grid)
@@ -343,7 +387,7 @@ bool features(GuessState *gs, const GGeom &g, const double *p, const double *rhs
   k_g_fold_shift<<<1, 1, 0, stream()>>>(gs->partial, nb, n, gs->d_stats);
   if (!launched("k_g_fold_shift")) return false;
   const int nbc = flat(gs->nc);
-  k_g_features<<<nbc, kNT, 0, stream()>>>(g, p, rhs, gs->d_stats, x, gs->partial);
+  k_g_features<<<nbc, kNT, 0, stream()>>>(g, gpairs(g), p, rhs, gs->d_stats, x, gs->partial);
   if (!launched("k_g_features")) return false;
   k_g_fold_features<<<1, 1, 0, stream()>>>(gs->partial, nbc, gs->nc, gs->d_stats);
   if (!launched("k_g_fold_features")) return false;
@@ -378,7 +422,7 @@ bool guess_before_solve(GuessState *gs, const Grid *grid, double *p, const doubl
   k_g_candidate<<<flat(n), 256, 0, stream()>>>(g, p, out, gs->d_stats, gs->aux);
   if (!launched("k_g_candidate")) return false;
   const int nb = flat(gs->nc);  // the features' grid (same summation order)
-  k_g_cand_norm<<<nb, kNT, 0, stream()>>>(g, gs->aux, rhs, gs->d_stats, gs->partial);
+  k_g_cand_norm<<<nb, kNT, 0, stream()>>>(g, gpairs(g), gs->aux, rhs, gs->d_stats, gs->partial);
   if (!launched("k_g_cand_norm")) return false;
   k_g_fold_select<<<1, 1, 0, stream()>>>(gs->partial, nb, gs->d_stats);
   if (!launched("k_g_fold_select")) return false;
