@@ -202,7 +202,8 @@ def bench_case(n: int, solver: str, itermax: int | None = None,
                graph: bool = True, arith: str = "df32") -> dict:
     from nusif.params import config2
     vals = config2(solver=solver)
-    vals.update(imax=n, jmax=n, kmax=n, arith=arith)
+    # fuse_dt: adaptUV keeps its velocity maxima, computeTimestep reads the ghost shell
+    vals.update(imax=n, jmax=n, kmax=n, arith=arith, fuse_dt=1)
     if itermax is not None:
         vals["itermax"] = itermax
     if solver in ("mg", "mg-mixed"):
@@ -402,6 +403,7 @@ def run_gpu(args, rank, world, local):
                              else "all FP64 stencils in FP64 instructions"),
                    "solve_launch": ("host-driven launches" if args.no_graph else
                                     "one CUDA graph per solve (device while-loops)"),
+                   "cfl_maxima": "fuse_dt 1: from adaptUV's output plus the ghost shell",
                    "l2": "no flush: 8 FP64 fields of %.0f MB each, far larger than L2" % (padded * 8 / 1e6),
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "solver_iterations_per_step": head["iters"],

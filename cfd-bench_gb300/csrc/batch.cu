@@ -279,6 +279,7 @@ int nusifBatchStep(NusifBatch *B, int steps)
   }
   // the batch runs on its own streams: queued field copies end first
   if (nusifWaitCopies() != NUSIF_OK) return NUSIF_ERR_CUDA;
+  for (auto &in : B->inst) velocity_written(disc_state(&in->d));
   for (int q = 0; q < steps; q++) {
     cudaGraphExec_t ex = B->exec[B->nt % 100 == 0 ? 1 : 0];
     if (!cuda_ok(cudaGraphLaunch(ex, B->main), "graph launch")) return NUSIF_ERR_CUDA;

@@ -6,6 +6,7 @@
 // layout ((imax+2)(jmax+2)(kmax+2) doubles, i fastest, one ghost layer,
 // src/util.h:19-34). Threads map x -> i so every warp touches consecutive
 // doubles. All arithmetic is FP64 (the reference computes in double).
+#include <algorithm>
 #include <cfloat>
 #include <initializer_list>
 #include <cstdio>
@@ -487,21 +488,136 @@ __global__ void __launch_bounds__(kBlock) k_rhs(Dims g, double rx_arg, double ry
 }
 
 // ---- adaptUV (discretization.c:654-681) ----
+// With MAX the block also folds the maxima of |u|, |v|, |w| it wrote (bit
+// patterns, NaN skipped, as k_max3) and raises one slot of amax_slots per
+// field with an integer atomic maximum (non-negative doubles order like their
+// bits); blocks spread over kAmaxSlots slots.
+template <bool MAX>
 __global__ void __launch_bounds__(kBlock) k_adapt(Dims g, double fx_arg, double fy_arg,
     double fz_arg, const StepScalars *sp, const double *__restrict__ f,
     const double *__restrict__ gg, const double *__restrict__ h, const double *__restrict__ p,
-    double *__restrict__ u, double *__restrict__ v, double *__restrict__ w)
+    double *__restrict__ u, double *__restrict__ v, double *__restrict__ w,
+    unsigned long long *amax_slots)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
-  if (i > g.imax || j > g.jmax || k > g.kmax) return;
-  const double fx = sp ? sp->fx : fx_arg, fy = sp ? sp->fy : fy_arg, fz = sp ? sp->fz : fz_arg;
-  const int64_t c = (int64_t)k * g.sk + (int64_t)j * g.sj + i;
-  const double pc = p[c];
-  u[c] = f[c] - (p[c + 1] - pc) * fx;
-  v[c] = gg[c] - (p[c + g.sj] - pc) * fy;
-  w[c] = h[c] - (p[c + g.sk] - pc) * fz;
+  const bool in = i <= g.imax && j <= g.jmax && k <= g.kmax;
+  unsigned uh = 0u, ul = 0u, vh = 0u, vl = 0u, wh = 0u, wl = 0u;
+  if (in) {
+    const double fx = sp ? sp->fx : fx_arg, fy = sp ? sp->fy : fy_arg, fz = sp ? sp->fz : fz_arg;
+    const int64_t c = (int64_t)k * g.sk + (int64_t)j * g.sj + i;
+    const double pc = p[c];
+    const double un = f[c] - (p[c + 1] - pc) * fx;
+    const double vn = gg[c] - (p[c + g.sj] - pc) * fy;
+    const double wn = h[c] - (p[c + g.sk] - pc) * fz;
+    u[c] = un;
+    v[c] = vn;
+    w[c] = wn;
+    if (MAX) {
+      abs_max_key(uh, ul, un);
+      abs_max_key(vh, vl, vn);
+      abs_max_key(wh, wl, wn);
+    }
+  }
+  if (!MAX) return;
+  // keys stay 32-bit pairs on the integer pipe: an FP64 maximum per thread
+  // would cost more than the whole kernel on GB300's FP64 rate
+  warp_key_max(uh, ul);
+  warp_key_max(vh, vl);
+  warp_key_max(wh, wl);
+  __shared__ unsigned sk[kBlock / 32][6];
+  const int t = flat_tid();
+  if ((t & 31) == 0) {
+    sk[t >> 5][0] = uh;
+    sk[t >> 5][1] = ul;
+    sk[t >> 5][2] = vh;
+    sk[t >> 5][3] = vl;
+    sk[t >> 5][4] = wh;
+    sk[t >> 5][5] = wl;
+  }
+  __syncthreads();
+  if (t == 0) {
+    for (int q = 1; q < kBlock / 32; q++) {
+      key_max(uh, ul, sk[q][0], sk[q][1]);
+      key_max(vh, vl, sk[q][2], sk[q][3]);
+      key_max(wh, wl, sk[q][4], sk[q][5]);
+    }
+    const unsigned b = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+    unsigned long long *slot = amax_slots + 3 * (b % kAmaxSlots);
+    atomicMax(slot + 0, ((unsigned long long)uh << 32) | ul);
+    atomicMax(slot + 1, ((unsigned long long)vh << 32) | vl);
+    atomicMax(slot + 2, ((unsigned long long)wh << 32) | wl);
+  }
+}
+
+// ---- computeTimestep's maxima after a fused adaptUV ----
+// max |u|, |v|, |w| over the padded cells adaptUV does not write (the ghost
+// shell: planes k = 0 and kmax + 1, rows j = 0 and jmax + 1 of the planes
+// between, cells i = 0 and imax + 1 of the rows between), folded with the
+// slots k_adapt<true> raised and the reference's DBL_MIN seed: the maximum
+// over the whole arrays, as k_max3. The last block zeroes the slots.
+__global__ void __launch_bounds__(kBlock) k_shell_max3(Dims g, const double *__restrict__ u,
+    const double *__restrict__ v, const double *__restrict__ w, unsigned long long *amax_slots,
+    double *__restrict__ partials, unsigned *ticket, double *__restrict__ out3)
+{
+  const int64_t P = g.imax + 2, PQ = (int64_t)g.sk;
+  const int64_t n1 = 2 * PQ, n2 = (int64_t)g.kmax * 2 * P, n3 = (int64_t)g.kmax * g.jmax * 2;
+  unsigned uh = 0u, ul = 0u, vh = 0u, vl = 0u, wh = 0u, wl = 0u;
+  for (int64_t q = blockIdx.x * (int64_t)kBlock + threadIdx.x; q < n1 + n2 + n3;
+       q += (int64_t)gridDim.x * kBlock) {
+    int64_t c;
+    if (q < n1) {
+      c = q < PQ ? q : (int64_t)(g.kmax + 1) * PQ + (q - PQ);
+    } else if (q < n1 + n2) {
+      const int64_t r = q - n1;
+      const int64_t k = 1 + r / (2 * P), rr = r % (2 * P);
+      c = k * PQ + (rr < P ? rr : (int64_t)(g.jmax + 1) * g.sj + (rr - P));
+    } else {
+      const int64_t r = q - n1 - n2;
+      const int64_t k = 1 + r / (2 * g.jmax), rr = r % (2 * g.jmax);
+      c = k * PQ + (1 + rr / 2) * g.sj + ((rr & 1) ? g.imax + 1 : 0);
+    }
+    abs_max_key(uh, ul, u[c]);
+    abs_max_key(vh, vl, v[c]);
+    abs_max_key(wh, wl, w[c]);
+  }
+  __shared__ double sm[3][kBlock / 32];
+  double mu = block_reduce_max<kBlock>(__hiloint2double((int)uh, (int)ul), sm[0]);
+  double mv = block_reduce_max<kBlock>(__hiloint2double((int)vh, (int)vl), sm[1]);
+  double mw = block_reduce_max<kBlock>(__hiloint2double((int)wh, (int)wl), sm[2]);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    partials[3 * blockIdx.x + 0] = mu;
+    partials[3 * blockIdx.x + 1] = mv;
+    partials[3 * blockIdx.x + 2] = mw;
+    last = ticket_is_last(ticket);
+  }
+  __syncthreads();
+  if (!last) return;
+  double a = DBL_MIN, b = DBL_MIN, c = DBL_MIN;
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += kBlock) {
+    a = fmax(a, ld_cg(partials + 3 * q + 0));
+    b = fmax(b, ld_cg(partials + 3 * q + 1));
+    c = fmax(c, ld_cg(partials + 3 * q + 2));
+  }
+  for (int q = threadIdx.x; q < kAmaxSlots; q += kBlock) {
+    a = fmax(a, __longlong_as_double((long long)amax_slots[3 * q + 0]));
+    b = fmax(b, __longlong_as_double((long long)amax_slots[3 * q + 1]));
+    c = fmax(c, __longlong_as_double((long long)amax_slots[3 * q + 2]));
+    amax_slots[3 * q + 0] = 0ull;
+    amax_slots[3 * q + 1] = 0ull;
+    amax_slots[3 * q + 2] = 0ull;
+  }
+  a = block_reduce_max<kBlock>(a, sm[0]);
+  b = block_reduce_max<kBlock>(b, sm[1]);
+  c = block_reduce_max<kBlock>(c, sm[2]);
+  if (threadIdx.x == 0) {
+    out3[0] = a;
+    out3[1] = b;
+    out3[2] = c;
+    *ticket = 0;
+  }
 }
 
 // ---- normalizePressure (discretization.c:403-429) ----
@@ -703,11 +819,28 @@ bool launch_subtract_mean(const Dims &g, double *p, const double *d_mean)
 
 bool launch_adapt_uv(const Dims &g, double dt, double dx, double dy, double dz,
     const double *f, const double *gg, const double *h, const double *p, double *u, double *v,
-    double *w, const StepScalars *sp)
+    double *w, const StepScalars *sp, unsigned long long *amax_slots)
 {
-  k_adapt<<<cell_grid(g, kCellBlock), kCellBlock, 0, stream()>>>(
-      g, dt / dx, dt / dy, dt / dz, sp, f, gg, h, p, u, v, w);
+  if (amax_slots)
+    k_adapt<true><<<cell_grid(g, kCellBlock), kCellBlock, 0, stream()>>>(
+        g, dt / dx, dt / dy, dt / dz, sp, f, gg, h, p, u, v, w, amax_slots);
+  else
+    k_adapt<false><<<cell_grid(g, kCellBlock), kCellBlock, 0, stream()>>>(
+        g, dt / dx, dt / dy, dt / dz, sp, f, gg, h, p, u, v, w, nullptr);
   return launched("k_adapt");
+}
+
+bool launch_shell_max3(const Dims &g, const double *u, const double *v, const double *w,
+    unsigned long long *amax_slots, ReduceScratch &red, double *d_out3)
+{
+  const int64_t shell = 2 * (int64_t)g.sk + (int64_t)g.kmax * 2 * (g.imax + 2) +
+                        (int64_t)g.kmax * g.jmax * 2;
+  int blocks = (int)std::min<int64_t>(4 * sm_count(), (shell + kBlock - 1) / kBlock);
+  if (blocks < 1) blocks = 1;
+  if (!reduce_scratch_alloc(red, 3 * blocks)) return false;
+  k_shell_max3<<<blocks, kBlock, 0, stream()>>>(g, u, v, w, amax_slots, red.partials, red.ticket,
+      d_out3);
+  return launched("k_shell_max3");
 }
 
 bool launch_fill(double *a, int64_t n, double value)
@@ -858,6 +991,11 @@ void initDiscretization(Discretization *s, Parameter *params)
     }
   }
   if (!cuda_ok(cudaMalloc(&st->d_scalars, 8 * sizeof(double)), "cudaMalloc(scalars)")) return;
+  const size_t amax_bytes = 3 * kAmaxSlots * sizeof(unsigned long long);
+  if (!cuda_ok(cudaMalloc(&st->d_amax, amax_bytes), "cudaMalloc(amax)")) return;
+  if (!cuda_ok(cudaMemsetAsync(st->d_amax, 0, amax_bytes, stream()), "cudaMemsetAsync(amax)"))
+    return;
+  st->amax = kAmaxReset;
   if (!cuda_ok(cudaMallocHost(&st->h_scalars, 8 * sizeof(double)), "cudaMallocHost(scalars)"))
     return;
   const double init[4] = { params->u_init, params->v_init, params->w_init, params->p_init };
@@ -880,7 +1018,21 @@ void computeTimestep(Discretization *s)
 {
   DiscState *st = need_state(s, "computeTimestep");
   if (!st || !await_arrays({ s->u, s->v, s->w })) return;
-  if (!launch_max3(st->dims, s->u, s->v, s->w, st->red, st->d_scalars)) return;
+  if (st->ext.fuse_dt && st->amax == kAmaxValid) {
+    // the interior maxima came with the last adaptUV: read the ghost shell only
+    if (!launch_shell_max3(st->dims, s->u, s->v, s->w, st->d_amax, st->red, st->d_scalars))
+      return;
+    st->dt_shell++;
+  } else {
+    if (!launch_max3(st->dims, s->u, s->v, s->w, st->red, st->d_scalars)) return;
+    st->dt_full++;
+    if (st->amax != kAmaxReset &&
+        !cuda_ok(cudaMemsetAsync(st->d_amax, 0, 3 * kAmaxSlots * sizeof(unsigned long long),
+                     stream()),
+            "computeTimestep reset"))
+      return;
+  }
+  st->amax = kAmaxReset;
   if (!cuda_ok(cudaMemcpyAsync(st->h_scalars, st->d_scalars, 3 * sizeof(double),
                    cudaMemcpyDeviceToHost, stream()),
           "computeTimestep copy"))
@@ -900,6 +1052,7 @@ void setBoundaryConditions(Discretization *s)
   DiscState *st = need_state(s, "setBoundaryConditions");
   if (!st || !await_arrays({ s->u, s->v, s->w })) return;
   const int bc[6] = { s->bcLeft, s->bcRight, s->bcBottom, s->bcTop, s->bcFront, s->bcBack };
+  velocity_written(st);
   launch_bc(st->dims, bc, PROBLEM_NONE, 0.0, 0.0, s->u, s->v, s->w);
 }
 
@@ -908,6 +1061,7 @@ void setSpecialBoundaryCondition(Discretization *s)
 {
   DiscState *st = need_state(s, "setSpecialBoundaryCondition");
   if (!st || !await_arrays({ s->u })) return;
+  velocity_written(st);
   launch_special(st->dims, problem_code(s->problem), st->ext.lid, st->ext.inflow, s->u);
 }
 
@@ -938,8 +1092,26 @@ void adaptUV(Discretization *s)
 {
   DiscState *st = need_state(s, "adaptUV");
   if (!st || !await_arrays({ s->f, s->g, s->h, s->p, s->u, s->v, s->w })) return;
-  launch_adapt_uv(st->dims, s->dt, s->grid.dx, s->grid.dy, s->grid.dz, s->f, s->g, s->h, s->p,
-      s->u, s->v, s->w);
+  // fuse_dt: the first adaptUV after computeTimestep keeps the maxima of what it writes
+  // (not with host_fields, whose arrays host code may write directly)
+  const bool keep = st->ext.fuse_dt && !st->ext.host_fields && st->amax == kAmaxReset;
+  if (!launch_adapt_uv(st->dims, s->dt, s->grid.dx, s->grid.dy, s->grid.dz, s->f, s->g, s->h,
+          s->p, s->u, s->v, s->w, nullptr, keep ? st->d_amax : nullptr))
+    return;
+  if (keep) st->amax = kAmaxValid;
+  else velocity_written(st);
+}
+
+int nusifTimestepCounts(const Discretization *s, long long *shell, long long *full)
+{
+  const DiscState *st = disc_state(s);
+  if (!st) {
+    fail(NUSIF_ERR_ARG, "nusifTimestepCounts: unknown discretization");
+    return NUSIF_ERR_ARG;
+  }
+  if (shell) *shell = st->dt_shell;
+  if (full) *full = st->dt_full;
+  return NUSIF_OK;
 }
 
 void nusifFreeDiscretization(Discretization *s)
@@ -954,6 +1126,7 @@ void nusifFreeDiscretization(Discretization *s)
     *fields[q] = nullptr;
   }
   if (st->d_scalars) cudaFree(st->d_scalars);
+  if (st->d_amax) cudaFree(st->d_amax);
   if (st->h_scalars) cudaFreeHost(st->h_scalars);
   reduce_scratch_free(st->red);
   disc_state_erase(s);

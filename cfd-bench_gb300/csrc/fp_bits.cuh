@@ -65,4 +65,20 @@ __device__ __forceinline__ void abs_max_key(unsigned &mh, unsigned &ml, double x
   ml = gt ? l : ml;
 }
 
+// the larger of two keys (high, low), lexicographically in 32-bit operations
+__device__ __forceinline__ void key_max(unsigned &mh, unsigned &ml, unsigned h, unsigned l)
+{
+  const bool gt = h > mh || (h == mh && l > ml);
+  mh = gt ? h : mh;
+  ml = gt ? l : ml;
+}
+
+// the warp's largest key, in every lane
+__device__ __forceinline__ void warp_key_max(unsigned &mh, unsigned &ml)
+{
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+    key_max(mh, ml, __shfl_xor_sync(0xffffffffu, mh, off), __shfl_xor_sync(0xffffffffu, ml, off));
+}
+
 }  // namespace nusif

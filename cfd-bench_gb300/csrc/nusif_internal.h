@@ -50,6 +50,8 @@ struct Extras {
   int fg_fp64 = 0;           // key fg_arith: computeFG in FP64 instructions (fp64) or FP32 pairs (df32)
   int arith_fp64 = 0;        // key arith: every FP64-bound stencil in FP64 instructions (fp64)
                              // or FP32 pairs (df32); also sets fg_arith
+  int fuse_dt = 0;           // key fuse_dt: adaptUV keeps the maxima of the velocities it writes
+                             // and the next computeTimestep reads only the ghost shell
 };
 Extras *extras_for(const Parameter *p, bool create);
 
@@ -94,6 +96,11 @@ struct StepScalars {
 };
 
 // Device state of one Discretization (kept beside the reference struct).
+// fuse_dt: per-slot maxima of |u|, |v|, |w| (bit patterns of non-negative
+// doubles) that adaptUV accumulates, and what they hold
+constexpr int kAmaxSlots = 1024;
+enum AmaxState { kAmaxReset = 0, kAmaxValid = 1, kAmaxDirty = 2 };
+
 struct DiscState {
   Dims dims;
   int problem = PROBLEM_NONE;
@@ -101,7 +108,18 @@ struct DiscState {
   ReduceScratch red;
   double *d_scalars = nullptr;  // device: [0..2] max |u|,|v|,|w|, [3] sum p
   double *h_scalars = nullptr;  // pinned host mirror
+  // fuse_dt: kAmaxReset, the slots are zero; kAmaxValid, they hold the
+  // interior maxima of exactly the last adaptUV and nothing wrote u, v, w
+  // since; kAmaxDirty, anything else
+  unsigned long long *d_amax = nullptr;  // [kAmaxSlots][3]
+  int amax = kAmaxReset;
+  long long dt_shell = 0, dt_full = 0;  // computeTimestep calls by path
 };
+// u, v or w changed other than by adaptUV: the kept maxima no longer hold
+inline void velocity_written(DiscState *st)
+{
+  if (st && st->amax == kAmaxValid) st->amax = kAmaxDirty;
+}
 DiscState *disc_state(const Discretization *d);
 
 // ---- kernels launched by the discretization entry points (discretization.cu) ----
@@ -119,7 +137,9 @@ bool launch_interior_sum(const Dims &g, const double *p, ReduceScratch &red, dou
 bool launch_subtract_mean(const Dims &g, double *p, const double *d_mean);
 bool launch_adapt_uv(const Dims &g, double dt, double dx, double dy, double dz,
     const double *f, const double *gg, const double *h, const double *p, double *u, double *v,
-    double *w, const StepScalars *sp = nullptr);
+    double *w, const StepScalars *sp = nullptr, unsigned long long *amax_slots = nullptr);
+bool launch_shell_max3(const Dims &g, const double *u, const double *v, const double *w,
+    unsigned long long *amax_slots, ReduceScratch &red, double *d_out3);
 bool launch_special(const Dims &g, int problem, double lid, double inflow, double *u);
 int problem_code(const char *name);
 

@@ -105,6 +105,7 @@ int apply_extra(Parameter *param, const char *tok, const char *val)
   if (starts_with(tok, "mg_chunk")) { x->mg_chunk = atoi(v); hit = 1; }
   if (starts_with(tok, "host_fields")) { x->host_fields = atoi(v); hit = 1; }
   if (starts_with(tok, "mg_probe")) { x->mg_guess_probe = atoi(v); hit = 1; }
+  if (starts_with(tok, "fuse_dt")) { x->fuse_dt = atoi(v); hit = 1; }
   if (starts_with(tok, "fg_arith")) {
     if (strcmp(v, "fp64") == 0) x->fg_fp64 = 1;
     else if (strcmp(v, "df32") == 0) x->fg_fp64 = 0;

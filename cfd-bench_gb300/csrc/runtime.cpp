@@ -270,6 +270,7 @@ int nusifUploadField(Discretization *d, int which, const double *host)
     fail(NUSIF_ERR_ARG, "nusifUploadField: unknown discretization or field %d", which);
     return NUSIF_ERR_ARG;
   }
+  velocity_written(st);
   size_t bytes = sizeof(double) * (size_t)st->dims.padded;
   const void *fp = dst;
   if (!await_copies(&fp, 1)) return NUSIF_ERR_CUDA;
@@ -288,6 +289,7 @@ int nusifUploadFieldAsync(Discretization *d, int which, const double *host)
     fail(NUSIF_ERR_ARG, "nusifUploadFieldAsync: unknown discretization or field %d", which);
     return NUSIF_ERR_ARG;
   }
+  velocity_written(st);
   const size_t bytes = sizeof(double) * (size_t)st->dims.padded;
   return queue_copy(dst, host, bytes, cudaMemcpyHostToDevice, dst) ? NUSIF_OK : NUSIF_ERR_CUDA;
 }

@@ -33,6 +33,7 @@
 #include <cuda_bf16.h>
 
 #include <cstdint>
+#include <cstdlib>
 #include <cstdio>
 
 #include "nusif_internal.h"
@@ -95,19 +96,39 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity)
   return ok != 0;
 }
 
+// the same test, the thread suspended (no issue slots) until the phase
+// completes or about `hint_ns` pass
+__device__ __forceinline__ bool mbar_try_sleep(uint32_t bar, uint32_t parity, uint32_t hint_ns)
+{
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity), "r"(hint_ns)
+      : "memory");
+  return ok != 0;
+}
+
 // wait for the phase of `parity` to complete; false after the time bound or
-// when another warp has raised the abort flag
+// when another warp has raised the abort flag. Waiting threads sleep in the
+// barrier rather than spin, so the single-thread producer and MMA issuer of
+// the block's other warps keep their issue slots; the abort flag and the
+// clock are read every 8th round.
 __device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int *abort_flag, int *err)
 {
   if (mbar_try(bar, parity)) return true;
   const uint64_t t0 = now_ns();
-  for (;;) {
-    if (mbar_try(bar, parity)) return true;
-    if (*abort_flag) return false;
-    if (now_ns() - t0 > kWaitNs) {
-      *abort_flag = 1;
-      atomicExch(err, 1);
-      return false;
+  for (uint32_t round = 1;; round++) {
+    if (mbar_try_sleep(bar, parity, 20000u)) return true;
+    if ((round & 7u) == 0) {
+      if (*abort_flag) return false;
+      if (now_ns() - t0 > kWaitNs) {
+        *abort_flag = 1;
+        atomicExch(err, 1);
+        return false;
+      }
     }
   }
 }
@@ -339,16 +360,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__
         }
         fence_after();
         const uint32_t sa = smem_u32(stage_base + (size_t)stage * stage_bytes);
+        // the descriptors' start-address field is (address >> 4) in 14 bits;
+        // every operand lies below 256 KB, so offsets add to it without carry
+        uint64_t a0[2], b0[2];
+        uint32_t da[2], db[2];
+        int ks[2];
+        for (int src = 0; src < 2; src++) {
+          ks[src] = (src == 0 ? P.C0 : P.C1) / 16;
+          const uint32_t rb = 32u * (uint32_t)ks[src];
+          a0[src] = smem_desc_sw(sa + P.a_off[src], rb);
+          b0[src] = smem_desc_sw(sa + P.b_off[src], rb);
+          da[src] = P.atom[src] >> 4;
+          db[src] = P.wtap[src] >> 4;
+        }
         for (int q = 0; q < 3; q++) {  // dx = q - 1: the box read q atoms in
           for (int src = 0; src < 2; src++) {
-            const int cs = src == 0 ? P.C0 : P.C1;
-            const uint32_t rb = 2u * (uint32_t)cs;
-            for (int j = 0; j < cs / 16; j++) {
-              const uint64_t adesc =
-                  smem_desc_sw(sa + P.a_off[src] + (uint32_t)q * P.atom[src] + 32u * j, rb);
-              const uint64_t bdesc =
-                  smem_desc_sw(sa + P.b_off[src] + (uint32_t)q * P.wtap[src] + 32u * j, rb);
-              mma_f16(d, adesc, bdesc, P.idesc, accumulate);
+            for (int j = 0; j < ks[src]; j++) {
+              mma_f16(d, a0[src] + (uint64_t)(q * da[src] + 2u * j),
+                  b0[src] + (uint64_t)(q * db[src] + 2u * j), P.idesc, accumulate);
               accumulate = 1;
               issued = true;
             }
@@ -544,9 +573,18 @@ bool launch_tc(const CUtensorMap &a0, const CUtensorMap &a1, const CUtensorMap &
   P.stage_bytes = off;
   P.tx_bytes = tx;
   const size_t stage_bytes = P.stage_bytes;
-  // as many stages as fit in ~96 KB (at least 2, at most kMaxStages): two
-  // blocks per SM, each keeping its stages' loads in flight
-  int stages = (int)((96 * 1024) / stage_bytes);
+  // two stages: the fewer the stages, the more blocks an SM holds, and more
+  // blocks measured faster than deeper pipelines (the 128^3 forward pass:
+  // 1.77 ms with 2 stages and six blocks of 16 -> 16 layers per SM, 1.81 ms
+  // with 4, 2.36 ms with 8, 2.43 ms with 16 stages and two blocks per SM);
+  // NUSIF_TC_STAGES overrides the count
+  int stages = 2;
+  if (const char *e = getenv("NUSIF_TC_STAGES")) {
+    const int s = atoi(e);
+    if (s >= 2) stages = s;
+  }
+  const int fit = (int)((227 * 1024 - kBarBytes - 1024) / stage_bytes);
+  if (stages > fit) stages = fit;
   if (stages > kMaxStages) stages = kMaxStages;
   if (stages < 2) stages = 2;
   P.stages = stages;
@@ -571,7 +609,14 @@ bool launch_tc(const CUtensorMap &a0, const CUtensorMap &a1, const CUtensorMap &
       return false;
     attr_set[dev] = true;
   }
+  // a persistent grid: no more blocks than can be resident at once, by shared
+  // memory (1 KB reserved per block), registers (8-register granules per
+  // thread) and tensor memory
+  cudaFuncAttributes fa{};
+  if (!cuda_ok(cudaFuncGetAttributes(&fa, k_conv_tc<NCH>), "k_conv_tc attributes")) return false;
+  const int regs_block = ((fa.numRegs + 7) / 8) * 8 * kThreads;
   int per_sm = (int)((228 * 1024) / (smem + 1024));
+  if (regs_block > 0 && per_sm > 65536 / regs_block) per_sm = 65536 / regs_block;
   if (per_sm > per_sm_tmem) per_sm = per_sm_tmem;
   if (per_sm < 1) per_sm = 1;
   int grid = sm_count_tc() * per_sm;

@@ -113,6 +113,8 @@ SIGNATURES = [
                                   C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("nusifBatchFree", None, [C.c_void_p]),
     ("nusifLaunchCount", C.c_ulonglong, []),
+    ("nusifTimestepCounts", C.c_int, [C.POINTER(Discretization), C.POINTER(C.c_longlong),
+                                      C.POINTER(C.c_longlong)]),
     ("nusifTimeKernel", C.c_int, [C.POINTER(Solver), c_double_p, c_double_p, C.c_int, C.c_int,
                                   C.POINTER(C.c_double)]),
     ("nusifVersion", C.c_char_p, []),

@@ -231,6 +231,10 @@ NUSIF_API int nusifBatchStats(NusifBatch *b, int idx, double *t, double *dt, int
 NUSIF_API void nusifBatchFree(NusifBatch *b);
 /* kernels this library launched since it was loaded (observability) */
 NUSIF_API unsigned long long nusifLaunchCount(void);
+/* computeTimestep calls on d that read only the ghost shell (key fuse_dt 1:
+ * the interior maxima came with the preceding adaptUV) and that read the
+ * whole arrays (observability) */
+NUSIF_API int nusifTimestepCounts(const Discretization *d, long long *shell, long long *full);
 /* Measurement hook (mg and mg-mixed solvers): average duration in ms of `reps`
  * launches of one fine-level kernel, timed with CUDA events on the library
  * stream; which = 0 the fine smoother (mg-mixed: one whole FP32 red-black

@@ -148,7 +148,7 @@ def test_extension_keys(nusif_lib, tmp_path):
                    ("mg_theta", "0.9"), ("mg_omega", "1.2"), ("mg_chunk", "8"),
                    ("mg_guess", "quadratic"), ("mg_tail", "0"), ("host_fields", "1"),
                    ("mg_probe", "8"), ("fg_arith", "fp64"), ("fg_arith", "df32"),
-                   ("arith", "fp64"), ("arith", "df32")]:
+                   ("arith", "fp64"), ("arith", "df32"), ("fuse_dt", "1")]:
         assert nusif_lib.nusifParameterSet(C.byref(p), k.encode(), val.encode()) == 0
     # extension keys do not disturb the reference members
     assert p.levels == 5 and p.presmooth == 5 and p.re == 100.0
