@@ -61,9 +61,9 @@ def parse_args():
                     help="FP64-bound stencils (computeFG, the mixed solver's fine residual) "
                          "in FP32 pairs (df32) or FP64 instructions (fp64)")
     ap.add_argument("--guess", default="quadratic",
-                    choices=["previous", "extrapolate", "quadratic"],
+                    choices=["previous", "extrapolate", "quadratic", "cubic"],
                     help="initial pressure of each V-cycle solve: p(n-1), 2 p(n-1) - p(n-2), "
-                         "or 3 p(n-1) - 3 p(n-2) + p(n-3)")
+                         "3 p(n-1) - 3 p(n-2) + p(n-3), or 4 p(n-1) - 6 p(n-2) + 4 p(n-3) - p(n-4)")
     ap.add_argument("--batch-n", type=int, default=96, help="instances of the batch workload")
     ap.add_argument("--workload", default="cavity",
                     choices=["cavity", "channel", "batch", "learned"],

@@ -107,7 +107,8 @@ struct MgHierarchy {
   double theta = 0.9;   // mg-mixed: FP32 correction target as a fraction of rtol
   int guess = 0;        // 1: start from 2 p(n-1) - p(n-2)
   double *p_prev = nullptr;   // padded copy of the previous solve's result (guess >= 1)
-  double *p_prev2 = nullptr;  // and of the one before (guess 2)
+  double *p_prev2 = nullptr;  // and of the one before (guess >= 2)
+  double *p_prev3 = nullptr;  // and of the one before that (guess 3)
   int *d_hist = nullptr;      // device: earlier solutions kept (0, 1, 2)
   // the solve as one CUDA graph (head, while-loops, tail) for fixed p / rhs
   cudaGraphExec_t graph = nullptr;
@@ -2303,39 +2304,45 @@ bool vcycle(MgHierarchy *H, int l, T **xs, T **bs, bool zero, bool inner_test)
 }
 
 // initial guess by extrapolation in time (whole padded arrays, ghosts
-// included): linear p <- 2 p(n-1) - p(n-2), or (quadratic, once two earlier
-// solutions exist) p <- 3 p(n-1) - 3 p(n-2) + p(n-3). hist[0] counts the
-// earlier solutions kept (0, 1, 2) on the device, so the same launches serve
-// host-driven and graph-captured steps. The quadratic history lives in two
-// buffers whose roles alternate (hist[1]): buf[par] holds p(n-2), buf[par ^ 1]
-// p(n-3), which this step overwrites with p(n-1) -- the next step's p(n-2) --
-// so no history value is copied (40 bytes per cell instead of 48). The linear
-// history is one buffer updated in place.
-__global__ void k_extrapolate(double *__restrict__ p, double *buf0, double *buf1, int64_t n,
-    const int *hist, int quadratic)
+// included): linear p <- 2 p(n-1) - p(n-2), quadratic (once two earlier
+// solutions exist) p <- 3 p(n-1) - 3 p(n-2) + p(n-3), or cubic (once three
+// exist) p <- 4 p(n-1) - 6 p(n-2) + 4 p(n-3) - p(n-4); until enough history
+// exists the next lower order. hist[0] counts the earlier solutions kept
+// (0 .. order) on the device, so the same launches serve host-driven and
+// graph-captured steps. The history lives in `order` buffers whose roles
+// rotate (hist[1]): buf[r] holds p(n-2), buf[r + 1] p(n-3), buf[r + 2] p(n-4)
+// (indices mod order); the oldest is overwritten with p(n-1), the next step's
+// p(n-2), so no history value is copied (quadratic: 40 bytes per cell instead
+// of 48). The linear history is one buffer updated in place.
+__global__ void k_extrapolate(double *__restrict__ p, double *buf0, double *buf1, double *buf2,
+    int64_t n, const int *hist, int order)
 {
-  const int h = hist[0], par = quadratic ? hist[1] : 0;
-  // linear: a and b are the same buffer (each cell read, then written)
-  const double *a = par ? buf1 : buf0;                  // p(n-2)
-  double *b = quadratic ? (par ? buf0 : buf1) : buf0;   // p(n-3), then p(n-1)
+  const int h = hist[0], r = order > 1 ? hist[1] : 0;
+  double *const buf[3] = { buf0, buf1, buf2 };
+  const double *a = buf[r];                            // p(n-2)
+  const double *b = buf[order > 1 ? (r + 1) % order : r];  // p(n-3)
+  const double *c = buf[order > 2 ? (r + 2) % order : r];  // p(n-4)
+  double *o = buf[(r + order - 1) % order];            // the oldest, then p(n-1)
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
        q += (int64_t)gridDim.x * blockDim.x) {
     const double cur = p[q];
     if (h >= 1) {
       const double prev = a[q];
-      if (quadratic && h >= 2)
+      if (order >= 3 && h >= 3)
+        p[q] = fma(4.0, cur + b[q], -fma(6.0, prev, c[q]));
+      else if (order >= 2 && h >= 2)
         p[q] = 3.0 * (cur - prev) + b[q];
       else
         p[q] = 2.0 * cur - prev;
     }
-    b[q] = cur;
+    o[q] = cur;
   }
 }
 
-__global__ void k_hist_advance(int *hist, int quadratic)
+__global__ void k_hist_advance(int *hist, int order)
 {
-  if (hist[0] < 2) hist[0] += 1;
-  if (quadratic) hist[1] ^= 1;
+  if (hist[0] < order) hist[0] += 1;
+  if (order > 1) hist[1] = (hist[1] + order - 1) % order;
 }
 
 __global__ void k_mx_fold(View<float> e, double *p, int p_sj, int p_sk, const MgState *st)
@@ -2457,7 +2464,7 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
   H->theta = x.mg_theta;
   H->mx_df = !x.arith_fp64;
   H->keep_on_skip = (H->pre % 2 != 0 || H->post % 2 != 0) ? 1 : 0;
-  H->guess = x.mg_guess == 1 || x.mg_guess == 2 ? x.mg_guess : 0;
+  H->guess = x.mg_guess >= 1 && x.mg_guess <= 3 ? x.mg_guess : 0;
   H->use_graph = x.mg_graph != 0;
   for (cudaStream_t &c : H->cap)
     if (!cuda_ok(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking), "mg capture stream"))
@@ -2466,7 +2473,9 @@ bool mg_setup(Solver *s, Discretization *d, SolverState *ss)
     const size_t padded =
         (size_t)(d->grid.imax + 2) * (d->grid.jmax + 2) * (d->grid.kmax + 2) * sizeof(double);
     if (!cuda_ok(cudaMalloc(&H->p_prev, padded), "cudaMalloc(p_prev)")) return false;
-    if (H->guess == 2 && !cuda_ok(cudaMalloc(&H->p_prev2, padded), "cudaMalloc(p_prev2)"))
+    if (H->guess >= 2 && !cuda_ok(cudaMalloc(&H->p_prev2, padded), "cudaMalloc(p_prev2)"))
+      return false;
+    if (H->guess >= 3 && !cuda_ok(cudaMalloc(&H->p_prev3, padded), "cudaMalloc(p_prev3)"))
       return false;
     if (!cuda_ok(cudaMalloc(&H->d_hist, 2 * sizeof(int)), "cudaMalloc(hist)") ||
         !cuda_ok(cudaMemset(H->d_hist, 0, 2 * sizeof(int)), "hist init"))
@@ -2618,10 +2627,10 @@ bool enqueue_warm_start(MgHierarchy *H, const View<double> &v0, double *p)
 {
   if (H->guess < 1) return true;
   const int64_t padded = (int64_t)(v0.nx + 2) * (v0.ny + 2) * (v0.nz + 2);
-  k_extrapolate<<<flat_blocks(padded), kNT, 0, stream()>>>(p, H->p_prev, H->p_prev2, padded,
-      H->d_hist, H->guess == 2 ? 1 : 0);
+  k_extrapolate<<<flat_blocks(padded), kNT, 0, stream()>>>(p, H->p_prev, H->p_prev2, H->p_prev3,
+      padded, H->d_hist, H->guess);
   if (!launched("k_extrapolate")) return false;
-  k_hist_advance<<<1, 1, 0, stream()>>>(H->d_hist, H->guess == 2 ? 1 : 0);
+  k_hist_advance<<<1, 1, 0, stream()>>>(H->d_hist, H->guess);
   return launched("k_hist_advance");
 }
 
@@ -3056,6 +3065,7 @@ void mg_free(Solver *s, SolverState *ss)
     if (c) cudaStreamDestroy(c);
   if (H->p_prev) cudaFree(H->p_prev);
   if (H->p_prev2) cudaFree(H->p_prev2);
+  if (H->p_prev3) cudaFree(H->p_prev3);
   if (H->d_hist) cudaFree(H->d_hist);
   if (H->minv64) cudaFree(H->minv64);
   if (H->minv32) cudaFree(H->minv32);

@@ -40,7 +40,8 @@ struct Extras {
   int mg_inner = 4;          // mg-mixed: most FP32 V-cycles per FP64 residual
   double mg_theta = 0.9;     // mg-mixed: FP32 correction target, a fraction of rtol
   double mg_omega = 1.0;     // relaxation of the multigrid red-black smoother (1: Gauss-Seidel)
-  int mg_guess = 0;          // initial guess: 0 previous p, 1 linear, 2 quadratic extrapolation in time
+  int mg_guess = 0;          // initial guess: 0 previous p, 1 linear, 2 quadratic, 3 cubic
+                             // extrapolation in time
   int mg_graph = 1;          // 1: each solve is one CUDA graph launch (while-loops on the device)
   int mg_tail = 0;           // levels of at most this many cells run as one kernel (0: off)
   int mg_chunk = 0;          // planes per block of the FP32 one-kernel sweep (0: autotuned)

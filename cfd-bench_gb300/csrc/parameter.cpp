@@ -128,6 +128,7 @@ int apply_extra(Parameter *param, const char *tok, const char *val)
     if (strcmp(v, "previous") == 0) x->mg_guess = 0;
     else if (strcmp(v, "extrapolate") == 0) x->mg_guess = 1;
     else if (strcmp(v, "quadratic") == 0) x->mg_guess = 2;
+    else if (strcmp(v, "cubic") == 0) x->mg_guess = 3;
     else x->mg_guess = atoi(v);
     hit = 1;
   }

@@ -186,7 +186,7 @@ def test_mg_time_loop_matches_oracle(nusif_lib, oracle_mod, solver):
 
 
 @pytest.mark.parametrize("solver,guess", [("mg", "extrapolate"), ("mg-mixed", "extrapolate"),
-                                          ("mg-mixed", "quadratic")])
+                                          ("mg-mixed", "quadratic"), ("mg-mixed", "cubic")])
 def test_mg_extrapolated_guess(nusif_lib, solver, guess):
     """mg_guess extrapolate / quadratic start each solve from 2 p(n-1) - p(n-2)
     / 3 p(n-1) - 3 p(n-2) + p(n-3): every step still ends at rtol, the
@@ -211,12 +211,13 @@ def test_mg_extrapolated_guess(nusif_lib, solver, guess):
         assert rel_err(fields[guess][f], fields["previous"][f]) < 1e-5, f
 
 
-@pytest.mark.parametrize("guess", ["extrapolate", "quadratic"])
+@pytest.mark.parametrize("guess", ["extrapolate", "quadratic", "cubic"])
 def test_warm_start_values(nusif_lib, guess):
     """The warm start itself: with rtol 1e30 a solve stops after its first
     residual, so p after solve() is the extrapolated start. Four solves from
     pressures A, B, C, D give A, 2B - A, then 3C - 3B + A and 3D - 3C + B
-    (quadratic; the history buffers alternate roles) or 2C - B and 2D - C
+    (quadratic; the history buffers alternate roles), 3C - 3B + A and
+    4D - 6C + 4B - A (cubic; three buffers rotate) or 2C - B and 2D - C
     (linear), over the whole interior."""
     rng = np.random.default_rng(43)
     with _sim((24, 16, 12), "mg-mixed", 1e30, mg_guess=guess) as sim:
@@ -231,6 +232,8 @@ def test_warm_start_values(nusif_lib, guess):
         A, B, C, D = (x[1:-1, 1:-1, 1:-1] for x in pres)
         if guess == "quadratic":
             want = [A, 2 * B - A, 3 * (C - B) + A, 3 * (D - C) + B]
+        elif guess == "cubic":
+            want = [A, 2 * B - A, 3 * (C - B) + A, 4 * D - 6 * C + 4 * B - A]
         else:
             want = [A, 2 * B - A, 2 * C - B, 2 * D - C]
         for q in range(4):
