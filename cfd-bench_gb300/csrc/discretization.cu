@@ -561,22 +561,22 @@ __global__ void __launch_bounds__(kBlock) k_shell_max3(Dims g, const double *__r
     const double *__restrict__ v, const double *__restrict__ w, unsigned long long *amax_slots,
     double *__restrict__ partials, unsigned *ticket, double *__restrict__ out3)
 {
-  const int64_t P = g.imax + 2, PQ = (int64_t)g.sk;
-  const int64_t n1 = 2 * PQ, n2 = (int64_t)g.kmax * 2 * P, n3 = (int64_t)g.kmax * g.jmax * 2;
+  // 32-bit indices: the padded size is below 2^31 (checked at init)
+  const int P = g.imax + 2, PQ = g.sk;
+  const int n1 = 2 * PQ, n2 = g.kmax * 2 * P, n3 = g.kmax * g.jmax * 2;
   unsigned uh = 0u, ul = 0u, vh = 0u, vl = 0u, wh = 0u, wl = 0u;
-  for (int64_t q = blockIdx.x * (int64_t)kBlock + threadIdx.x; q < n1 + n2 + n3;
-       q += (int64_t)gridDim.x * kBlock) {
-    int64_t c;
+  for (int q = blockIdx.x * kBlock + threadIdx.x; q < n1 + n2 + n3; q += gridDim.x * kBlock) {
+    int c;
     if (q < n1) {
-      c = q < PQ ? q : (int64_t)(g.kmax + 1) * PQ + (q - PQ);
+      c = q < PQ ? q : (g.kmax + 1) * PQ + (q - PQ);
     } else if (q < n1 + n2) {
-      const int64_t r = q - n1;
-      const int64_t k = 1 + r / (2 * P), rr = r % (2 * P);
-      c = k * PQ + (rr < P ? rr : (int64_t)(g.jmax + 1) * g.sj + (rr - P));
+      const int r = q - n1;
+      const int k = 1 + r / (2 * P), rr = r - (k - 1) * (2 * P);
+      c = k * PQ + (rr < P ? rr : (g.jmax + 1) * g.sj + (rr - P));
     } else {
-      const int64_t r = q - n1 - n2;
-      const int64_t k = 1 + r / (2 * g.jmax), rr = r % (2 * g.jmax);
-      c = k * PQ + (1 + rr / 2) * g.sj + ((rr & 1) ? g.imax + 1 : 0);
+      const int r = q - n1 - n2;
+      const int k = 1 + r / (2 * g.jmax), rr = r - (k - 1) * (2 * g.jmax);
+      c = k * PQ + (1 + (rr >> 1)) * g.sj + ((rr & 1) ? g.imax + 1 : 0);
     }
     abs_max_key(uh, ul, u[c]);
     abs_max_key(vh, vl, v[c]);
