@@ -314,6 +314,7 @@ def run_gpu(args, rank, world, local):
 
     # ---- dominant kernels, timed live with CUDA events on the library stream ----
     roofs = [] if args.no_roofline else kernel_rooflines(sim, solver, stream, ncell, args.arith)
+    live_shares(roofs, solver, head["iters"], head["ms_per_step"], MG_SHAPE["mg-mixed"][2])
 
     phases = step_phases(sim, solver, stream) if args.phases else None
 
@@ -578,12 +579,43 @@ def _traffic(kernel: str, ncell: int):
 
 
 def dominant(roofs: list[dict]):
-    """The entry of the kernel with the largest share of the step's device time
-    (the share measured in the committed ncu launch list of the same step);
-    ties or missing shares keep the first entry."""
+    """The entry of the kernel with the largest share of the step's device time:
+    the live share (launch time x launches per step / ms per step) where the
+    launches per step are known, else the share in the committed ncu launch
+    list of the same step; ties or missing shares keep the first entry."""
     if not roofs:
         return None
-    return max(roofs, key=lambda r: r.get("share_of_step") or 0.0)
+    return max(roofs, key=lambda r: r.get("share_of_step_live") or r.get("share_of_step") or 0.0)
+
+
+def live_shares(roofs: list[dict], solver: str, iters, ms_per_step: float, inner: int) -> None:
+    """Adds ``launches_per_step`` and ``share_of_step_live`` to each entry:
+    computeFG runs once per step; the mixed solver's fine sweep twice per FP32
+    V-cycle (the solve graph's finest level starts every V-cycle from the
+    residual kernel's zeroed correction with a general sweep) and its fine
+    residual once per refinement step plus once before the first; the FP64
+    smoother's colour pass 2 x (pre + post) per V-cycle; a red-black SOR
+    iteration two colour passes."""
+    if not iters or not ms_per_step:
+        return
+    mean_it = sum(iters) / len(iters)
+    pre, post = MG_SHAPE["mg"][0], MG_SHAPE["mg"][1]
+    for r in roofs:
+        k = r.get("kernel", "")
+        n = None
+        if k.startswith("k_fgh"):
+            n = 1.0
+        elif k.startswith("k_rbgs_sweep"):
+            n = 2.0 * mean_it
+        elif k.startswith("k_mx_residual"):
+            n = sum(-(-it // inner) + 1 for it in iters) / len(iters)
+        elif k.startswith("k_mg_smooth"):
+            n = 2.0 * (pre + post) * mean_it
+        elif k.startswith("k_sor_pass"):
+            n = 2.0 * mean_it
+        if n is not None:
+            r["launches_per_step"] = n
+            r["share_of_step_live"] = r["launch_ms"] * n / ms_per_step
 
 
 # FP64 issue peak of a GB300: 2 FP64 lanes per SM and clock

@@ -78,3 +78,28 @@ def test_headline_network_file():
     assert np.all(np.isfinite(z["params"]))
     meta = saved_meta(path)
     assert meta["pairs"] > 0 and "seed" in meta["cases"]
+
+
+def test_roofline_kernel_is_the_largest_live_share():
+    """The line's roofline entry is the kernel with the largest live share of
+    the step: launch time x launches per step / ms per step (computeFG once,
+    the fine sweep twice per V-cycle, the fine residual once per refinement
+    step plus once), not the cold-cache ncu share."""
+    roofs = [
+        {"kernel": "k_rbgs_sweep_v: sweep", "launch_ms": 0.056, "share_of_step": 0.199},
+        {"kernel": "k_mx_residual_df: residual", "launch_ms": 0.146, "share_of_step": 0.088},
+        {"kernel": "k_fgh_df: computeFG", "launch_ms": 0.685, "share_of_step": 0.176},
+    ]
+    bench.live_shares(roofs, "mg-mixed", [4, 4, 4, 5], 2.72, 4)
+    by = {r["kernel"].split(":")[0]: r for r in roofs}
+    assert by["k_fgh_df"]["launches_per_step"] == 1.0
+    assert by["k_rbgs_sweep_v"]["launches_per_step"] == pytest.approx(2 * 4.25)
+    # 4 V-cycles: one refinement step (+1); 5: two (+1)
+    assert by["k_mx_residual_df"]["launches_per_step"] == pytest.approx((2 + 2 + 2 + 3) / 4)
+    assert by["k_fgh_df"]["share_of_step_live"] == pytest.approx(0.685 / 2.72)
+    assert bench.dominant(roofs)["kernel"].startswith("k_fgh_df")
+    # without live shares the committed list's shares decide
+    bare = [dict(r) for r in roofs]
+    for r in bare:
+        r.pop("share_of_step_live")
+    assert bench.dominant(bare)["kernel"].startswith("k_rbgs_sweep_v")
