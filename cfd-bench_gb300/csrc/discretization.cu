@@ -863,13 +863,16 @@ using namespace nusif;
 
 namespace {
 
-// the launch stream waits for queued asynchronous copies of these fields
-bool await_arrays(std::initializer_list<const double *> fields)
+// the launch stream waits for queued asynchronous copies of the fields an
+// entry point reads (their uploads) and writes (every copy)
+bool await_arrays(std::initializer_list<const double *> reads,
+    std::initializer_list<const double *> writes)
 {
-  const void *f[8];
-  int n = 0;
-  for (const double *x : fields) f[n++] = x;
-  return await_copies(f, n);
+  const void *r[8], *w[8];
+  int nr = 0, nw = 0;
+  for (const double *x : reads) r[nr++] = x;
+  for (const double *x : writes) w[nw++] = x;
+  return await_uploads(r, nr) && await_copies(w, nw);
 }
 
 DiscState *need_state(const Discretization *d, const char *what)
@@ -1017,7 +1020,7 @@ void initDiscretization(Discretization *s, Parameter *params)
 void computeTimestep(Discretization *s)
 {
   DiscState *st = need_state(s, "computeTimestep");
-  if (!st || !await_arrays({ s->u, s->v, s->w })) return;
+  if (!st || !await_arrays({ s->u, s->v, s->w }, {})) return;
   if (st->ext.fuse_dt && st->amax == kAmaxValid) {
     // the interior maxima came with the last adaptUV: read the ghost shell only
     if (!launch_shell_max3(st->dims, s->u, s->v, s->w, st->d_amax, st->red, st->d_scalars))
@@ -1050,7 +1053,7 @@ void computeTimestep(Discretization *s)
 void setBoundaryConditions(Discretization *s)
 {
   DiscState *st = need_state(s, "setBoundaryConditions");
-  if (!st || !await_arrays({ s->u, s->v, s->w })) return;
+  if (!st || !await_arrays({}, { s->u, s->v, s->w })) return;
   const int bc[6] = { s->bcLeft, s->bcRight, s->bcBottom, s->bcTop, s->bcFront, s->bcBack };
   velocity_written(st);
   launch_bc(st->dims, bc, PROBLEM_NONE, 0.0, 0.0, s->u, s->v, s->w);
@@ -1060,7 +1063,7 @@ void setBoundaryConditions(Discretization *s)
 void setSpecialBoundaryCondition(Discretization *s)
 {
   DiscState *st = need_state(s, "setSpecialBoundaryCondition");
-  if (!st || !await_arrays({ s->u })) return;
+  if (!st || !await_arrays({}, { s->u })) return;
   velocity_written(st);
   launch_special(st->dims, problem_code(s->problem), st->ext.lid, st->ext.inflow, s->u);
 }
@@ -1068,7 +1071,7 @@ void setSpecialBoundaryCondition(Discretization *s)
 void computeFG(Discretization *s)
 {
   DiscState *st = need_state(s, "computeFG");
-  if (!st || !await_arrays({ s->u, s->v, s->w, s->f, s->g, s->h })) return;
+  if (!st || !await_arrays({ s->u, s->v, s->w }, { s->f, s->g, s->h })) return;
   launch_fgh(st->dims, s->re, s->gamma, s->gx, s->gy, s->gz, s->dt, s->grid.dx, s->grid.dy,
       s->grid.dz, s->u, s->v, s->w, s->f, s->g, s->h, nullptr, 0, st->ext.fg_fp64 != 0);
 }
@@ -1076,14 +1079,14 @@ void computeFG(Discretization *s)
 void computeRHS(Discretization *s)
 {
   DiscState *st = need_state(s, "computeRHS");
-  if (!st || !await_arrays({ s->f, s->g, s->h, s->rhs })) return;
+  if (!st || !await_arrays({ s->f, s->g, s->h }, { s->rhs })) return;
   launch_rhs(st->dims, s->dt, s->grid.dx, s->grid.dy, s->grid.dz, s->f, s->g, s->h, s->rhs);
 }
 
 void normalizePressure(Discretization *s)
 {
   DiscState *st = need_state(s, "normalizePressure");
-  if (!st || !await_arrays({ s->p })) return;
+  if (!st || !await_arrays({}, { s->p })) return;
   if (!launch_interior_sum(st->dims, s->p, st->red, st->d_scalars + 3)) return;
   launch_subtract_mean(st->dims, s->p, st->d_scalars + 4);
 }
@@ -1091,7 +1094,7 @@ void normalizePressure(Discretization *s)
 void adaptUV(Discretization *s)
 {
   DiscState *st = need_state(s, "adaptUV");
-  if (!st || !await_arrays({ s->f, s->g, s->h, s->p, s->u, s->v, s->w })) return;
+  if (!st || !await_arrays({ s->f, s->g, s->h, s->p }, { s->u, s->v, s->w })) return;
   // fuse_dt: the first adaptUV after computeTimestep keeps the maxima of what it writes
   // (not with host_fields, whose arrays host code may write directly)
   const bool keep = st->ext.fuse_dt && !st->ext.host_fields && st->amax == kAmaxReset;

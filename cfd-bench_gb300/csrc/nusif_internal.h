@@ -15,8 +15,11 @@ bool cuda_ok(cudaError_t e, const char *what);  // false after recording a failu
 bool has_error();                              // an error is pending (record mode)
 cudaStream_t stream();
 // asynchronous field copies (runtime.cpp): make the launch stream wait for the
-// queued copies of these device arrays / of every array / of d's eight fields
+// queued copies of these device arrays (before work that writes them) / for
+// their queued uploads only (before work that only reads them) / of every
+// array / of d's eight fields
 bool await_copies(const void *const *ptrs, int n);
+bool await_uploads(const void *const *ptrs, int n);
 bool await_all_copies();
 bool await_fields(const Discretization *d);
 // after every kernel launch: counts it and checks the launch error

@@ -119,11 +119,20 @@ void disc_state_erase(const Discretization *d)
 // The first later entry point that touches that pointer makes the launch
 // stream wait for the event (on the device: the host does not wait), so an
 // upload can overlap the kernels that do not read its field, and a queued
-// download is never overwritten by a later kernel.
+// download is never overwritten by a later kernel. A kernel that only reads
+// the field waits for a pending upload but not for a pending download (both
+// only read the device array), so a download of p can overlap adaptUV.
 namespace {
+// the copies of one device array still in flight: `done` completes with the
+// last of them (the copy stream runs them in order); `upload`: one of them
+// writes the array
+struct Pending {
+  cudaEvent_t done = nullptr;
+  bool upload = false;
+};
 std::mutex g_copy_mu;
-std::unordered_map<int, cudaStream_t> g_copy_streams;     // device -> copy stream
-std::unordered_map<const void *, cudaEvent_t> g_pending;  // device pointer -> its last copy
+std::unordered_map<int, cudaStream_t> g_copy_streams;  // device -> copy stream
+std::unordered_map<const void *, Pending> g_pending;   // device pointer -> its copies in flight
 std::vector<cudaEvent_t> g_spare_events;
 
 cudaEvent_t take_event()
@@ -164,11 +173,13 @@ bool queue_copy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, c
             cuda_ok(cudaMemcpyAsync(dst, src, bytes, kind, cs), "field copy");
   g_spare_events.push_back(after);  // the wait is queued: the event may be recorded again
   if (!ok) return false;
-  auto it = g_pending.find(field);
-  cudaEvent_t done = it != g_pending.end() ? it->second : take_event();
-  if (!done) return false;
-  g_pending[field] = done;
-  return cuda_ok(cudaEventRecord(done, cs), "copy done record");
+  Pending &pd = g_pending[field];
+  if (!pd.done) pd.done = take_event();
+  if (!pd.done) return false;
+  // re-recording the event makes it the completion of this copy, which in
+  // stream order implies the earlier ones
+  if (kind == cudaMemcpyHostToDevice) pd.upload = true;
+  return cuda_ok(cudaEventRecord(pd.done, cs), "copy done record");
 }
 
 }  // namespace
@@ -181,8 +192,23 @@ bool await_copies(const void *const *ptrs, int n)
   for (int q = 0; q < n; q++) {
     auto it = g_pending.find(ptrs[q]);
     if (it == g_pending.end()) continue;
-    ok = cuda_ok(cudaStreamWaitEvent(g_stream, it->second, 0), "wait for field copy") && ok;
-    g_spare_events.push_back(it->second);
+    ok = cuda_ok(cudaStreamWaitEvent(g_stream, it->second.done, 0), "wait for field copy") && ok;
+    g_spare_events.push_back(it->second.done);
+    g_pending.erase(it);
+  }
+  return ok;
+}
+
+bool await_uploads(const void *const *ptrs, int n)
+{
+  std::lock_guard<std::mutex> lock(g_copy_mu);
+  if (g_pending.empty()) return true;
+  bool ok = true;
+  for (int q = 0; q < n; q++) {
+    auto it = g_pending.find(ptrs[q]);
+    if (it == g_pending.end() || !it->second.upload) continue;  // downloads only: reads go on
+    ok = cuda_ok(cudaStreamWaitEvent(g_stream, it->second.done, 0), "wait for field upload") && ok;
+    g_spare_events.push_back(it->second.done);
     g_pending.erase(it);
   }
   return ok;
@@ -193,8 +219,8 @@ bool await_all_copies()
   std::lock_guard<std::mutex> lock(g_copy_mu);
   bool ok = true;
   for (auto &kv : g_pending) {
-    ok = cuda_ok(cudaStreamWaitEvent(g_stream, kv.second, 0), "wait for field copy") && ok;
-    g_spare_events.push_back(kv.second);
+    ok = cuda_ok(cudaStreamWaitEvent(g_stream, kv.second.done, 0), "wait for field copy") && ok;
+    g_spare_events.push_back(kv.second.done);
   }
   g_pending.clear();
   return ok;
@@ -254,7 +280,7 @@ int nusifDownloadField(const Discretization *d, int which, double *host)
   }
   size_t bytes = sizeof(double) * (size_t)st->dims.padded;
   const void *fp = src;
-  if (!await_copies(&fp, 1)) return NUSIF_ERR_CUDA;
+  if (!await_uploads(&fp, 1)) return NUSIF_ERR_CUDA;
   if (!cuda_ok(cudaMemcpyAsync(host, src, bytes, cudaMemcpyDeviceToHost, g_stream),
           "download field"))
     return NUSIF_ERR_CUDA;
@@ -326,7 +352,7 @@ int nusifWaitCopies(void)
   if (!ok) return NUSIF_ERR_CUDA;
   // every queued copy has ended: nothing is pending any more
   std::lock_guard<std::mutex> lock(g_copy_mu);
-  for (auto &kv : g_pending) g_spare_events.push_back(kv.second);
+  for (auto &kv : g_pending) g_spare_events.push_back(kv.second.done);
   g_pending.clear();
   return NUSIF_OK;
 }

@@ -495,8 +495,8 @@ double solve(Solver *s, double *p, const double *rhs)
     fail(NUSIF_ERR_STATE, "solve: solver not initialised by initSolver");
     return NAN;
   }
-  const void *fields[2] = { p, rhs };
-  if (!await_copies(fields, 2)) return NAN;
+  const void *pf = p, *rf = rhs;
+  if (!await_uploads(&rf, 1) || !await_copies(&pf, 1)) return NAN;
   switch (ss->kind) {
   case SOLVER_RB: return solve_rb(s, ss, p, rhs);
   case SOLVER_MG_REF: return solve_mg_ref(s, ss, p, rhs);

@@ -141,7 +141,9 @@ class Simulation:
         return self.lib.nusifSolverIterations(C.byref(self.s))
 
     # ---- the time loop body, reference src/main.c:61-79 ----
-    def step(self) -> StepInfo:
+    def step(self, after_solve=None) -> StepInfo:
+        """One time step. ``after_solve``: called between solve() and adaptUV
+        (p is final there: a queued download of p can overlap adaptUV)."""
         if self.d.tau > 0.0:
             self.compute_timestep()
         self.set_boundary_conditions()
@@ -152,6 +154,8 @@ class Simulation:
             self.normalize_pressure()
         res = self.solve()
         it = self.iterations
+        if after_solve is not None:
+            after_solve()
         self.adapt_uv()
         dt = self.d.dt
         self.t += dt

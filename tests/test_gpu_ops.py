@@ -231,7 +231,9 @@ def test_queued_field_copies_match_synchronous_copies(nusif_lib):
     and downloaded to pinned host arrays: with the queued copies
     (nusifUploadFieldAsync / nusifDownloadFieldAsync / nusifWaitCopies, the
     library's kernels waiting on the device for the fields they use) the host
-    arrays end bit-identical to the same loop with the synchronous copies."""
+    arrays end bit-identical to the same loop with the synchronous copies,
+    also with p's download queued between solve() and adaptUV (which reads p
+    while the copy runs and does not wait for it)."""
     import ctypes as C
 
     import torch
@@ -241,21 +243,25 @@ def test_queued_field_copies_match_synchronous_copies(nusif_lib):
     vals = cavity(24, te=1e9, solver="mg-mixed", rtol=1e-8, mg_guess="quadratic")
     idx = abi.FIELD_INDEX
     out = {}
-    for mode in ("sync", "queued"):
+    for mode in ("sync", "queued", "p_early"):
         with Simulation(vals) as sim:
             n = int(np.prod(sim.padded_shape))
             host = {f: torch.zeros(n, dtype=torch.float64, pin_memory=True) for f in "uvwp"}
             ptrs = {f: C.cast(host[f].data_ptr(), abi.c_double_p) for f in "uvwp"}
+            down = nusif_lib.nusifDownloadField if mode == "sync" else \
+                nusif_lib.nusifDownloadFieldAsync
             for _ in range(3):
                 for f in "uvwp":
                     fn = nusif_lib.nusifUploadField if mode == "sync" else \
                         nusif_lib.nusifUploadFieldAsync
                     assert fn(C.byref(sim.d), idx[f], ptrs[f]) == 0
-                sim.step()
+                early = "p" if mode == "p_early" else ""
+                sim.step(after_solve=(lambda: down(C.byref(sim.d), idx["p"], ptrs["p"]))
+                         if early else None)
                 for f in "uvwp":
-                    fn = nusif_lib.nusifDownloadField if mode == "sync" else \
-                        nusif_lib.nusifDownloadFieldAsync
-                    assert fn(C.byref(sim.d), idx[f], ptrs[f]) == 0
+                    if f == early:
+                        continue
+                    assert down(C.byref(sim.d), idx[f], ptrs[f]) == 0
                 assert nusif_lib.nusifWaitCopies() == 0
                 abi.check(nusif_lib)
             out[mode] = {f: host[f].numpy().copy() for f in "uvwp"}
@@ -264,3 +270,29 @@ def test_queued_field_copies_match_synchronous_copies(nusif_lib):
     for f in "uvwp":
         assert np.any(out["sync"][f] != 0.0) or f != "u"
         np.testing.assert_array_equal(out["queued"][f], out["sync"][f])
+        np.testing.assert_array_equal(out["p_early"][f], out["sync"][f])
+
+
+def test_write_after_queued_download_waits_for_it(nusif_lib):
+    """A queued download of p followed at once by an entry point that writes p
+    (normalizePressure): the write waits for the copy on the device, so the
+    host array holds p as it was when the download was queued."""
+    import ctypes as C
+
+    import torch
+
+    from nusif import Simulation, abi
+    from nusif.params import cavity
+    rng = np.random.default_rng(61)
+    with Simulation(cavity((40, 36, 33), te=1e9)) as sim:
+        p0 = rng.standard_normal(sim.padded_shape) + 3.0
+        sim.set_field("p", p0)
+        n = int(np.prod(sim.padded_shape))
+        host = torch.zeros(n, dtype=torch.float64, pin_memory=True)
+        ptr = C.cast(host.data_ptr(), abi.c_double_p)
+        assert nusif_lib.nusifDownloadFieldAsync(C.byref(sim.d), abi.FIELD_INDEX["p"], ptr) == 0
+        sim.normalize_pressure()  # subtracts the mean from p on the device
+        assert nusif_lib.nusifWaitCopies() == 0
+        abi.check(nusif_lib)
+        np.testing.assert_array_equal(host.numpy().reshape(sim.padded_shape), p0)
+        assert not np.array_equal(sim.field("p"), p0)
