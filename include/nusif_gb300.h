@@ -164,9 +164,12 @@ NUSIF_API int nusifUploadField(Discretization *d, int which, const double *host)
 /* The same copies queued asynchronously (no counterpart in the reference,
  * whose fields live in host memory): each runs on a copy stream of the
  * library after the work already queued on the launch stream, and the first
- * later call taking the Discretization (or solve() with the field as p or
- * rhs) waits for it on the device, not on the host -- so an upload of p
- * overlaps computeTimestep .. computeRHS, which do not read p. The host array
+ * later call that uses the field (or solve() with it as p or rhs) waits for it
+ * on the device, not on the host -- a call that writes the field for every
+ * queued copy of it, a call that only reads it for its queued uploads only --
+ * so an upload of p overlaps computeTimestep .. computeRHS, which do not read
+ * p, and a download of p queued after solve() overlaps adaptUV, which only
+ * reads it. The host array
  * must stay untouched, and a downloaded one unread, until nusifWaitCopies()
  * returns; pinned host memory makes the copies asynchronous. Entry points
  * that take bare device pointers and the batch API do not wait per field:
