@@ -925,8 +925,10 @@ def run_channel(args, local):
     lib.nusifSetStream(C.c_void_p(stream.cuda_stream))
     steps = args.steps
     # the FP64 run is FP64 throughout (every stencil in FP64 instructions)
-    sims = {"mg-mixed": nusif.Simulation(channel(solver="mg-mixed", rtol=1e-8, arith=args.arith)),
-            "mg": nusif.Simulation(channel(solver="mg", rtol=1e-8, arith="fp64"))}
+    # fuse_dt: the CFL maxima from adaptUV in both runs (the same dt bit for bit)
+    sims = {"mg-mixed": nusif.Simulation(channel(solver="mg-mixed", rtol=1e-8, arith=args.arith,
+                                                 fuse_dt=1)),
+            "mg": nusif.Simulation(channel(solver="mg", rtol=1e-8, arith="fp64", fuse_dt=1))}
     shape = sims["mg"].padded_shape
 
     def view(sim, f):
