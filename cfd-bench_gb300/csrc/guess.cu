@@ -133,23 +133,37 @@ __device__ __forceinline__ void block_partials(double (&v)[K], double *partial)
   }
 }
 
+// component k of K per-block partials stored interleaved, summed by one whole
+// block in a fixed order (thread t takes the blocks t, t + kNT, ..., then a
+// fixed tree): deterministic, and the same order for every call on the same
+// sequence of partials
+template <int K>
+__device__ __forceinline__ double fold_k(const double *partial, int nb, int k, double *sm)
+{
+  double s = 0.0;
+  for (int q = threadIdx.x; q < nb; q += kNT) s += partial[K * q + k];
+  return block_reduce_sum<kNT>(s, sm);
+}
+
+// sum of b over the interior: a block per interior row (j, k), its threads
+// along the row
 __global__ void __launch_bounds__(kNT) k_g_sum_b(GGeom g, const double *b, double *partial)
 {
-  const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+  const int rows = g.ny * g.nz;
   double v[1] = { 0.0 };
-  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n; q += (int64_t)gridDim.x * kNT) {
-    const int i = (int)(q % g.nx);
-    const int64_t r = q / g.nx;
-    v[0] += b[g.pidx(i, (int)(r % g.ny), (int)(r / g.ny))];
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+    const double *row = b + g.pidx(0, r % g.ny, r / g.ny);
+    for (int i = threadIdx.x; i < g.nx; i += kNT) v[0] += row[i];
   }
   block_partials<1>(v, partial);
 }
 
-__global__ void k_g_fold_shift(const double *partial, int nb, int64_t n, GuessStats *st)
+__global__ void __launch_bounds__(kNT) k_g_fold_shift(const double *partial, int nb, int64_t n,
+    GuessStats *st)
 {
-  double s = 0.0;
-  for (int q = 0; q < nb; q++) s += partial[q];
-  st->shift = s / (double)n;
+  __shared__ double sm[kNT / 32];
+  const double s = fold_k<1>(partial, nb, 0, sm);
+  if (threadIdx.x == 0) st->shift = s / (double)n;
 }
 
 // one thread per coarse cell: restricted residual and rhs (unnormalised) into
@@ -164,10 +178,10 @@ __global__ void __launch_bounds__(kNT) k_g_features(GGeom g, GPairs pc, const do
   GPairs c = pc;
   c.ms = df::split(-st->shift);
   double v[4] = { 0.0, 0.0, 0.0, 0.0 };
-  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n; q += (int64_t)gridDim.x * kNT) {
-    const int I = (int)(q % cx);
-    const int64_t r = q / cx;
-    const int J = (int)(r % cy), K = (int)(r / cy);
+  // 32-bit indices: the padded grid is below 2^31 cells (checked at init)
+  for (int q = blockIdx.x * kNT + threadIdx.x; q < (int)n; q += gridDim.x * kNT) {
+    const int I = q % cx, r = q / cx;
+    const int J = r % cy, K = r / cy;
     df::f2 rs, bs;
     float rr2, bb2;
     coarse_features(g, c, p, b, I, J, K, rs, bs, rr2, bb2);
@@ -181,11 +195,13 @@ __global__ void __launch_bounds__(kNT) k_g_features(GGeom g, GPairs pc, const do
   block_partials<4>(v, partial);
 }
 
-__global__ void k_g_fold_features(const double *partial, int nb, int64_t nc, GuessStats *st)
+__global__ void __launch_bounds__(kNT) k_g_fold_features(const double *partial, int nb,
+    int64_t nc, GuessStats *st)
 {
-  double t[4] = { 0.0, 0.0, 0.0, 0.0 };
-  for (int q = 0; q < nb; q++)
-    for (int k = 0; k < 4; k++) t[k] += partial[4 * q + k];
+  __shared__ double sm[kNT / 32];
+  double t[4];
+  for (int k = 0; k < 4; k++) t[k] = fold_k<4>(partial, nb, k, sm);
+  if (threadIdx.x != 0) return;
   st->r2_warm = t[0];
   st->nb2 = t[1];
   st->rc2 = t[2];
@@ -237,37 +253,37 @@ __global__ void k_g_candidate(GGeom g, const double *p0, const float *out, const
     double *p1)
 {
   const int cx = g.nx / 2, cy = g.ny / 2, cz = g.nz / 2;
-  const int64_t n = (int64_t)g.nx * g.ny * g.nz;
   const float scale = (float)(st->sigma_r / g.kappa);
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
-       q += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(q % g.nx);
-    const int64_t r = q / g.nx;
-    const int j = (int)(r % g.ny), k = (int)(r / g.ny);
-    const int P[3] = { i >> 1, j >> 1, k >> 1 };
-    const int C[3] = { cx, cy, cz };
-    const int F[3] = { i, j, k };
-    int Q[3];
-    for (int a = 0; a < 3; a++) {
-      const int nb = (F[a] & 1) ? P[a] + 1 : P[a] - 1;
-      Q[a] = (nb < 0 || nb >= C[a]) ? P[a] : nb;
-    }
-    float e = 0.0f;
+  // a block per interior row (j, k), its threads along the row
+  for (int row = blockIdx.x; row < g.ny * g.nz; row += gridDim.x) {
+    const int j = row % g.ny, k = row / g.ny;
+    for (int i = threadIdx.x; i < g.nx; i += blockDim.x) {
+      const int P[3] = { i >> 1, j >> 1, k >> 1 };
+      const int C[3] = { cx, cy, cz };
+      const int F[3] = { i, j, k };
+      int Q[3];
+      for (int a = 0; a < 3; a++) {
+        const int nb = (F[a] & 1) ? P[a] + 1 : P[a] - 1;
+        Q[a] = (nb < 0 || nb >= C[a]) ? P[a] : nb;
+      }
+      float e = 0.0f;
 #pragma unroll
-    for (int c = 0; c < 8; c++) {
-      const int X = (c & 1) ? Q[0] : P[0], Y = ((c >> 1) & 1) ? Q[1] : P[1], Z = (c >> 2) ? Q[2] : P[2];
-      const float w = ((c & 1) ? 0.25f : 0.75f) * (((c >> 1) & 1) ? 0.25f : 0.75f) * ((c >> 2) ? 0.25f : 0.75f);
-      e = fmaf(w, out[((int64_t)Z * cy + Y) * cx + X], e);
+      for (int c = 0; c < 8; c++) {
+        const int X = (c & 1) ? Q[0] : P[0], Y = ((c >> 1) & 1) ? Q[1] : P[1], Z = (c >> 2) ? Q[2] : P[2];
+        const float w = ((c & 1) ? 0.25f : 0.75f) * (((c >> 1) & 1) ? 0.25f : 0.75f) *
+                        ((c >> 2) ? 0.25f : 0.75f);
+        e = fmaf(w, out[(Z * cy + Y) * cx + X], e);
+      }
+      const int64_t pc = g.pidx(i, j, k);
+      const double v = p0[pc] + to_f64(e * scale);
+      p1[pc] = v;
+      if (i == 0) p1[pc - 1] = v;
+      if (i == g.nx - 1) p1[pc + 1] = v;
+      if (j == 0) p1[pc - g.sj] = v;
+      if (j == g.ny - 1) p1[pc + g.sj] = v;
+      if (k == 0) p1[pc - g.sk] = v;
+      if (k == g.nz - 1) p1[pc + g.sk] = v;
     }
-    const int64_t pc = g.pidx(i, j, k);
-    const double v = p0[pc] + to_f64(e * scale);
-    p1[pc] = v;
-    if (i == 0) p1[pc - 1] = v;
-    if (i == g.nx - 1) p1[pc + 1] = v;
-    if (j == 0) p1[pc - g.sj] = v;
-    if (j == g.ny - 1) p1[pc + g.sj] = v;
-    if (k == 0) p1[pc - g.sk] = v;
-    if (k == g.nz - 1) p1[pc + g.sk] = v;
   }
 }
 
@@ -282,10 +298,10 @@ __global__ void __launch_bounds__(kNT) k_g_cand_norm(GGeom g, GPairs pc, const d
   GPairs c = pc;
   c.ms = df::split(-st->shift);
   double v[2] = { 0.0, 0.0 };
-  for (int64_t q = blockIdx.x * (int64_t)kNT + threadIdx.x; q < n; q += (int64_t)gridDim.x * kNT) {
-    const int I = (int)(q % cx);
-    const int64_t r = q / cx;
-    const int J = (int)(r % cy), K = (int)(r / cy);
+  // 32-bit indices: the padded grid is below 2^31 cells (checked at init)
+  for (int q = blockIdx.x * kNT + threadIdx.x; q < (int)n; q += gridDim.x * kNT) {
+    const int I = q % cx, r = q / cx;
+    const int J = r % cy, K = r / cy;
     df::f2 rs, bs;
     float rr2, bb2;
     coarse_features(g, c, p1, b, I, J, K, rs, bs, rr2, bb2);
@@ -298,13 +314,12 @@ __global__ void __launch_bounds__(kNT) k_g_cand_norm(GGeom g, GPairs pc, const d
 // the guess is kept when its restricted residual is smaller: the smooth error
 // is what the V-cycles pay for; the high-frequency residual that interpolating
 // a coarse correction leaves is removed by the first smoothing sweep
-__global__ void k_g_fold_select(const double *partial, int nb, GuessStats *st)
+__global__ void __launch_bounds__(kNT) k_g_fold_select(const double *partial, int nb,
+    GuessStats *st)
 {
-  double s = 0.0, sc = 0.0;
-  for (int q = 0; q < nb; q++) {
-    s += partial[2 * q];
-    sc += partial[2 * q + 1];
-  }
+  __shared__ double sm[kNT / 32];
+  const double s = fold_k<2>(partial, nb, 0, sm), sc = fold_k<2>(partial, nb, 1, sm);
+  if (threadIdx.x != 0) return;
   st->r2_cand = s;
   st->rc2_cand = sc;
   st->used = sc < st->rc2 ? 1 : 0;
@@ -384,12 +399,12 @@ bool features(GuessState *gs, const GGeom &g, const double *p, const double *rhs
   const int nb = flat(n);
   k_g_sum_b<<<nb, kNT, 0, stream()>>>(g, rhs, gs->partial);
   if (!launched("k_g_sum_b")) return false;
-  k_g_fold_shift<<<1, 1, 0, stream()>>>(gs->partial, nb, n, gs->d_stats);
+  k_g_fold_shift<<<1, kNT, 0, stream()>>>(gs->partial, nb, n, gs->d_stats);
   if (!launched("k_g_fold_shift")) return false;
   const int nbc = flat(gs->nc);
   k_g_features<<<nbc, kNT, 0, stream()>>>(g, gpairs(g), p, rhs, gs->d_stats, x, gs->partial);
   if (!launched("k_g_features")) return false;
-  k_g_fold_features<<<1, 1, 0, stream()>>>(gs->partial, nbc, gs->nc, gs->d_stats);
+  k_g_fold_features<<<1, kNT, 0, stream()>>>(gs->partial, nbc, gs->nc, gs->d_stats);
   if (!launched("k_g_fold_features")) return false;
   k_g_normalize<<<flat(gs->nc), 256, 0, stream()>>>(x, gs->nc, gs->d_stats);
   return launched("k_g_normalize");
@@ -424,7 +439,7 @@ bool guess_before_solve(GuessState *gs, const Grid *grid, double *p, const doubl
   const int nb = flat(gs->nc);  // the features' grid (same summation order)
   k_g_cand_norm<<<nb, kNT, 0, stream()>>>(g, gpairs(g), gs->aux, rhs, gs->d_stats, gs->partial);
   if (!launched("k_g_cand_norm")) return false;
-  k_g_fold_select<<<1, 1, 0, stream()>>>(gs->partial, nb, gs->d_stats);
+  k_g_fold_select<<<1, kNT, 0, stream()>>>(gs->partial, nb, gs->d_stats);
   if (!launched("k_g_fold_select")) return false;
   k_g_take<<<flat(padded), 256, 0, stream()>>>(p, gs->aux, padded, gs->d_stats);
   if (!launched("k_g_take")) return false;
