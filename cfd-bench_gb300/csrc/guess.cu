@@ -75,61 +75,23 @@ struct GGeom {
   }
 };
 
-// b - s - A p at fine interior cell (i, j, k), Neumann operator without
-// ghosts, in double-float pairs (about 2^-47 of the operands) on the FP32
-// pipe; nb = the pair of b - s at the cell
+// the operator's constants as double-float pairs: 1/h^2 per axis, -s
 struct GPairs {
-  df::f2 ex, ey, ez, ms;  // 1/h^2 per axis, -s
+  df::f2 ex, ey, ez, ms;
 };
-
-__device__ __forceinline__ df::f2 resid_df(const GGeom &g, const GPairs &c, const double *p,
-    const double *b, int i, int j, int k, df::f2 &nb)
-{
-  using namespace df;
-  const int64_t q = g.pidx(i, j, k);
-  const f2 xc = split(p[q]);
-  const f2 x2 = f2{ 2.0f * xc.hi, 2.0f * xc.lo };  // exact
-  const f2 xw = i > 0 ? split(p[q - 1]) : xc, xe = i < g.nx - 1 ? split(p[q + 1]) : xc;
-  const f2 xs = j > 0 ? split(p[q - g.sj]) : xc, xn = j < g.ny - 1 ? split(p[q + g.sj]) : xc;
-  const f2 xb = k > 0 ? split(p[q - g.sk]) : xc, xt = k < g.nz - 1 ? split(p[q + g.sk]) : xc;
-  f2 lap = mul_u(c.ex, sub_u(add_u(xw, xe), x2));
-  lap = fma_u(c.ey, sub_u(add_u(xs, xn), x2), lap);
-  lap = fma_u(c.ez, sub_u(add_u(xb, xt), x2), lap);
-  nb = add(split(b[q]), c.ms);
-  return sub(nb, lap);
-}
-
-// the features of one coarse cell: 8 children's residuals and b - s, their
-// means (pairs) and the sums of their squares (FP32 over the 8 children)
-__device__ __forceinline__ void coarse_features(const GGeom &g, const GPairs &c, const double *p,
-    const double *b, int I, int J, int K, df::f2 &rs, df::f2 &bs, float &rr2, float &bb2)
-{
-  using namespace df;
-  rs = f2{ 0.0f, 0.0f };
-  bs = f2{ 0.0f, 0.0f };
-  rr2 = 0.0f;
-  bb2 = 0.0f;
-#pragma unroll
-  for (int ch = 0; ch < 8; ch++) {
-    f2 nb;
-    const f2 rr = resid_df(g, c, p, b, 2 * I + (ch & 1), 2 * J + ((ch >> 1) & 1), 2 * K + (ch >> 2), nb);
-    rs = add(rs, rr);
-    bs = add(bs, nb);
-    rr2 = fmaf_(rr.hi, rr.hi, rr2);
-    bb2 = fmaf_(nb.hi, nb.hi, bb2);
-  }
-  rs = f2{ 0.125f * rs.hi, 0.125f * rs.lo };
-  bs = f2{ 0.125f * bs.hi, 0.125f * bs.lo };
-}
 
 template <int K>
 __device__ __forceinline__ void block_partials(double (&v)[K], double *partial)
 {
   __shared__ double sm[kNT / 32];
+  // one slot per block of a 1-, 2- or 3-D grid, written by its first thread
+  const int64_t bid =
+      blockIdx.x + (int64_t)gridDim.x * (blockIdx.y + (int64_t)gridDim.y * blockIdx.z);
+  const bool first = threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0;
 #pragma unroll
   for (int q = 0; q < K; q++) {
     const double t = block_reduce_sum<kNT>(v[q], sm);
-    if (threadIdx.x == 0) partial[(int64_t)blockIdx.x * K + q] = t;
+    if (first) partial[bid * K + q] = t;
   }
 }
 
@@ -166,33 +128,141 @@ __global__ void __launch_bounds__(kNT) k_g_fold_shift(const double *partial, int
   if (threadIdx.x == 0) st->shift = s / (double)n;
 }
 
-// one thread per coarse cell: restricted residual and rhs (unnormalised) into
-// x, and the four sums of squares; the residuals in double-float pairs (the
-// warm start's residual cancels b - A p to a small fraction of b), the squares
-// in FP32 over a coarse cell's children, then in FP64
-__global__ void __launch_bounds__(kNT) k_g_features(GGeom g, GPairs pc, const double *p,
-    const double *b, const GuessStats *st, float *x, double *partial)
+// The restricted residual R(b - s - A p) (and, with FEAT, R(b - s)) on 32 x 8
+// tiles of fine columns marching an even chunk of fine planes. Each fine
+// cell's residual b - s - A p of the ghost-free Neumann operator (a missing
+// neighbour is the cell itself) in double-float pairs (about 2^-47 of the
+// operands: the warm start's residual cancels b - A p to a small fraction of
+// b), from a shared-memory plane of p split once per block and plane with a
+// one-cell ring; a coarse cell's eight children combined in a fixed order: x
+// pairs by shuffle, z pairs in registers, y pairs through shared memory. The
+// squares are summed in FP32 over a coarse cell's children, then in FP64 per
+// thread and block. FEAT writes the features x (unnormalised) and four sums
+// of squares [fine residual, fine rhs, coarse residual, coarse rhs]; without
+// it the kernel writes the two of the candidate [fine, coarse residual] with
+// the same operations in the same order, so p1 == p0 gives the same bits.
+constexpr int kGX = 32, kGY = 8;
+template <bool FEAT>
+__global__ void __launch_bounds__(kNT) k_g_coarse(GGeom g, GPairs pc, const double *p,
+    const double *b, const GuessStats *st, float *x, double *partial, int kb)
 {
-  const int cx = g.nx / 2, cy = g.ny / 2, cz = g.nz / 2;
-  const int64_t n = (int64_t)cx * cy * cz;
-  GPairs c = pc;
-  c.ms = df::split(-st->shift);
-  double v[4] = { 0.0, 0.0, 0.0, 0.0 };
-  // 32-bit indices: the padded grid is below 2^31 cells (checked at init)
-  for (int q = blockIdx.x * kNT + threadIdx.x; q < (int)n; q += gridDim.x * kNT) {
-    const int I = q % cx, r = q / cx;
-    const int J = r % cy, K = r / cy;
-    df::f2 rs, bs;
-    float rr2, bb2;
-    coarse_features(g, c, p, b, I, J, K, rs, bs, rr2, bb2);
-    v[0] += to_f64(rr2);
-    v[1] += to_f64(bb2);
-    v[2] += to_f64(rs.hi * rs.hi);
-    v[3] += to_f64(bs.hi * bs.hi);
-    x[2 * q] = rs.hi;
-    x[2 * q + 1] = bs.hi;
+  using namespace df;
+  __shared__ f2 pl[2][kGY + 2][kGX + 2];
+  __shared__ float ysum[kGY / 2][kGX / 2][6];  // odd rows' pair sums: rs, bs (pairs), rr2, bb2
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kGX + tx;
+  const int i0 = blockIdx.x * kGX, j0 = blockIdx.y * kGY;
+  const bool act = i0 + tx < g.nx;  // rows: ny is a multiple of 8
+  const int i = min(i0 + tx, g.nx - 1), j = j0 + ty;
+  const int k0 = blockIdx.z * kb, k1 = min(k0 + kb, g.nz);
+  const auto at = [&](const double *a, int ii, int jj, int kk) {
+    return a[g.pidx(min(max(ii, 0), g.nx - 1), min(max(jj, 0), g.ny - 1), min(max(kk, 0), g.nz - 1))];
+  };
+  // ring cell of this thread (threads 0..79): rows j0-1 and j0+8, columns i0-1 and i0+32
+  const bool ring = tid < 2 * kGX + 2 * kGY;
+  int rr = 0, rc = 0;
+  if (ring) {
+    if (tid < 2 * kGX) {
+      rc = (tid & (kGX - 1)) + 1;
+      rr = tid < kGX ? 0 : kGY + 1;
+    } else {
+      const int q = tid - 2 * kGX;
+      rr = (q & (kGY - 1)) + 1;
+      rc = q < kGY ? 0 : kGX + 1;
+    }
   }
-  block_partials<4>(v, partial);
+  const f2 ex = pc.ex, ey = pc.ey, ez = pc.ez, ms = split(-st->shift);
+  f2 zb = split(at(p, i, j, k0 - 1)), zc = split(at(p, i, j, k0));
+  double xn = at(p, i, j, k0 + 1);
+  double rn = ring ? at(p, i0 - 1 + rc, j0 - 1 + rr, k0) : 0.0;
+  f2 zr{ 0.0f, 0.0f }, zq{ 0.0f, 0.0f };  // z-pair sums of the x-pair sums of residual and rhs
+  float zr2 = 0.0f, zb2 = 0.0f;
+  constexpr int NV = FEAT ? 4 : 2;
+  double v[NV];
+#pragma unroll
+  for (int q = 0; q < NV; q++) v[q] = 0.0;
+  const int cx = g.nx / 2, cy = g.ny / 2;
+  int buf = 0;
+  for (int k = k0; k < k1; k++) {
+    pl[buf][ty + 1][tx + 1] = zc;
+    if (ring) pl[buf][rr][rc] = split(rn);
+    const f2 zt = split(xn);
+    if (k + 1 < k1) {
+      xn = at(p, i, j, k + 2);
+      if (ring) rn = at(p, i0 - 1 + rc, j0 - 1 + rr, k + 1);
+    }
+    const double bv = at(b, i, j, k);
+    __syncthreads();
+    // this cell's residual: the ghost-free Neumann Laplacian in pairs
+    const f2 x2 = f2{ 2.0f * zc.hi, 2.0f * zc.lo };  // exact
+    f2 lap = mul_u(ex, sub_u(add_u(pl[buf][ty + 1][tx], pl[buf][ty + 1][tx + 2]), x2));
+    lap = fma_u(ey, sub_u(add_u(pl[buf][ty][tx + 1], pl[buf][ty + 2][tx + 1]), x2), lap);
+    lap = fma_u(ez, sub_u(add_u(zb, zt), x2), lap);
+    const f2 nb = add(split(bv), ms);
+    const f2 r = sub(nb, lap);
+    // x pairs (even lane + odd lane), then z pairs over the plane pair
+    const f2 ro{ __shfl_xor_sync(0xffffffffu, r.hi, 1), __shfl_xor_sync(0xffffffffu, r.lo, 1) };
+    const f2 bo{ __shfl_xor_sync(0xffffffffu, nb.hi, 1), __shfl_xor_sync(0xffffffffu, nb.lo, 1) };
+    const f2 xr = add(r, ro), xb = add(nb, bo);
+    const float xr2 = fmaf(ro.hi, ro.hi, r.hi * r.hi), xb2 = fmaf(bo.hi, bo.hi, nb.hi * nb.hi);
+    if (((k - k0) & 1) == 0) {
+      zr = xr;
+      zq = xb;
+      zr2 = xr2;
+      zb2 = xb2;
+    } else {
+      zr = add(zr, xr);
+      zq = add(zq, xb);
+      zr2 += xr2;
+      zb2 += xb2;
+      // y pairs: the odd row hands its sums to the even row
+      const bool lead = !(tx & 1);
+      if ((ty & 1) && lead) {
+        float *o = ysum[ty >> 1][tx >> 1];
+        o[0] = zr.hi;
+        o[1] = zr.lo;
+        o[2] = zq.hi;
+        o[3] = zq.lo;
+        o[4] = zr2;
+        o[5] = zb2;
+      }
+      __syncthreads();
+      if (!(ty & 1) && lead && act) {
+        const float *o = ysum[ty >> 1][tx >> 1];
+        f2 rs = add(zr, f2{ o[0], o[1] }), bs = add(zq, f2{ o[2], o[3] });
+        const float rr2 = zr2 + o[4], bb2 = zb2 + o[5];
+        rs = f2{ 0.125f * rs.hi, 0.125f * rs.lo };  // exact
+        bs = f2{ 0.125f * bs.hi, 0.125f * bs.lo };
+        v[0] += to_f64(rr2);
+        if (FEAT) {
+          v[1] += to_f64(bb2);
+          v[2] += to_f64(rs.hi * rs.hi);
+          v[3] += to_f64(bs.hi * bs.hi);
+          const int q = ((k >> 1) * cy + (j >> 1)) * cx + (i >> 1);
+          x[2 * q] = rs.hi;
+          x[2 * q + 1] = bs.hi;
+        } else {
+          v[NV - 1] += to_f64(rs.hi * rs.hi);
+        }
+      }
+    }
+    zb = zc;
+    zc = zt;
+    buf ^= 1;
+  }
+  block_partials<NV>(v, partial);
+}
+
+// the tiled kernel's grid: tiles of 32 x 8 columns, the planes in even chunks,
+// at most kBlocks blocks where the tiles allow (the partials buffer's size)
+dim3 coarse_grid(const GGeom &g, int &kb)
+{
+  const int tiles = ((g.nx + kGX - 1) / kGX) * (g.ny / kGY);
+  int chunks = tiles >= kBlocks ? 1 : kBlocks / tiles;
+  if (chunks > g.nz / 2) chunks = g.nz / 2;
+  if (chunks < 1) chunks = 1;
+  kb = ((g.nz / 2 + chunks - 1) / chunks) * 2;  // even
+  chunks = (g.nz + kb - 1) / kb;
+  return dim3((g.nx + kGX - 1) / kGX, g.ny / kGY, chunks);
 }
 
 __global__ void __launch_bounds__(kNT) k_g_fold_features(const double *partial, int nb,
@@ -287,30 +357,6 @@ __global__ void k_g_candidate(GGeom g, const double *p0, const float *out, const
   }
 }
 
-// ||b - s - A p1||^2 with the very arithmetic and summation order of
-// k_g_features (same grid, same per-thread walk over coarse cells and
-// children), so that p1 == p0 gives the same numbers bit for bit
-__global__ void __launch_bounds__(kNT) k_g_cand_norm(GGeom g, GPairs pc, const double *p1,
-    const double *b, const GuessStats *st, double *partial)
-{
-  const int cx = g.nx / 2, cy = g.ny / 2, cz = g.nz / 2;
-  const int64_t n = (int64_t)cx * cy * cz;
-  GPairs c = pc;
-  c.ms = df::split(-st->shift);
-  double v[2] = { 0.0, 0.0 };
-  // 32-bit indices: the padded grid is below 2^31 cells (checked at init)
-  for (int q = blockIdx.x * kNT + threadIdx.x; q < (int)n; q += gridDim.x * kNT) {
-    const int I = q % cx, r = q / cx;
-    const int J = r % cy, K = r / cy;
-    df::f2 rs, bs;
-    float rr2, bb2;
-    coarse_features(g, c, p1, b, I, J, K, rs, bs, rr2, bb2);
-    v[0] += to_f64(rr2);
-    v[1] += to_f64(rs.hi * rs.hi);
-  }
-  block_partials<2>(v, partial);
-}
-
 // the guess is kept when its restricted residual is smaller: the smooth error
 // is what the V-cycles pay for; the high-frequency residual that interpolating
 // a coarse correction leaves is removed by the first smoothing sweep
@@ -384,9 +430,13 @@ bool ensure(GuessState *gs, const Grid *grid)
   gs->nz = grid->kmax;
   gs->nc = (int64_t)gs->nx * gs->ny * gs->nz / 8;
   const size_t padded = (size_t)(gs->nx + 2) * (gs->ny + 2) * (gs->nz + 2);
+  // partials: kBlocks for the flat kernels, one per block of the tiled one (at
+  // least one per 32 x 8 tile)
+  const size_t tiles = (size_t)((gs->nx + kGX - 1) / kGX) * (gs->ny / kGY);
+  const size_t nparts = tiles > (size_t)kBlocks ? tiles : (size_t)kBlocks;
   return cuda_ok(cudaMalloc(&gs->x, gs->nc * 2 * sizeof(float)), "cudaMalloc(guess)") &&
          cuda_ok(cudaMalloc(&gs->aux, padded * sizeof(double)), "cudaMalloc(guess)") &&
-         cuda_ok(cudaMalloc(&gs->partial, kBlocks * 4 * sizeof(double)), "cudaMalloc(guess)") &&
+         cuda_ok(cudaMalloc(&gs->partial, nparts * 4 * sizeof(double)), "cudaMalloc(guess)") &&
          cuda_ok(cudaMalloc(&gs->d_stats, sizeof(GuessStats)), "cudaMalloc(guess)") &&
          cuda_ok(cudaMallocHost(&gs->h_stats, sizeof(GuessStats)), "cudaMallocHost(guess)") &&
          cuda_ok(cudaMemsetAsync(gs->d_stats, 0, sizeof(GuessStats), stream()), "guess init");
@@ -401,9 +451,12 @@ bool features(GuessState *gs, const GGeom &g, const double *p, const double *rhs
   if (!launched("k_g_sum_b")) return false;
   k_g_fold_shift<<<1, kNT, 0, stream()>>>(gs->partial, nb, n, gs->d_stats);
   if (!launched("k_g_fold_shift")) return false;
-  const int nbc = flat(gs->nc);
-  k_g_features<<<nbc, kNT, 0, stream()>>>(g, gpairs(g), p, rhs, gs->d_stats, x, gs->partial);
-  if (!launched("k_g_features")) return false;
+  int kb = 0;
+  const dim3 grid = coarse_grid(g, kb);
+  const int nbc = (int)(grid.x * grid.y * grid.z);
+  k_g_coarse<true><<<grid, dim3(kGX, kGY), 0, stream()>>>(g, gpairs(g), p, rhs, gs->d_stats, x,
+      gs->partial, kb);
+  if (!launched("k_g_coarse")) return false;
   k_g_fold_features<<<1, kNT, 0, stream()>>>(gs->partial, nbc, gs->nc, gs->d_stats);
   if (!launched("k_g_fold_features")) return false;
   k_g_normalize<<<flat(gs->nc), 256, 0, stream()>>>(x, gs->nc, gs->d_stats);
@@ -436,9 +489,13 @@ bool guess_before_solve(GuessState *gs, const Grid *grid, double *p, const doubl
   const int64_t n = (int64_t)g.nx * g.ny * g.nz;
   k_g_candidate<<<flat(n), 256, 0, stream()>>>(g, p, out, gs->d_stats, gs->aux);
   if (!launched("k_g_candidate")) return false;
-  const int nb = flat(gs->nc);  // the features' grid (same summation order)
-  k_g_cand_norm<<<nb, kNT, 0, stream()>>>(g, gpairs(g), gs->aux, rhs, gs->d_stats, gs->partial);
-  if (!launched("k_g_cand_norm")) return false;
+  // the features' kernel and grid: the same summation order
+  int kb = 0;
+  const dim3 cgrid = coarse_grid(g, kb);
+  const int nb = (int)(cgrid.x * cgrid.y * cgrid.z);
+  k_g_coarse<false><<<cgrid, dim3(kGX, kGY), 0, stream()>>>(g, gpairs(g), gs->aux, rhs,
+      gs->d_stats, nullptr, gs->partial, kb);
+  if (!launched("k_g_coarse")) return false;
   k_g_fold_select<<<1, kNT, 0, stream()>>>(gs->partial, nb, gs->d_stats);
   if (!launched("k_g_fold_select")) return false;
   k_g_take<<<flat(padded), 256, 0, stream()>>>(p, gs->aux, padded, gs->d_stats);
