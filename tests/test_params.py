@@ -146,7 +146,8 @@ def test_extension_keys(nusif_lib, tmp_path):
     for k, val in [("solver", "mg-mixed"), ("lid", "1.5"), ("inflow", "1.0"), ("rtol", "1e-8"),
                    ("mg_levels", "5"), ("mg_pre", "3"), ("mg_post", "1"), ("mg_inner", "3"),
                    ("mg_theta", "0.9"), ("mg_omega", "1.2"), ("mg_chunk", "8"),
-                   ("mg_guess", "quadratic"), ("mg_tail", "0"), ("host_fields", "1"),
+                   ("mg_guess", "quadratic"), ("mg_guess", "cubic"), ("mg_tail", "0"),
+                   ("host_fields", "1"),
                    ("mg_probe", "8"), ("fg_arith", "fp64"), ("fg_arith", "df32"),
                    ("arith", "fp64"), ("arith", "df32"), ("fuse_dt", "1")]:
         assert nusif_lib.nusifParameterSet(C.byref(p), k.encode(), val.encode()) == 0
