@@ -250,8 +250,12 @@ __device__ __forceinline__ Tile tile_of(const TcParams &P, int t)
   return r;
 }
 
+// resident blocks per SM the compiler keeps registers for: eight of the
+// 16-channel layers (the full-resolution ones, bound by per-block latency)
+constexpr int conv_min_blocks(int nch) { return nch == 16 ? 8 : 1; }
+
 template <int NCH>  // output channels, a multiple of 16
-__global__ void __launch_bounds__(kThreads, 1) k_conv_tc(const __grid_constant__ CUtensorMap tm_a0,
+__global__ void __launch_bounds__(kThreads, conv_min_blocks(NCH)) k_conv_tc(const __grid_constant__ CUtensorMap tm_a0,
     const __grid_constant__ CUtensorMap tm_a1, const __grid_constant__ CUtensorMap tm_w0,
     const __grid_constant__ CUtensorMap tm_w1, const TcParams P)
 {
@@ -575,7 +579,8 @@ bool launch_tc(const CUtensorMap &a0, const CUtensorMap &a1, const CUtensorMap &
   const size_t stage_bytes = P.stage_bytes;
   // two stages: the fewer the stages, the more blocks an SM holds, and more
   // blocks measured faster than deeper pipelines (the 128^3 forward pass:
-  // 1.77 ms with 2 stages and six blocks of 16 -> 16 layers per SM, 1.81 ms
+  // 1.77 ms with 2 stages and six blocks of 16 -> 16 layers per SM (1.73 ms
+  // with eight, their registers capped for it), 1.81 ms
   // with 4, 2.36 ms with 8, 2.43 ms with 16 stages and two blocks per SM);
   // NUSIF_TC_STAGES overrides the count
   int stages = 2;
